@@ -1,0 +1,73 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own code.
+
+Runs oracle/_ref/qsf_ref (the reference's unmodified header-only implementation,
+compiled by `make -C oracle ref` against the single-rank MPI / FFTW stand-ins) on small
+seeded cases and stores its outputs -- the binary .dat rows written by the reference's
+BufferedOutputs and the raw complex128 wavefunctions -- as compressed .npz files.
+
+Needs the reference checkout (so it runs in the development container only); the
+fixtures it writes are committed and are all the tests need elsewhere.
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.path.join(ROOT, "oracle", "_ref", "qsf_ref")
+
+# name -> (harness case, params, IM dat columns, RE dat columns, grid dims)
+CASES = {
+    "prim2d": ("prim2d", dict(n=16, dx=0.4, nCAP=3, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, p_NS=4, p_SD=3,
+                              p_DT=2, p_CAP=6, seed=7, delta=0.37, F0=0.11), 0, 0, 2),
+    "prim3d": ("prim3d", dict(n=12, dx=0.5, nCAP=2, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, p_NS=4, p_SD=3,
+                              p_DT=2, p_CAP=5, seed=11, delta=0.29, F0=0.07), 0, 0, 3),
+    "c1_vg": ("c1", dict(n=512, dx=0.2, nCAP=51, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=100,
+                         re_dt=0.05, F0=0.05338, omega=0.5, ncycles=2, phase=0.0, box=100, lg=0), 6, 6, 1),
+    "c1_lg": ("c1", dict(n=512, dx=0.2, nCAP=51, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=100,
+                         re_dt=0.05, F0=0.05338, omega=0.5, ncycles=2, phase=0.25, box=100, lg=1), 6, 6, 1),
+    "c2_vg": ("c2", dict(n=48, dx=0.3, nCAP=5, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=40,
+                         re_dt=0.05, F0=0.11936, omega=1.0, ncycles=2, phase=0.0, p_NS=6, p_SD=4, p_DT=3, p_CAP=15,
+                         lg=0), 6, 12, 2),
+    "c3_lg": ("c3", dict(n=16, dx=0.4, nCAP=2, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=20,
+                         re_dt=0.05, F0=0.1688, omega=1.5, ncycles=1, phase=0.0, p_NS=4, p_SD=3, p_DT=2, p_CAP=6,
+                         lg=1), 6, 13, 3),
+}
+
+
+def _read_psi(path, shape):
+    return np.fromfile(path, dtype=np.complex128).reshape(shape)
+
+
+def make(name):
+    case, params, im_cols, re_cols, dim = CASES[name]
+    shape = (int(params["n"]),) * dim
+    with tempfile.TemporaryDirectory() as tmp:
+        args = [REF, case, tmp] + [f"{k}={v}" for k, v in params.items()]
+        subprocess.run(args, check=True, stdout=subprocess.DEVNULL)
+        out = {"params": json.dumps(params), "case": case, "dim": dim}
+        if case.startswith("prim"):
+            for f in ("psi_in", "psi_xre", "psi_xim", "psi_p", "psi_back", "psi_pvg", "psi_norm"):
+                out[f] = _read_psi(os.path.join(tmp, f + ".bin"), shape)
+            out["scalars"] = np.fromfile(os.path.join(tmp, "prim.bin"), dtype=np.float64)
+        else:
+            for f in ("im_psi0", "im_psi", "re_psi0", "re_psi"):
+                out[f] = _read_psi(os.path.join(tmp, f + ".bin"), shape)
+            out["im_rows"] = np.fromfile(os.path.join(tmp, "IM.dat"), dtype=np.float64).reshape(-1, im_cols)
+            out["re_rows"] = np.fromfile(os.path.join(tmp, "RE.dat"), dtype=np.float64).reshape(-1, re_cols)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return out
+
+
+if __name__ == "__main__":
+    if not os.path.exists(REF):
+        sys.exit("build the harness first: make -C oracle ref")
+    for name in (sys.argv[1:] or CASES):
+        o = make(name)
+        print(name, {k: getattr(v, "shape", v) for k, v in o.items() if k != "params"})
