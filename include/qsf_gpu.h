@@ -1,0 +1,187 @@
+/*
+ * qsf_gpu.h -- C ABI of libqsfgpu.so, the GB300 (sm_103a) implementation of QSF's
+ * split-operator time step for the reduced-dimensionality multi-electron TDSE.
+ *
+ * The reference (QSF-physics/QSF) is a header-only C++ library whose grid type
+ * LocalGrid<Hamiltonian, BaseGrid, ...> (include/wf/grid.h) owns the wavefunction and
+ * exposes fourier / evolve / average / current_map / flux / operation / maskRegion to
+ * the propagator (include/propagator.h).  This ABI replaces those members with calls
+ * that run hand-written CUDA kernels on one GPU; every entry point below names the
+ * reference member it stands in for.  The wavefunction lives in device memory owned
+ * by a qsf_grid handle.  All arithmetic is FP64 / complex128.
+ *
+ * Conventions
+ *  - Arrays of complex numbers are interleaved doubles (re, im), C order, last axis
+ *    contiguous -- the reference's layout (grid.h:226-237, cxd = std::complex<double>).
+ *  - Every function returns QSF_OK (0) or a QSF_E* status; nothing aborts and no C++
+ *    exception crosses the ABI (the reference instead aborts via logError,
+ *    basics/logging.h:114).
+ *  - A handle is used from one host thread at a time; calls on one handle are
+ *    ordered on that handle's CUDA stream.
+ */
+#ifndef QSF_GPU_H
+#define QSF_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define QSF_OK 0
+#define QSF_EINVAL 1     /* bad argument or unsupported grid                        */
+#define QSF_ENOMEM 2     /* device allocation failed                                */
+#define QSF_ECUDA 3      /* a CUDA runtime call failed                              */
+#define QSF_ETIMEDOUT 4  /* a bounded wait ran out                                  */
+#define QSF_ENUMERIC 5   /* NaN/Inf or a non-positive norm in a reduction           */
+#define QSF_ESTATE 6     /* call not valid in the handle's current state            */
+#define QSF_EBUSY 7      /* admission refused (no slot or not enough free HBM)      */
+
+/* ------------------------------------------------------ reference enums */
+/* MODE (basics/enums.h:15-21), REP (36-42) */
+#define QSF_MODE_IM 1
+#define QSF_MODE_RE 2
+#define QSF_REP_X 1
+#define QSF_REP_P 2
+/* potentials: ReducedDimInteraction<Eberly|EckhardSacha> (potential.h:97-179),
+ * CoulombInteraction (potential.h:21-82) */
+#define QSF_POT_EBERLY 0
+#define QSF_POT_ECKHARDT_SACHA 1
+#define QSF_POT_COULOMB 2
+#define QSF_POT_NONE 3
+/* gauges: DipoleCoupling<VelocityGauge> couples in P (coupling.h:101-118);
+ * the length gauge couples x.E(t) in X */
+#define QSF_GAUGE_VELOCITY 0
+#define QSF_GAUGE_LENGTH 1
+/* averaged operators: Identity, PotentialEnergy, KineticEnergy (grid.h:7-22) */
+#define QSF_OP_IDENTITY 0
+#define QSF_OP_POTENTIAL 1
+#define QSF_OP_KINETIC 2
+/* flux border types (fluxes/borders.h:39-257) */
+#define QSF_B_BOX 0
+#define QSF_B_S2CAP 1
+#define QSF_B_D2CAP 2
+#define QSF_B_N2S 3
+#define QSF_B_N2D 4
+#define QSF_B_N2D_SYM 5
+#define QSF_B_N2D_ASYM 6
+#define QSF_B_S2D 7
+#define QSF_B_S2D_SYM 8
+#define QSF_B_S2D_ASYM 9
+#define QSF_B_N2T 10
+#define QSF_B_S2T 11
+#define QSF_B_D2T 12
+#define QSF_B_T2CAP 13
+#define QSF_MAX_BORDERS 16
+
+/* ---------------------------------------------------------------- grid */
+/* CAP<CartesianGrid<dim>> (wf/coords.h:14-139, wf/absorbers.h:15-60) together with
+ * the Spin0 Hamiltonian's potential and coupling (hamiltonian.h:8-98). */
+typedef struct qsf_grid_desc {
+  int dim;            /* 1, 2 or 3                                                 */
+  int64_t n[3];       /* nodes per axis; dim >= 2 needs n and dx equal on all axes  */
+  double dx[3];       /* spacing per axis (atomic units)                           */
+  int64_t nCAP;       /* absorber margin in nodes (0: no absorber)                 */
+  int potential;      /* QSF_POT_*                                                 */
+  double Ncharge, Echarge, Nsoft, Esoft;
+  int gauge;          /* QSF_GAUGE_*                                               */
+  int n_fields;       /* fields in the coupling; 0 makes the coupling term exactly 0 */
+  int p_axis_swap;    /* 1: apply the axis-0 coupling to axis 1 and vice versa in P
+                         space, as the reference's transposed P layout does
+                         (grid.h:242-247); ignored for dim == 1                    */
+  int64_t border_nodes[4]; /* p_NS, p_SD, p_DT, p_CAP (borders.h:30-36); 0 = default */
+} qsf_grid_desc;
+
+typedef struct qsf_grid qsf_grid;
+
+/* LocalGrid constructor (grid.h:115-133, 275-293): allocates the device state.
+ * `stream` is a cudaStream_t or NULL (the handle then creates its own stream). */
+int qsf_grid_create(const qsf_grid_desc* desc, void* stream, qsf_grid** out);
+int qsf_grid_destroy(qsf_grid* g);
+/* number of grid points m and the device address of psi (complex128[m]) */
+int qsf_grid_size(const qsf_grid* g, int64_t* m);
+int qsf_psi_device_ptr(qsf_grid* g, void** dptr);
+
+/* copies between host memory (interleaved complex128, m elements) and the grid.
+ * operator[] / save / load of the reference (grid.h:296-297, 789-1153). */
+int qsf_upload(qsf_grid* g, const double* host_psi, int64_t m);
+int qsf_download(qsf_grid* g, double* host_psi, int64_t m);
+int qsf_synchronize(qsf_grid* g);
+
+/* ------------------------------------------------------ granular members */
+/* fourier<R>() (grid.h:369-378): forward DFT (FFTW_FORWARD) to P or backward DFT
+ * to X followed by the 1/m rescale (normalizeAfterTwoFFT, grid.h:363-367).  P space
+ * is kept in natural (untransposed) order. */
+int qsf_fourier(qsf_grid* g, int to_rep);
+/* evolve<M, R>(delta) (grid.h:394-423): psi *= expOp(delta * H_R(r)) and, in X,
+ * the absorber (absorbers.h:40-46).  coupling[3] holds the coupling values per axis
+ * (A in the velocity gauge, E in the length gauge, as _coupling[Axis<d>] returns). */
+int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* coupling3);
+/* average<R, Op>() (grid.h:425-441). */
+int qsf_average(qsf_grid* g, int rep, int op, double* out);
+/* operation<M, R, Normalize>() (grid.h:601-606); returns the norm divided out. */
+int qsf_normalize(qsf_grid* g, double* norm_out);
+/* FLUX<B...> (propagator.h:259-265): current_map (grid.h:467-528), the
+ * velocity-gauge correction curr += A |psi|^2 (propagator.h:249-257; pass A = NULL
+ * in the length gauge) and flux<X, B>() (grid.h:559-573) for each border type. */
+int qsf_flux(qsf_grid* g, const double* A3, int nborders, const int* border_types, int64_t box_size,
+             double* out);
+/* maskRegion() (grid.h:582-597) with CAP::mask (absorbers.h:48-54). */
+int qsf_mask_region(qsf_grid* g, const int* bounded3);
+/* addUsingCoordinateFunction(gaussian(at, delta, x...)) (grid.h:775-778,
+ * wf/preset.h:5-10): psi += gaussian. */
+int qsf_add_gaussian(qsf_grid* g, double at, double delta);
+
+/* ------------------------------------------------------- fused Strang steps */
+/* One call runs `nsteps` consecutive makeStep()s of SplitPropagator with
+ * Split3Base<X,P,X> (propagator.h:311-346, splitting.h:18-27) plus the per-step
+ * computeEach observables (propagator.h:275-300), fused into a few passes per step.
+ *
+ * coupling (host, read during the call):
+ *   velocity gauge: nsteps x 3 doubles, A(t) per axis at the step's P sub-step
+ *                   (also the A of the flux correction, propagator.h:263);
+ *   length gauge:   nsteps x 6 doubles, E(t) per axis at the first and at the
+ *                   second X half-step.
+ *   May be NULL when the grid has no fields.
+ * rows (host, written): nsteps x (3 + nborders) doubles per step, measured on the
+ *   wavefunction right after the step and before any Normalize:
+ *   [ <psi|psi> dV, <psi|V|psi> dV, <psi|T|psi> dV/m (0 unless QSF_OBS_EKIN),
+ *     flux_0 .. flux_{nborders-1} ].
+ * With normalize != 0 the step ends with OPERATION<Normalize> (grid.h:601-606).
+ * In imaginary time with state_accuracy > 0 the run follows shouldContinue()
+ * (propagator.h:304-309): after the first step whose |E_n - E_{n-1}| <= accuracy
+ * exactly one more step runs and the call returns; *steps_done says how many ran.
+ * E_n = epot + ekin; bit 0 of energy_after_normalize divides epot, bit 1 divides ekin
+ * by the step's norm (the observables declared after OPERATION<Normalize>). */
+#define QSF_OBS_NORM 1u
+#define QSF_OBS_EPOT 2u
+#define QSF_OBS_EKIN 4u
+#define QSF_OBS_FLUX 8u
+typedef struct qsf_step_desc {
+  int mode;                 /* QSF_MODE_IM or QSF_MODE_RE                     */
+  double dt;
+  int64_t nsteps;
+  const double* coupling;   /* see above                                       */
+  uint32_t obs;             /* QSF_OBS_* mask                                  */
+  int normalize;            /* OPERATION<Normalize> after each step            */
+  int nborders;             /* flux borders (QSF_OBS_FLUX)                     */
+  int border_types[QSF_MAX_BORDERS];
+  int64_t box_size;         /* BOX<size> parameter                             */
+  double state_accuracy;    /* IM convergence threshold (0: run all nsteps)    */
+  double last_energy;       /* E before the first step of this call            */
+  int energy_after_normalize; /* bit 0: epot, bit 1: ekin seen after Normalize */
+} qsf_step_desc;
+int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done);
+
+/* ------------------------------------------------------------ diagnostics */
+/* last CUDA error text seen by the library (thread-local, never NULL) */
+const char* qsf_last_error(void);
+/* FFT radices chosen for a line of n points (for tests and the autotuner) */
+int qsf_fft_plan_radices(int64_t n, int* radices, int* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QSF_GPU_H */

@@ -1,0 +1,112 @@
+"""ctypes binding of libqsfgpu.so (include/qsf_gpu.h).
+
+The shared library is built in-tree by qsf_gb300/build.py.  There is no fallback:
+if the library is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqsfgpu.so")
+
+QSF_OK = 0
+ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ETIMEDOUT", 5: "ENUMERIC", 6: "ESTATE", 7: "EBUSY"}
+MAX_BORDERS = 16
+
+
+class QsfError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str):
+        super().__init__(f"{where}: QSF_{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int),
+        ("n", ctypes.c_int64 * 3),
+        ("dx", ctypes.c_double * 3),
+        ("nCAP", ctypes.c_int64),
+        ("potential", ctypes.c_int),
+        ("Ncharge", ctypes.c_double),
+        ("Echarge", ctypes.c_double),
+        ("Nsoft", ctypes.c_double),
+        ("Esoft", ctypes.c_double),
+        ("gauge", ctypes.c_int),
+        ("n_fields", ctypes.c_int),
+        ("p_axis_swap", ctypes.c_int),
+        ("border_nodes", ctypes.c_int64 * 4),
+    ]
+
+
+class StepDesc(ctypes.Structure):
+    _fields_ = [
+        ("mode", ctypes.c_int),
+        ("dt", ctypes.c_double),
+        ("nsteps", ctypes.c_int64),
+        ("coupling", ctypes.POINTER(ctypes.c_double)),
+        ("obs", ctypes.c_uint32),
+        ("normalize", ctypes.c_int),
+        ("nborders", ctypes.c_int),
+        ("border_types", ctypes.c_int * MAX_BORDERS),
+        ("box_size", ctypes.c_int64),
+        ("state_accuracy", ctypes.c_double),
+        ("last_energy", ctypes.c_double),
+        ("energy_after_normalize", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """Load libqsfgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m qsf_gb300.build`")
+    L = ctypes.CDLL(LIB_PATH)
+    vp = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    i64 = ctypes.c_int64
+    sig = {
+        "qsf_grid_create": [ctypes.POINTER(GridDesc), vp, ctypes.POINTER(vp)],
+        "qsf_grid_destroy": [vp],
+        "qsf_grid_size": [vp, ctypes.POINTER(i64)],
+        "qsf_psi_device_ptr": [vp, ctypes.POINTER(vp)],
+        "qsf_upload": [vp, dp, i64],
+        "qsf_download": [vp, dp, i64],
+        "qsf_synchronize": [vp],
+        "qsf_fourier": [vp, ctypes.c_int],
+        "qsf_evolve": [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp],
+        "qsf_average": [vp, ctypes.c_int, ctypes.c_int, dp],
+        "qsf_normalize": [vp, dp],
+        "qsf_flux": [vp, dp, ctypes.c_int, ip, i64, dp],
+        "qsf_mask_region": [vp, ip],
+        "qsf_add_gaussian": [vp, ctypes.c_double, ctypes.c_double],
+        "qsf_step": [vp, ctypes.POINTER(StepDesc), dp, ctypes.POINTER(i64)],
+        "qsf_fft_plan_radices": [i64, ip, ip],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    L.qsf_last_error.argtypes = []
+    L.qsf_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def check(rc: int, where: str) -> None:
+    if rc != QSF_OK:
+        raise QsfError(rc, where, lib().qsf_last_error().decode(errors="replace"))
+
+
+def exported_symbols(header: str):
+    """Names of the functions declared in a C header (for ABI completeness checks)."""
+    import re
+    text = open(header).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b(qsf_\w+)\s*\(", text, re.M)))

@@ -1,0 +1,752 @@
+// qsf_api.cu -- host side of libqsfgpu.so: the C ABI declared in include/qsf_gpu.h.
+//
+// Owns the device state of each grid (wavefunction, phase tables, twiddles, flux
+// point lists, reduction scratch), plans the FFTs (radix 16/8/4/2 first, then 3, 5),
+// evaluates the border vectors once per border set, and launches the kernels of
+// qsf_kernels.cuh -- per step through a captured CUDA graph that a device-side step
+// counter makes reusable for every step of a call.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "qsf_gpu.h"
+#include "qsf_borders.h"
+#define QSF_DEFINE_KERNELS
+#include "qsf_kernels.cuh"
+
+using namespace qsf;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define QSF_CU(call)                                                                       \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail(QSF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dev_alloc(T*& p, size_t count) {
+  if (p) cudaFree(p);
+  p = nullptr;
+  if (count == 0) return QSF_OK;
+  if (cudaMalloc((void**)&p, count * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+    return fail(QSF_ENOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed");
+  }
+  return QSF_OK;
+}
+template <class T>
+int dev_reserve(T*& p, size_t& cap, size_t count) {
+  if (count <= cap && p) return QSF_OK;
+  size_t c = std::max(count, cap * 2);
+  int rc = dev_alloc(p, c);
+  cap = rc == QSF_OK ? c : 0;
+  return rc;
+}
+
+// the compile-time radix plan of qsf_fft.cuh, for reporting
+bool plan_radices(int64_t n, std::vector<int>& r) {
+  r.clear();
+  if (n < 2 || n > (1 << 24) || !is_smooth((int)n)) return false;
+  for (int i = 0; i < nstages((int)n); ++i) r.push_back(radix_at((int)n, i));
+  return true;
+}
+
+std::vector<KernelSet>& kernel_table();
+
+// kernel launch geometry
+constexpr int kMaxLine1D = 8192;        // 1D line held in shared memory (complex128)
+constexpr int kMaxTile = 4096;          // points per block in row / axis passes
+constexpr int kMaxSmemOptin = 227 * 1024;
+
+}  // namespace
+
+namespace qsf {
+void add_sizes_p2a(std::vector<KernelSet>& out);
+void add_sizes_p2b(std::vector<KernelSet>& out);
+void add_sizes_r3(std::vector<KernelSet>& out);
+void add_sizes_r5(std::vector<KernelSet>& out);
+const KernelSet* kernels_for(int n) {
+  for (const KernelSet& k : kernel_table())
+    if (k.n == n) return &k;
+  return nullptr;
+}
+}  // namespace qsf
+
+struct qsf_grid {
+  qsf_grid_desc desc{};
+  GridDev G{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  BorderNodes bn;
+  std::vector<double2*> tw_owned;
+  const KernelSet* ks = nullptr;  // kernels for this grid's line length
+  // static tables
+  double2* xs = nullptr;
+  double* V = nullptr;
+  int xs_mode = 0;
+  double xs_delta = 0.0;
+  bool V_ready = false;
+  // per-step tables
+  double2* ptab = nullptr;
+  double2* xdyn = nullptr;
+  int nmax = 0;
+  // reductions
+  double* partials = nullptr;
+  int pmax = 0;
+  double* fpartials = nullptr;
+  size_t fpmax = 0;
+  long long* ctl = nullptr;
+  double* energy = nullptr;
+  double* scale = nullptr;
+  double* rows_dev = nullptr;
+  size_t rows_cap = 0;
+  double* coup_dev = nullptr;
+  size_t coup_cap = 0;
+  // flux structures
+  std::vector<int> fl_borders;
+  int64_t fl_box = -1;
+  bool fl_ready = false;
+  double2* snap = nullptr;
+  long long* snap_idx = nullptr;
+  int* row_ptr = nullptr;
+  FluxPoint* fpts = nullptr;
+  FluxTerm* fterms = nullptr;
+  int nsnap = 0, nfterms = 0, nfpts = 0, nfblk = 1;
+  // launch geometry
+  int row_L = 1;
+  int nrowblk = 1;
+  size_t row_smem = 0;
+  int ax_C[3] = {1, 1, 1};
+  int ax_blocks[3] = {0, 0, 0};
+  size_t ax_smem[3] = {0, 0, 0};
+};
+
+namespace {
+
+// The table of kernel sets, one per supported line length (qsf_sizes_*.cu), with the
+// dynamic shared memory limits raised once.
+std::vector<KernelSet>& kernel_table() {
+  static std::vector<KernelSet> t;
+  return t;
+}
+
+int init_kernel_table() {
+  static bool done = false;
+  if (done) return QSF_OK;
+  std::vector<KernelSet>& t = kernel_table();
+  add_sizes_p2a(t);
+  add_sizes_p2b(t);
+  add_sizes_r3(t);
+  add_sizes_r5(t);
+  auto lim = [](const void* f, int bytes) -> int {
+    if (!f) return QSF_OK;
+    QSF_CU(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return QSF_OK;
+  };
+  for (const KernelSet& k : t) {
+    const int tile = std::min(kMaxSmemOptin, std::max(48 * 1024, k.n * 16 * 4));
+    int rc;
+    if ((rc = lim((const void*)k.row_open, tile)) || (rc = lim((const void*)k.row_close, tile)) ||
+        (rc = lim((const void*)k.axis_fwd, tile)) || (rc = lim((const void*)k.axis_inv, tile)) ||
+        (rc = lim((const void*)k.axis_fpi, tile)) || (rc = lim((const void*)k.axis_ekin, tile)) ||
+        (rc = lim((const void*)k.axis_fft_f, tile)) || (rc = lim((const void*)k.axis_fft_b, tile)) ||
+        (rc = lim((const void*)k.row_fft_f, kMaxSmemOptin)) || (rc = lim((const void*)k.row_fft_b, kMaxSmemOptin)) ||
+        (rc = lim((const void*)k.line_step, kMaxSmemOptin)))
+      return rc;
+  }
+  done = true;
+  return QSF_OK;
+}
+
+int grid_blocks(long long m) {
+  long long b = (m + 255) / 256;
+  return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 16);
+}
+
+int ensure_static(qsf_grid* g, int mode, double delta) {
+  const long long m = g->G.m;
+  if (!g->V) {
+    int rc = dev_alloc(g->V, (size_t)m);
+    if (rc) return rc;
+  }
+  if (!g->xs) {
+    int rc = dev_alloc(g->xs, (size_t)m);
+    if (rc) return rc;
+  }
+  if (g->xs_mode == mode && g->xs_delta == delta && g->V_ready) return QSF_OK;
+  k_build_static<<<grid_blocks(m), 256, 0, g->stream>>>(g->G, mode, delta, g->xs, g->V);
+  QSF_CU(cudaGetLastError());
+  g->xs_mode = mode;
+  g->xs_delta = delta;
+  g->V_ready = true;
+  return QSF_OK;
+}
+
+int ensure_flux(qsf_grid* g, int nb, const int* types, int64_t box) {
+  std::vector<int> want(types, types + nb);
+  if (g->fl_ready && want == g->fl_borders && box == g->fl_box) return QSF_OK;
+  const int D = g->G.dim;
+  const int64_t R = border_reach(g->bn, box);
+  int64_t lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+  for (int d = 0; d < D; ++d) {
+    const int64_t n = g->G.ax[d].n, n2 = g->G.ax[d].n2;
+    lo[d] = std::max<int64_t>(0, n2 - R);
+    hi[d] = std::min<int64_t>(n, n2 + R + 1);
+  }
+  struct Pt {
+    long long p;
+    double w[QSF_MAX_BORDERS][3];
+    unsigned mask;
+  };
+  std::vector<Pt> pts;
+  std::vector<long long> need;
+  const long long m = g->G.m;
+  for (int64_t i0 = lo[0]; i0 < hi[0]; ++i0)
+    for (int64_t i1 = lo[1]; i1 < hi[1]; ++i1)
+      for (int64_t i2 = lo[2]; i2 < hi[2]; ++i2) {
+        const int64_t idx[3] = {i0, i1, i2};
+        int64_t ci[3];
+        long long p = 0;
+        for (int d = 0; d < D; ++d) {
+          ci[d] = idx[d] - g->G.ax[d].n2;
+          p = p * g->G.ax[d].n + idx[d];
+        }
+        Pt pt{};
+        pt.p = p;
+        pt.mask = 0;
+        for (int b = 0; b < nb; ++b) {
+          double w[3];
+          if (!border_vector(types[b], box, D, ci, g->bn, w))
+            return fail(QSF_EINVAL, "border type " + std::to_string(types[b]) + " is not defined for dim " +
+                                        std::to_string(D));
+          bool nz = false;
+          for (int d = 0; d < D; ++d) {
+            pt.w[b][d] = w[d];
+            nz = nz || w[d] != 0.0;
+          }
+          if (nz) pt.mask |= 1u << b;
+        }
+        if (pt.mask) pts.push_back(pt);
+      }
+  // snapshot indices: every point and its valid +-stride neighbours (grid.h:470-472)
+  for (const Pt& pt : pts) {
+    need.push_back(pt.p);
+    for (int d = 0; d < D; ++d) {
+      const long long s = g->G.ax[d].stride;
+      if (pt.p - s > 0 && pt.p + s < m) {
+        need.push_back(pt.p + s);
+        need.push_back(pt.p - s);
+      }
+    }
+  }
+  std::sort(need.begin(), need.end());
+  need.erase(std::unique(need.begin(), need.end()), need.end());
+  auto slot = [&](long long p) { return (int)(std::lower_bound(need.begin(), need.end(), p) - need.begin()); };
+  std::vector<FluxPoint> fps;
+  std::vector<FluxTerm> fts;
+  for (const Pt& pt : pts) {
+    FluxPoint fp{};
+    fp.c = slot(pt.p);
+    for (int d = 0; d < 3; ++d) fp.p[d] = fp.q[d] = -1;
+    for (int d = 0; d < D; ++d) {
+      const long long s = g->G.ax[d].stride;
+      if (pt.p - s > 0 && pt.p + s < m) {
+        fp.p[d] = slot(pt.p + s);
+        fp.q[d] = slot(pt.p - s);
+      }
+    }
+    const int pi = (int)fps.size();
+    fps.push_back(fp);
+    for (int b = 0; b < nb; ++b)
+      if (pt.mask & (1u << b)) {
+        FluxTerm ft{};
+        ft.point = pi;
+        ft.border = b;
+        for (int d = 0; d < 3; ++d) ft.w[d] = d < D ? pt.w[b][d] : 0.0;
+        fts.push_back(ft);
+      }
+  }
+  const long long nlast = g->G.ax[D - 1].n;
+  const long long nrows = m / nlast;
+  std::vector<int> rp((size_t)nrows + 1, 0);
+  for (long long p : need) rp[(size_t)(p / nlast) + 1]++;
+  for (long long r = 0; r < nrows; ++r) rp[(size_t)r + 1] += rp[(size_t)r];
+  int rc;
+  if ((rc = dev_alloc(g->snap, std::max<size_t>(need.size(), 1)))) return rc;
+  if ((rc = dev_alloc(g->snap_idx, std::max<size_t>(need.size(), 1)))) return rc;
+  if ((rc = dev_alloc(g->row_ptr, rp.size()))) return rc;
+  if ((rc = dev_alloc(g->fpts, std::max<size_t>(fps.size(), 1)))) return rc;
+  if ((rc = dev_alloc(g->fterms, std::max<size_t>(fts.size(), 1)))) return rc;
+  if (!need.empty())
+    QSF_CU(cudaMemcpy(g->snap_idx, need.data(), need.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  QSF_CU(cudaMemcpy(g->row_ptr, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (!fps.empty()) QSF_CU(cudaMemcpy(g->fpts, fps.data(), fps.size() * sizeof(FluxPoint), cudaMemcpyHostToDevice));
+  if (!fts.empty()) QSF_CU(cudaMemcpy(g->fterms, fts.data(), fts.size() * sizeof(FluxTerm), cudaMemcpyHostToDevice));
+  g->nsnap = (int)need.size();
+  g->nfpts = (int)fps.size();
+  g->nfterms = (int)fts.size();
+  g->nfblk = (int)std::min<long long>(64, std::max<long long>(1, (g->nfterms + 2047) / 2048));
+  if ((rc = dev_reserve(g->fpartials, g->fpmax, (size_t)g->nfblk * kMaxFluxBorders))) return rc;
+  g->fl_borders = want;
+  g->fl_box = box;
+  g->fl_ready = true;
+  return QSF_OK;
+}
+
+// one step's launches (all read the device step counter)
+int launch_step(qsf_grid* g, const StepDev& S) {
+  const GridDev& G = g->G;
+  const int D = G.dim;
+  cudaStream_t st = g->stream;
+  const KernelSet& K = *g->ks;
+  const int ntab = D * S.nmax * (G.gauge == 1 ? 3 : 1);
+  k_tables<<<std::max(1, std::min(64, (ntab + 255) / 256)), 256, 0, st>>>(G, S);
+  if (D == 1) {
+    K.line_step<<<1, kLineThreads, (size_t)G.ax[0].n * sizeof(double2), st>>>(G, S);
+  } else {
+    K.row_open<<<g->nrowblk, kRowThreads, g->row_smem, st>>>(G, S, g->row_L);
+    if (D == 3) K.axis_fwd<<<g->ax_blocks[1], kRowThreads, g->ax_smem[1], st>>>(G, S, 1, g->ax_C[1]);
+    K.axis_fpi<<<g->ax_blocks[0], kRowThreads, g->ax_smem[0], st>>>(G, S, 0, g->ax_C[0]);
+    if (D == 3) K.axis_inv<<<g->ax_blocks[1], kRowThreads, g->ax_smem[1], st>>>(G, S, 1, g->ax_C[1]);
+    K.row_close<<<g->nrowblk, kRowThreads, g->row_smem, st>>>(G, S, g->row_L);
+    if (S.obs & QSF_OBS_EKIN)
+      for (int ax = 0; ax < D - 1; ++ax)
+        K.axis_ekin<<<g->ax_blocks[ax], kRowThreads, g->ax_smem[ax], st>>>(G, S, ax, g->ax_C[ax]);
+  }
+  k_finalize<<<S.nfterms > 0 ? g->nfblk : 1, 256, 0, st>>>(G, S);
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+}  // namespace
+
+// ======================================================================== C ABI
+extern "C" {
+
+const char* qsf_last_error(void) { return g_err.c_str(); }
+
+int qsf_fft_plan_radices(int64_t n, int* radices, int* count) {
+  std::vector<int> r;
+  if (!plan_radices(n, r)) return fail(QSF_EINVAL, "size " + std::to_string(n) + " is not 2^a 3^b 5^c");
+  if (count) *count = (int)r.size();
+  if (radices)
+    for (size_t i = 0; i < r.size(); ++i) radices[i] = r[i];
+  return QSF_OK;
+}
+
+int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
+  if (!d || !out) return fail(QSF_EINVAL, "null argument");
+  *out = nullptr;
+  if (d->dim < 1 || d->dim > 3) return fail(QSF_EINVAL, "dim must be 1, 2 or 3");
+  for (int k = 0; k < d->dim; ++k)
+    if (d->n[k] < 2 || !(d->dx[k] > 0)) return fail(QSF_EINVAL, "n >= 2 and dx > 0 required on every axis");
+  if (d->dim >= 2)
+    for (int k = 1; k < d->dim; ++k)
+      if (d->n[k] != d->n[0] || d->dx[k] != d->dx[0])
+        return fail(QSF_EINVAL, "dim >= 2 needs the same n and dx on every axis (the reference's P layout)");
+  if (d->dim == 1 && d->n[0] > kMaxLine1D)
+    return fail(QSF_EINVAL, "1D lines longer than " + std::to_string(kMaxLine1D) + " points are not supported");
+  if (d->dim >= 2 && d->n[0] > kMaxTile) return fail(QSF_EINVAL, "axes longer than 4096 points are not supported");
+  if (d->potential < 0 || d->potential > 3) return fail(QSF_EINVAL, "unknown potential");
+  if (d->gauge != QSF_GAUGE_VELOCITY && d->gauge != QSF_GAUGE_LENGTH) return fail(QSF_EINVAL, "unknown gauge");
+  if (int rc = init_kernel_table()) return rc;
+  const KernelSet* ks = kernels_for((int)d->n[0]);
+  if (!ks) return fail(QSF_EINVAL, "grid size " + std::to_string(d->n[0]) + " has no kernels in this build");
+  qsf_grid* g = new qsf_grid();
+  g->desc = *d;
+  g->ks = ks;
+  GridDev& G = g->G;
+  G.dim = d->dim;
+  G.m = 1;
+  for (int k = 0; k < d->dim; ++k) G.m *= d->n[k];
+  if (stream) {
+    g->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete g;
+      return fail(QSF_ECUDA, "cudaStreamCreate failed");
+    }
+    g->own_stream = true;
+  }
+  // coords.h:55-93
+  G.dV = 1.0;
+  long long s = 1;
+  for (int k = d->dim - 1; k >= 0; --k) {
+    G.ax[k].stride = s;
+    s *= d->n[k];
+  }
+  std::map<int64_t, double2*> tws;
+  for (int k = 0; k < d->dim; ++k) {
+    AxisDev& a = G.ax[k];
+    a.n = (int)d->n[k];
+    a.n2 = a.n / 2;
+    a.dx = d->dx[k];
+    G.dV *= d->dx[k];
+    const double L = d->dx[k] * (double)(d->n[k] - 1);
+    a.xmin = -0.5 * L;
+    a.inv_2dx = (1.0 / d->dx[k]) / 2.0;
+    a.dp = 2.0 * M_PI / (double)d->n[k] / d->dx[k];
+    auto it = tws.find(a.n);
+    if (it == tws.end()) {
+      std::vector<double2> h((size_t)a.n);
+      const long double twopi = 6.283185307179586476925286766559005768L;
+      for (int t = 0; t < a.n; ++t) {
+        const long double ang = twopi * (long double)t / (long double)a.n;
+        h[(size_t)t] = make_double2((double)cosl(ang), -(double)sinl(ang));
+      }
+      double2* dptr = nullptr;
+      if (int rc = dev_alloc(dptr, h.size())) {
+        qsf_grid_destroy(g);
+        return rc;
+      }
+      cudaMemcpy(dptr, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice);
+      g->tw_owned.push_back(dptr);
+      tws[a.n] = dptr;
+      a.tw = dptr;
+    } else {
+      a.tw = it->second;
+    }
+  }
+  G.inv_m = 1.0 / (double)G.m;
+  G.dVm = G.dV * G.inv_m;
+  G.nCAP = d->nCAP;
+  if (d->nCAP > 0) {
+    const double t = 3.0 / (double)d->nCAP;
+    G.eta = t * (t * (t * t));
+  }
+  G.pot = d->potential;
+  G.NEcharge = d->Ncharge * d->Echarge;
+  G.EEcharge = d->Echarge * d->Echarge;
+  G.Nsoft = d->Nsoft;
+  G.Esoft = d->Esoft;
+  G.gauge = d->gauge;
+  G.n_fields = d->n_fields;
+  G.p_swap = d->p_axis_swap ? 1 : 0;
+  if (d->border_nodes[0] > 0) g->bn.NS = d->border_nodes[0];
+  if (d->border_nodes[1] > 0) g->bn.SD = d->border_nodes[1];
+  if (d->border_nodes[2] > 0) g->bn.DT = d->border_nodes[2];
+  if (d->border_nodes[3] > 0) g->bn.CAP = d->border_nodes[3];
+  int rc;
+  if ((rc = dev_alloc(G.psi, (size_t)G.m))) { qsf_grid_destroy(g); return rc; }
+  cudaMemsetAsync(G.psi, 0, (size_t)G.m * sizeof(double2), g->stream);
+  // launch geometry
+  const int D = d->dim;
+  const int nlast = G.ax[D - 1].n;
+  const long long nrows = G.m / nlast;
+  if (D >= 2) {
+    g->row_L = (int)std::max<long long>(1, std::min<long long>(nrows, kMaxTile / nlast));
+    g->nrowblk = (int)((nrows + g->row_L - 1) / g->row_L);
+    g->row_smem = (size_t)g->row_L * nlast * sizeof(double2);
+    for (int ax = 0; ax < D - 1; ++ax) {
+      const AxisDev& a = G.ax[ax];
+      const long long inner = a.stride;
+      int C = (int)std::max<long long>(1, std::min<long long>({64, kMaxTile / a.n, inner}));
+      g->ax_C[ax] = C;
+      const long long outer = G.m / ((long long)a.n * inner);
+      g->ax_blocks[ax] = (int)(outer * ((inner + C - 1) / C));
+      g->ax_smem[ax] = (size_t)a.n * C * sizeof(double2);
+    }
+  } else {
+    g->nrowblk = 1;
+  }
+  g->nmax = 0;
+  for (int k = 0; k < D; ++k) g->nmax = std::max(g->nmax, G.ax[k].n);
+  g->pmax = std::max({g->nrowblk, g->ax_blocks[0], g->ax_blocks[1], g->ax_blocks[2], 256});
+  if ((rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)2 * D * g->nmax)) ||
+      (rc = dev_alloc(g->partials, (size_t)5 * g->pmax)) || (rc = dev_alloc(g->ctl, 8)) ||
+      (rc = dev_alloc(g->energy, 2)) || (rc = dev_alloc(g->scale, 2))) {
+    qsf_grid_destroy(g);
+    return rc;
+  }
+  cudaMemsetAsync(g->partials, 0, sizeof(double) * 5 * g->pmax, g->stream);
+  if (cudaStreamSynchronize(g->stream) != cudaSuccess) {
+    qsf_grid_destroy(g);
+    return fail(QSF_ECUDA, "grid initialisation failed");
+  }
+  *out = g;
+  return QSF_OK;
+}
+
+int qsf_grid_destroy(qsf_grid* g) {
+  if (!g) return QSF_OK;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  auto fr = [](void* p) {
+    if (p) cudaFree(p);
+  };
+  fr(g->G.psi);
+  for (double2* t : g->tw_owned) fr(t);
+  fr(g->xs);
+  fr(g->V);
+  fr(g->ptab);
+  fr(g->xdyn);
+  fr(g->partials);
+  fr(g->fpartials);
+  fr(g->ctl);
+  fr(g->energy);
+  fr(g->scale);
+  fr(g->rows_dev);
+  fr(g->coup_dev);
+  fr(g->snap);
+  fr(g->snap_idx);
+  fr(g->row_ptr);
+  fr(g->fpts);
+  fr(g->fterms);
+  if (g->own_stream) cudaStreamDestroy(g->stream);
+  delete g;
+  return QSF_OK;
+}
+
+int qsf_grid_size(const qsf_grid* g, int64_t* m) {
+  if (!g || !m) return fail(QSF_EINVAL, "null argument");
+  *m = g->G.m;
+  return QSF_OK;
+}
+
+int qsf_psi_device_ptr(qsf_grid* g, void** dptr) {
+  if (!g || !dptr) return fail(QSF_EINVAL, "null argument");
+  *dptr = g->G.psi;
+  return QSF_OK;
+}
+
+int qsf_upload(qsf_grid* g, const double* host, int64_t m) {
+  if (!g || !host) return fail(QSF_EINVAL, "null argument");
+  if (m != g->G.m) return fail(QSF_EINVAL, "size mismatch");
+  QSF_CU(cudaMemcpyAsync(g->G.psi, host, (size_t)m * sizeof(double2), cudaMemcpyHostToDevice, g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  return QSF_OK;
+}
+
+int qsf_download(qsf_grid* g, double* host, int64_t m) {
+  if (!g || !host) return fail(QSF_EINVAL, "null argument");
+  if (m != g->G.m) return fail(QSF_EINVAL, "size mismatch");
+  QSF_CU(cudaMemcpyAsync(host, g->G.psi, (size_t)m * sizeof(double2), cudaMemcpyDeviceToHost, g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  return QSF_OK;
+}
+
+int qsf_synchronize(qsf_grid* g) {
+  if (!g) return fail(QSF_EINVAL, "null argument");
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  return QSF_OK;
+}
+
+int qsf_fourier(qsf_grid* g, int to_rep) {
+  if (!g || (to_rep != QSF_REP_X && to_rep != QSF_REP_P)) return fail(QSF_EINVAL, "bad argument");
+  const GridDev& G = g->G;
+  const KernelSet& K = *g->ks;
+  const int D = G.dim;
+  const bool fwd = to_rep == QSF_REP_P;
+  const double last_scale = fwd ? 1.0 : G.inv_m;
+  cudaStream_t st = g->stream;
+  for (int ax = D - 1; ax >= 0; --ax) {
+    const double sc = ax == 0 ? last_scale : 1.0;
+    if (ax == D - 1) {
+      // rows of the last axis with up to 16 * kLineThreads points per block
+      const int n = G.ax[ax].n;
+      const long long nrows = G.m / n;
+      const int L = (int)std::max<long long>(1, std::min<long long>(nrows, (16LL * kLineThreads) / n));
+      const int blocks = (int)((nrows + L - 1) / L);
+      const size_t smem = (size_t)L * n * sizeof(double2);
+      if (fwd) K.row_fft_f<<<blocks, kLineThreads, smem, st>>>(G, L, sc);
+      else K.row_fft_b<<<blocks, kLineThreads, smem, st>>>(G, L, sc);
+    } else {
+      if (fwd) K.axis_fft_f<<<g->ax_blocks[ax], kRowThreads, g->ax_smem[ax], st>>>(G, ax, g->ax_C[ax], sc);
+      else K.axis_fft_b<<<g->ax_blocks[ax], kRowThreads, g->ax_smem[ax], st>>>(G, ax, g->ax_C[ax], sc);
+    }
+  }
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* c3) {
+  if (!g || (mode != 1 && mode != 2) || (rep != 1 && rep != 2)) return fail(QSF_EINVAL, "bad argument");
+  const double c0 = c3 ? c3[0] : 0.0, c1 = c3 ? c3[1] : 0.0, c2 = c3 ? c3[2] : 0.0;
+  k_evolve<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, mode, rep, delta, c0, c1, c2);
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+int qsf_average(qsf_grid* g, int rep, int op, double* out) {
+  if (!g || !out || (rep != 1 && rep != 2) || op < 0 || op > 2) return fail(QSF_EINVAL, "bad argument");
+  const int nb = std::min(256, grid_blocks(g->G.m));
+  k_average<<<nb, 256, 0, g->stream>>>(g->G, rep, op, g->partials);
+  const double vol = rep == QSF_REP_X ? g->G.dV : g->G.dVm;
+  k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nb, vol, g->energy + 1);
+  QSF_CU(cudaGetLastError());
+  QSF_CU(cudaMemcpyAsync(out, g->energy + 1, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  return QSF_OK;
+}
+
+int qsf_normalize(qsf_grid* g, double* norm_out) {
+  double nrm = 0.0;
+  if (int rc = qsf_average(g, QSF_REP_X, QSF_OP_IDENTITY, &nrm)) return rc;
+  if (!(nrm > 0.0)) return fail(QSF_ENUMERIC, "norm is not positive");
+  const double s = std::sqrt(1.0 / nrm);
+  QSF_CU(cudaMemcpyAsync(g->scale + 1, &s, sizeof(double), cudaMemcpyHostToDevice, g->stream));
+  k_scale<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G.psi, g->G.m, g->scale + 1);
+  QSF_CU(cudaGetLastError());
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  if (norm_out) *norm_out = nrm;
+  return QSF_OK;
+}
+
+int qsf_flux(qsf_grid* g, const double* A3, int nb, const int* types, int64_t box, double* out) {
+  if (!g || !out || nb < 0 || nb > QSF_MAX_BORDERS || (nb && !types)) return fail(QSF_EINVAL, "bad argument");
+  if (nb == 0) return QSF_OK;
+  if (int rc = ensure_flux(g, nb, types, box)) return rc;
+  std::vector<double> res((size_t)nb, 0.0);
+  if (g->nfterms > 0) {
+    k_gather<<<std::max(1, std::min(1024, (g->nsnap + 255) / 256)), 256, 0, g->stream>>>(g->G.psi, g->snap_idx,
+                                                                                         g->nsnap, g->snap);
+    k_flux<<<g->nfblk, 256, 0, g->stream>>>(g->G, g->fpts, g->fterms, g->nfterms, g->snap, A3 ? A3[0] : 0.0,
+                                            A3 ? A3[1] : 0.0, A3 ? A3[2] : 0.0, A3 ? 1 : 0, nb, g->fpartials);
+    QSF_CU(cudaGetLastError());
+    std::vector<double> part((size_t)g->nfblk * kMaxFluxBorders);
+    QSF_CU(cudaMemcpyAsync(part.data(), g->fpartials, part.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                           g->stream));
+    QSF_CU(cudaStreamSynchronize(g->stream));
+    for (int k = 0; k < g->nfblk; ++k)
+      for (int b = 0; b < nb; ++b) res[(size_t)b] += part[(size_t)k * kMaxFluxBorders + b];
+  }
+  for (int b = 0; b < nb; ++b) out[b] = res[(size_t)b] * g->G.dV / g->G.ax[0].dx;
+  return QSF_OK;
+}
+
+int qsf_mask_region(qsf_grid* g, const int* b3) {
+  if (!g || !b3) return fail(QSF_EINVAL, "null argument");
+  k_mask<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, b3[0], g->G.dim > 1 ? b3[1] : 1, g->G.dim > 2 ? b3[2] : 1);
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+int qsf_add_gaussian(qsf_grid* g, double at, double delta) {
+  if (!g || !(delta > 0)) return fail(QSF_EINVAL, "bad argument");
+  k_add_gaussian<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, at, delta);
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done) {
+  if (!g || !d) return fail(QSF_EINVAL, "null argument");
+  if (d->mode != QSF_MODE_IM && d->mode != QSF_MODE_RE) return fail(QSF_EINVAL, "mode must be IM or RE");
+  if (d->nsteps < 0) return fail(QSF_EINVAL, "nsteps < 0");
+  if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
+  if (steps_done) *steps_done = 0;
+  if (d->nsteps == 0) return QSF_OK;
+  const GridDev& G = g->G;
+  const int D = G.dim;
+  int rc;
+  if ((rc = ensure_static(g, d->mode, d->dt * 0.5))) return rc;
+  const bool want_flux = (d->obs & QSF_OBS_FLUX) && d->nborders > 0;
+  if (want_flux && (rc = ensure_flux(g, d->nborders, d->border_types, d->box_size))) return rc;
+  const int nb = want_flux ? d->nborders : 0;
+  const int ncol = 3 + nb;
+  const int cstride = G.gauge == QSF_GAUGE_LENGTH ? 6 : 3;
+  if ((rc = dev_reserve(g->rows_dev, g->rows_cap, (size_t)d->nsteps * ncol))) return rc;
+  const double* coup = nullptr;
+  if (d->coupling) {
+    if ((rc = dev_reserve(g->coup_dev, g->coup_cap, (size_t)d->nsteps * cstride))) return rc;
+    QSF_CU(cudaMemcpyAsync(g->coup_dev, d->coupling, (size_t)d->nsteps * cstride * sizeof(double),
+                           cudaMemcpyHostToDevice, g->stream));
+    coup = g->coup_dev;
+  }
+  long long ctl_h[8] = {0, (long long)d->nsteps, 0, 0, 0, 0, 0, 0};
+  double en_h[2] = {d->last_energy, 0.0};
+  double sc_h[2] = {1.0, 1.0};
+  QSF_CU(cudaMemcpyAsync(g->ctl, ctl_h, sizeof(ctl_h), cudaMemcpyHostToDevice, g->stream));
+  QSF_CU(cudaMemcpyAsync(g->energy, en_h, sizeof(en_h), cudaMemcpyHostToDevice, g->stream));
+  QSF_CU(cudaMemcpyAsync(g->scale, sc_h, sizeof(sc_h), cudaMemcpyHostToDevice, g->stream));
+
+  StepDev S{};
+  S.mode = d->mode;
+  S.dt = d->dt;
+  S.nsteps = d->nsteps;
+  S.coupling = coup;
+  S.coup_stride = cstride;
+  S.xs = g->xs;
+  S.V = g->V;
+  S.ptab = g->ptab;
+  S.xdyn = g->xdyn;
+  S.nmax = g->nmax;
+  S.partials = g->partials;
+  S.pmax = g->pmax;
+  S.nrowblk = g->nrowblk;
+  for (int ax = 0; ax < 3; ++ax) S.naxblk[ax] = g->ax_blocks[ax];
+  S.obs = d->obs | QSF_OBS_NORM;
+  if (nb == 0) S.obs &= ~QSF_OBS_FLUX;
+  S.normalize = d->normalize;
+  S.energy_after_normalize = d->energy_after_normalize;
+  S.state_accuracy = d->mode == QSF_MODE_IM ? d->state_accuracy : 0.0;
+  S.nborders = nb;
+  if (want_flux) {
+    S.snap = g->snap;
+    S.row_ptr = g->row_ptr;
+    S.snap_idx = g->snap_idx;
+    S.fpts = g->fpts;
+    S.fterms = g->fterms;
+    S.nfterms = g->nfterms;
+    S.fpartials = g->fpartials;
+  }
+  if (!S.fpartials) {
+    if ((rc = dev_reserve(g->fpartials, g->fpmax, (size_t)kMaxFluxBorders))) return rc;
+    S.fpartials = g->fpartials;
+  }
+  S.ctl = g->ctl;
+  S.energy_state = g->energy;
+  S.rows = g->rows_dev;
+  S.scale = g->scale;
+
+  if (d->nsteps < 4) {
+    for (int64_t k = 0; k < d->nsteps; ++k)
+      if ((rc = launch_step(g, S))) return rc;
+  } else {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    QSF_CU(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+    rc = launch_step(g, S);
+    cudaError_t ce = cudaStreamEndCapture(g->stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    for (int64_t k = 0; k < d->nsteps; ++k) {
+      ce = cudaGraphLaunch(exec, g->stream);
+      if (ce != cudaSuccess) {
+        cudaGraphExecDestroy(exec);
+        return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
+      }
+    }
+    cudaGraphExecDestroy(exec);
+  }
+  if (d->normalize) {
+    k_scale<<<grid_blocks(G.m), 256, 0, g->stream>>>(G.psi, G.m, g->scale);
+    QSF_CU(cudaGetLastError());
+  }
+  QSF_CU(cudaMemcpyAsync(ctl_h, g->ctl, sizeof(ctl_h), cudaMemcpyDeviceToHost, g->stream));
+  if (rows)
+    QSF_CU(cudaMemcpyAsync(rows, g->rows_dev, (size_t)d->nsteps * ncol * sizeof(double), cudaMemcpyDeviceToHost,
+                           g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  if (steps_done) *steps_done = ctl_h[2];
+  if (ctl_h[4]) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a step's reductions");
+  return QSF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,17 @@
+// Kernel instantiations for grid sizes 3 * 2^k (12 .. 6144).
+#include <vector>
+#include "qsf_kernels.cuh"
+namespace qsf {
+void add_sizes_r3(std::vector<KernelSet>& out) {
+  out.push_back(make_kernel_set<12>());
+  out.push_back(make_kernel_set<24>());
+  out.push_back(make_kernel_set<48>());
+  out.push_back(make_kernel_set<96>());
+  out.push_back(make_kernel_set<192>());
+  out.push_back(make_kernel_set<384>());
+  out.push_back(make_kernel_set<768>());
+  out.push_back(make_kernel_set<1536>());
+  out.push_back(make_kernel_set<3072>());
+  out.push_back(make_kernel_set<6144>());
+}
+}  // namespace qsf

@@ -1,0 +1,168 @@
+"""Python mirror of the reference's grid / wavefunction members over the C ABI.
+
+``Grid`` stands for LocalGrid<Spin0<CAP<CartesianGrid<dim>>, V, C>, ...>
+(include/wf/grid.h:63-1301): the wavefunction lives on the GPU and every member
+runs CUDA kernels of libqsfgpu.so.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+
+from ._lib import GridDesc, StepDesc, MAX_BORDERS, check, lib
+
+MODE_IM, MODE_RE = 1, 2
+REP_X, REP_P = 1, 2
+OP_IDENTITY, OP_POTENTIAL, OP_KINETIC = 0, 1, 2
+POT_EBERLY, POT_ECKHARDT_SACHA, POT_COULOMB, POT_NONE = 0, 1, 2, 3
+OBS_NORM, OBS_EPOT, OBS_EKIN, OBS_FLUX = 1, 2, 4, 8
+
+BORDERS = {
+    "BOX": 0, "S2CAP": 1, "D2CAP": 2, "N2S": 3, "N2D": 4, "N2D_SYM": 5, "N2D_ASYM": 6,
+    "S2D": 7, "S2D_SYM": 8, "S2D_ASYM": 9, "N2T": 10, "S2T": 11, "D2T": 12, "T2CAP": 13,
+}
+# computations.h:68-70
+ZOA_FLUX_3D = ["N2S", "N2D", "N2T", "S2D", "S2T", "S2CAP", "D2CAP", "T2CAP"]
+ZOA_FLUX_2D_SIMPLE = ["N2S", "N2D", "S2D", "S2CAP", "D2CAP"]
+ZOA_FLUX_2D = ["N2S", "N2D_SYM", "N2D_ASYM", "S2D_SYM", "S2D_ASYM", "S2CAP", "D2CAP"]
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Grid:
+    def __init__(self, dim: int, n, dx, nCAP: int = 0, potential: int = POT_EBERLY, Ncharge: float = 1.0,
+                 Echarge: float = -1.0, Nsoft: float = 1.0, Esoft: float = 1.0, gauge: int = 0,
+                 n_fields: int = 0, p_axis_swap: Optional[bool] = None, border_nodes=(25, 14, 10, 40),
+                 stream: Optional[int] = None):
+        n = [int(n)] * dim if np.isscalar(n) else [int(v) for v in n]
+        dx = [float(dx)] * dim if np.isscalar(dx) else [float(v) for v in dx]
+        d = GridDesc()
+        d.dim = dim
+        for k in range(dim):
+            d.n[k] = n[k]
+            d.dx[k] = dx[k]
+        d.nCAP = int(nCAP)
+        d.potential = potential
+        d.Ncharge, d.Echarge, d.Nsoft, d.Esoft = Ncharge, Echarge, Nsoft, Esoft
+        d.gauge = gauge
+        d.n_fields = n_fields
+        d.p_axis_swap = int(dim >= 2 if p_axis_swap is None else p_axis_swap)
+        for k in range(4):
+            d.border_nodes[k] = int(border_nodes[k])
+        self.desc = d
+        self.dim, self.n, self.dx = dim, n, dx
+        self.shape = tuple(n)
+        self.m = int(np.prod(n))
+        self.gauge = gauge
+        h = ctypes.c_void_p()
+        check(lib().qsf_grid_create(ctypes.byref(d), ctypes.c_void_p(stream or 0), ctypes.byref(h)),
+              "qsf_grid_create")
+        self._h = h
+
+    # ------------------------------------------------------------ lifetime
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().qsf_grid_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        check(lib().qsf_psi_device_ptr(self._h, ctypes.byref(p)), "qsf_psi_device_ptr")
+        return int(p.value)
+
+    # ------------------------------------------------------------ data
+    def upload(self, psi: np.ndarray) -> None:
+        a = np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1)
+        assert a.size == self.m
+        check(lib().qsf_upload(self._h, _dp(a.view(np.float64)), self.m), "qsf_upload")
+
+    def download(self) -> np.ndarray:
+        a = np.empty(self.m, dtype=np.complex128)
+        check(lib().qsf_download(self._h, _dp(a.view(np.float64)), self.m), "qsf_download")
+        return a.reshape(self.shape)
+
+    def synchronize(self) -> None:
+        check(lib().qsf_synchronize(self._h), "qsf_synchronize")
+
+    # ------------------------------------------------------------ members
+    def fourier(self, to_rep: int) -> None:
+        check(lib().qsf_fourier(self._h, to_rep), "qsf_fourier")
+
+    def evolve(self, mode: int, rep: int, delta: float, coupling: Optional[Sequence[float]] = None) -> None:
+        c = (ctypes.c_double * 3)(*(list(coupling) + [0.0] * (3 - len(coupling)))) if coupling is not None else None
+        check(lib().qsf_evolve(self._h, mode, rep, delta, c), "qsf_evolve")
+
+    def average(self, rep: int, op: int) -> float:
+        out = ctypes.c_double()
+        check(lib().qsf_average(self._h, rep, op, ctypes.byref(out)), "qsf_average")
+        return out.value
+
+    def normalize(self) -> float:
+        out = ctypes.c_double()
+        check(lib().qsf_normalize(self._h, ctypes.byref(out)), "qsf_normalize")
+        return out.value
+
+    def flux(self, borders: Sequence[str], box_size: int = 0, A: Optional[Sequence[float]] = None):
+        nb = len(borders)
+        types = (ctypes.c_int * max(nb, 1))(*[BORDERS[b] for b in borders])
+        out = (ctypes.c_double * max(nb, 1))()
+        a = (ctypes.c_double * 3)(*(list(A) + [0.0] * (3 - len(A)))) if A is not None else None
+        check(lib().qsf_flux(self._h, a, nb, types, int(box_size), out), "qsf_flux")
+        return list(out)[:nb]
+
+    def mask_region(self, bounded: Sequence[int]) -> None:
+        b = (ctypes.c_int * 3)(*(list(bounded) + [1] * (3 - len(bounded))))
+        check(lib().qsf_mask_region(self._h, b), "qsf_mask_region")
+
+    def add_gaussian(self, at: float = 0.0, delta: float = 1.0) -> None:
+        check(lib().qsf_add_gaussian(self._h, at, delta), "qsf_add_gaussian")
+
+    # ------------------------------------------------------------ fused steps
+    def step(self, mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None, obs: int = OBS_NORM,
+             normalize: bool = False, borders: Sequence[str] = (), box_size: int = 0,
+             state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0):
+        """Run nsteps fused Strang steps; returns (rows [nsteps, 3 + nb], steps_done)."""
+        d = StepDesc()
+        d.mode = mode
+        d.dt = dt
+        d.nsteps = int(nsteps)
+        cp = None
+        if coupling is not None:
+            cp = np.ascontiguousarray(coupling, dtype=np.float64)
+            d.coupling = _dp(cp)
+        d.obs = obs | (OBS_FLUX if borders else 0)
+        d.normalize = int(bool(normalize))
+        d.nborders = len(borders)
+        assert len(borders) <= MAX_BORDERS
+        for i, b in enumerate(borders):
+            d.border_types[i] = BORDERS[b]
+        d.box_size = int(box_size)
+        d.state_accuracy = state_accuracy
+        d.last_energy = last_energy
+        d.energy_after_normalize = int(energy_after_normalize)
+        rows = np.zeros((max(int(nsteps), 1), 3 + len(borders)), dtype=np.float64)
+        done = ctypes.c_int64()
+        check(lib().qsf_step(self._h, ctypes.byref(d), _dp(rows), ctypes.byref(done)), "qsf_step")
+        del cp
+        return rows[: int(nsteps)], int(done.value)
+
+
+def fft_radices(n: int):
+    r = (ctypes.c_int * 32)()
+    c = ctypes.c_int()
+    check(lib().qsf_fft_plan_radices(int(n), r, ctypes.byref(c)), "qsf_fft_plan_radices")
+    return list(r)[: c.value]

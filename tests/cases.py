@@ -87,3 +87,42 @@ def oracle_re(p, dim, psi0):
 
 def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+# ---------------------------------------------------------------- GPU side
+def gpu_grid(p, dim, gauge, n_fields):
+    import qsf_gb300 as Q
+    nodes = (int(p.get("p_NS", 25)), int(p.get("p_SD", 14)), int(p.get("p_DT", 10)), int(p.get("p_CAP", 40)))
+    return Q.Grid(dim, int(p["n"]), p["dx"], nCAP=int(p["nCAP"]), potential=Q.POT_EBERLY, Ncharge=p["Ncharge"],
+                  Echarge=p["Echarge"], Nsoft=p["Nsoft"], Esoft=p["Esoft"], gauge=gauge, n_fields=n_fields,
+                  border_nodes=nodes)
+
+
+def gpu_pulse(p):
+    import qsf_gb300 as Q
+    return Q.Pulse(field=p["F0"], omega=p["omega"], ncycles=p["ncycles"], phase_in_pi_units=p.get("phase", 0.0),
+                   delay_in_cycles=p.get("delay", 0.0), shape=Q.PULSE_SIN2_SIN)
+
+
+def gpu_im(p, dim, psi0=None):
+    import qsf_gb300 as Q
+    g = gpu_grid(p, dim, Q.GAUGE_VELOCITY, 0)
+    if psi0 is None:
+        g.add_gaussian(0.0, 1.0)
+    else:
+        g.upload(psi0)
+    prop = Q.SplitPropagator(Q.MODE_IM, p["im_dt"], int(p["im_steps"]), g, Q.Coupling(Q.GAUGE_VELOCITY),
+                             IM_OUTPUTS)
+    rows = prop.run()
+    return g, rows
+
+
+def gpu_re(p, dim, psi0):
+    import qsf_gb300 as Q
+    gauge = Q.GAUGE_LENGTH if p.get("lg", 0) else Q.GAUGE_VELOCITY
+    c = Q.Coupling(gauge, [Q.Field(field_axis(dim), [gpu_pulse(p)])])
+    g = gpu_grid(p, dim, gauge, 1)
+    g.upload(psi0)
+    prop = Q.SplitPropagator(Q.MODE_RE, p["re_dt"], 0, g, c, re_outputs(dim, int(p.get("box", 0))))
+    rows = prop.run()
+    return g, rows

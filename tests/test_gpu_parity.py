@@ -1,0 +1,126 @@
+"""GPU path (libqsfgpu.so through the C ABI) against the reference's own outputs.
+
+Golden fixtures come from the reference's header-only implementation itself
+(tests/golden/make_golden.py); the CPU oracle is pinned to the same fixtures in
+test_oracle_golden.py.  Tolerances: 1e-12 relative for single primitives, and the
+spec bar for full runs -- relative L2 of psi <= 1e-10 after the run, norm /
+energies / border fluxes within 1e-9.
+"""
+import numpy as np
+import pytest
+
+from tests import cases as C
+
+pytestmark = pytest.mark.gpu
+
+PRIM_TOL = 1e-12
+PSI_TOL = 1e-10
+OBS_TOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def Q():
+    import qsf_gb300
+    return qsf_gb300
+
+
+@pytest.mark.parametrize("name", ["prim2d", "prim3d"])
+def test_primitives(Q, name):
+    z = C.load(name)
+    p, dim = z["params"], int(z["dim"])
+    s = z["scalars"]
+    lg = C.gpu_grid(p, dim, Q.GAUGE_LENGTH, 1)
+    vg = C.gpu_grid(p, dim, Q.GAUGE_VELOCITY, 1)
+    lg.upload(z["psi_in"])
+    vg.upload(z["psi_in"])
+    assert lg.average(Q.REP_X, Q.OP_IDENTITY) == pytest.approx(s[0], rel=PRIM_TOL)
+    assert lg.average(Q.REP_X, Q.OP_POTENTIAL) == pytest.approx(s[1], rel=PRIM_TOL)
+    names = ["S2CAP", "D2CAP", "N2S", "N2D", "S2D"]
+    names += ["N2D_SYM", "N2D_ASYM", "S2D_SYM", "S2D_ASYM"] if dim == 2 else ["N2T", "S2T", "D2T", "T2CAP"]
+    fl = lg.flux(["BOX"], 3) + lg.flux(names)
+    np.testing.assert_allclose(fl, s[2:2 + len(fl)], rtol=PRIM_TOL, atol=1e-14)
+    E = [p["F0"]] * 3
+    lg.evolve(Q.MODE_RE, Q.REP_X, p["delta"], E)
+    assert C.rel_l2(lg.download(), z["psi_xre"]) < PRIM_TOL
+    lg.evolve(Q.MODE_IM, Q.REP_X, p["delta"], E)
+    assert C.rel_l2(lg.download(), z["psi_xim"]) < PRIM_TOL
+    lg.fourier(Q.REP_P)
+    assert C.rel_l2(np.swapaxes(lg.download(), 0, 1), z["psi_p"]) < PRIM_TOL
+    assert lg.average(Q.REP_P, Q.OP_KINETIC) == pytest.approx(s[-1], rel=PRIM_TOL)
+    lg.fourier(Q.REP_X)
+    assert C.rel_l2(lg.download(), z["psi_back"]) < PRIM_TOL
+    vg.fourier(Q.REP_P)
+    A = [-p["F0"]] * 3
+    vg.evolve(Q.MODE_RE, Q.REP_P, p["delta"], A)
+    vg.evolve(Q.MODE_IM, Q.REP_P, p["delta"] * 0.25, A)
+    vg.fourier(Q.REP_X)
+    assert C.rel_l2(vg.download(), z["psi_pvg"]) < PRIM_TOL
+    vg.normalize()
+    assert C.rel_l2(vg.download(), z["psi_norm"]) < PRIM_TOL
+
+
+@pytest.mark.parametrize("name", ["c1_vg", "c1_lg", "c2_vg", "c3_lg"])
+def test_full_runs(Q, name):
+    z = C.load(name)
+    p, dim = z["params"], int(z["dim"])
+    g, rows = C.gpu_im(p, dim)
+    got = np.array([C.im_dat_row(r) for r in rows])
+    ref = z["im_rows"]
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got, ref, rtol=OBS_TOL, atol=OBS_TOL)
+    assert C.rel_l2(g.download(), z["im_psi"]) < PSI_TOL
+    g2, rows2 = C.gpu_re(p, dim, z["re_psi0"])
+    nb = len(C.re_borders(dim))
+    got = np.array([C.re_dat_row(r, nb) for r in rows2])
+    ref = z["re_rows"]
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got[:, :2], ref[:, :2], rtol=1e-14, atol=0)  # step and time are exact
+    np.testing.assert_allclose(got[:, 2:], ref[:, 2:], rtol=OBS_TOL, atol=OBS_TOL)
+    assert C.rel_l2(g2.download(), z["re_psi"]) < PSI_TOL
+
+
+@pytest.mark.parametrize("n", [8, 12, 16, 20, 48, 64, 96, 160, 256, 384, 512, 640, 768, 1024, 2048, 4096, 8192])
+def test_fft_1d_matches_numpy(Q, n):
+    rng = np.random.default_rng(n)
+    psi = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    g = Q.Grid(1, n, 0.1)
+    g.upload(psi)
+    g.fourier(Q.REP_P)
+    ref = np.fft.fft(psi)
+    assert C.rel_l2(g.download(), ref) < 1e-14 * max(1.0, np.log2(n))
+    g.fourier(Q.REP_X)
+    assert C.rel_l2(g.download(), psi) < 1e-14 * max(1.0, np.log2(n))
+
+
+@pytest.mark.parametrize("dim,n", [(2, 64), (2, 384), (2, 2048), (3, 16), (3, 48), (3, 256)])
+def test_fft_nd_matches_numpy(Q, dim, n):
+    rng = np.random.default_rng(7 * n + dim)
+    shape = (n,) * dim
+    psi = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    g = Q.Grid(dim, n, 0.1)
+    g.upload(psi)
+    g.fourier(Q.REP_P)
+    assert C.rel_l2(g.download(), np.fft.fftn(psi)) < 2e-14 * np.log2(n ** dim)
+    g.fourier(Q.REP_X)
+    assert C.rel_l2(g.download(), psi) < 2e-14 * np.log2(n ** dim)
+
+
+def test_fused_step_is_deterministic(Q):
+    z = C.load("c2_vg")
+    p = z["params"]
+    out = []
+    for _ in range(2):
+        g, rows = C.gpu_re(p, 2, z["re_psi0"])
+        out.append((g.download(), np.array([C.re_dat_row(r, 7) for r in rows])))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_bad_sizes_are_rejected(Q):
+    with pytest.raises(Q.QsfError) as e:
+        Q.Grid(1, 7, 0.1)
+    assert e.value.code == 1
+    with pytest.raises(Q.QsfError):
+        Q.Grid(2, [64, 32], 0.1)
+    with pytest.raises(Q.QsfError):
+        Q.Grid(1, 16384 * 2, 0.1)
