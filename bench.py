@@ -1,0 +1,356 @@
+"""Benchmark of the GB300 split-operator step on the plain 2D workload.
+
+Workload (the plain-method configuration the headline metric is quoted on): two
+electrons in 1D each, a 2048 x 2048 grid with dx = 0.3, soft-core e-n charge 2 and
+e-e softening 1 (Eberly model), absorber of 205 nodes per side, velocity gauge,
+3-cycle sin^2 pulse at 800 nm and 5e14 W/cm^2, dt = 0.05, with the norm, the
+potential energy and the seven ZOA_FLUX_2D border fluxes computed every step.
+Data are synthetic: a normalised Gaussian start state on the host (seeded), no
+datasets.
+
+One "step" is one Strang step X(dt/2) P(dt) X(dt/2) of the whole grid plus its
+observables.  `value` is grid-point-steps/s over K timed steps with psi resident in
+HBM (CUDA events on the grid's stream around each step, L2 flushed between steps by
+writing a 512 MiB buffer); `e2e` is the same metric measured through the C ABI with
+host buffers: pinned host psi uploaded, K fused steps whose per-step coupling rows
+come from host memory and whose observables rows come back to host memory, psi
+downloaded -- all inside the host-timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the workload on
+its own GPU (a single solve does not shard without an all-to-all); `value` is the
+sum over ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt-steps/s batched+served vs plain @1e-10 L2; HBM GB/s; p50/p99 solve"
+UNIT = "grid-pt-steps/s"
+N_EDGE, DX, NCAP = 2048, 0.3, 205
+NCHARGE, ECHARGE, NSOFT, ESOFT = 2.0, -1.0, 1.0, 1.0
+DT = 0.05
+INTENSITY, WAVELENGTH, NCYCLES = 5e14, 800.0, 3.0
+BYTES_PER_PT_STEP = 64  # algorithmic psi traffic of a 2D step: 2 passes x (16 B read + 16 B write)
+BYTES_PER_PT_PASS = 32
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def _initial_psi(seed=0):
+    """Seeded synthetic start state: a normalised Gaussian with small seeded noise."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(N_EDGE) - (N_EDGE - 1) / 2.0) * DX
+    g = np.exp(-0.5 * x * x)
+    psi = np.outer(g, g).astype(np.complex128)
+    psi += 1e-6 * (rng.standard_normal(psi.shape) + 1j * rng.standard_normal(psi.shape))
+    psi /= math.sqrt(float(np.sum(np.abs(psi) ** 2)) * DX * DX)
+    return psi
+
+
+def _pulse_args():
+    import qsf_gb300 as Q
+    return dict(field=Q.field_from_intensity(INTENSITY), omega=Q.omega_from_wavelength(WAVELENGTH), ncycles=NCYCLES)
+
+
+class _Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    def __init__(self, index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [t.strip() for t in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _ncu_traffic(kernel_kind):
+    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_kind}_2d2048.md")
+    try:
+        txt = open(path).read()
+        m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+# ------------------------------------------------------------------ CPU legs
+def _oracle_sample(nsteps):
+    """Time `nsteps` steps of the CPU oracle (C restatement) on the full workload."""
+    from oracle import oracle as O
+    O.set_border_nodes(25, 14, 10, 40)
+    pa = _pulse_args()
+    c = O.Coupling(O.GAUGE_VELOCITY, [O.Field(3, [O.Pulse(**pa)])])
+    g = O.Grid(2, N_EDGE, DX, nCAP=NCAP, Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT, Esoft=ESOFT, coupling=c)
+    g.psi[...] = _initial_psi()
+    prop = O.Propagator(O.MODE_RE, DT, 0, g, ["norm", "epot", ("flux", O.ZOA_FLUX_2D, 0)])
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        prop.make_step()
+        prop.compute_each()
+    return time.perf_counter() - t0
+
+
+def _cpu_worker(args):
+    nsteps = args
+    return _oracle_sample(nsteps)
+
+
+def cpu_baseline(all_cores: bool, budget_s: float = 20.0):
+    """The oracle port timed on host cores over a bounded sample of the workload."""
+    from oracle import oracle as O
+    O.build()
+    t1 = _oracle_sample(1)
+    nsteps = max(1, min(8, int(budget_s / max(t1, 1e-3))))
+    m = N_EDGE * N_EDGE
+    if not all_cores:
+        t = _oracle_sample(nsteps)
+        return {"value": m * nsteps / t, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": f"{nsteps} Strang steps of the 2048^2 workload (norm, E_pot, 7 ZOA_FLUX_2D fluxes) "
+                          f"on one core, after one untimed step"}
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        pool.map(_cpu_worker, [nsteps] * cores)
+        wall = time.perf_counter() - t0
+    return {"value": m * nsteps * cores / wall, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cores} independent single-core replicas x {nsteps} Strang steps of the 2048^2 workload "
+                      f"(wall clock incl. process start)"}
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    ws, rank, local = _dist()
+    import torch
+    torch.cuda.set_device(local)
+    import qsf_gb300 as Q
+
+    stream = torch.cuda.Stream()
+    pa = _pulse_args()
+    coupling = Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(3, [Q.Pulse(**pa)])])
+    grid = Q.Grid(2, N_EDGE, DX, nCAP=NCAP, potential=Q.POT_EBERLY, Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT,
+                  Esoft=ESOFT, gauge=Q.GAUGE_VELOCITY, n_fields=1, stream=stream.cuda_stream)
+    psi0 = _initial_psi(seed=rank)
+    grid.upload(psi0)
+    outputs = ["norm", "epot", ("flux", Q.ZOA_FLUX_2D, 0)]
+    prop = Q.SplitPropagator(Q.MODE_RE, DT, 0, grid, coupling, outputs)
+    m = grid.m
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def one_step(profile=None):
+        sched = prop._schedule(1)
+        rows, _ = grid.step(Q.MODE_RE, DT, 1, sched, obs=Q.OBS_NORM | Q.OBS_EPOT, borders=Q.ZOA_FLUX_2D,
+                            profile=profile)
+        return rows
+
+    for _ in range(args.warmup):
+        one_step()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    clocks = _Clocks(local)
+    profile = {}
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            one_step(profile)
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    clk = clocks.stop()
+    total_ms = _max_over_ranks(ws, float(sum(step_ms)))
+    _barrier(ws)
+    pts = _sum_over_ranks(ws, float(m) * args.steps)
+    value = pts / (total_ms / 1e3)
+
+    # e2e through the C ABI with host buffers (pinned psi, coupling rows from host)
+    pinned = torch.empty((m * 2,), dtype=torch.float64, pin_memory=True)
+    host_psi = pinned.numpy().view(np.complex128).reshape(grid.shape)
+    host_psi[...] = psi0
+    e2e_prop = Q.SplitPropagator(Q.MODE_RE, DT, 0, grid, Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(3, [Q.Pulse(**pa)])]),
+                                 outputs)
+    sched = e2e_prop._schedule(args.steps)
+    _barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grid.upload(host_psi)
+    rows, done = grid.step(Q.MODE_RE, DT, args.steps, sched, obs=Q.OBS_NORM | Q.OBS_EPOT, borders=Q.ZOA_FLUX_2D)
+    host_psi[...] = grid.download()
+    e2e_s = _max_over_ranks(ws, time.perf_counter() - t0)
+    e2e_value = _sum_over_ranks(ws, float(m) * args.steps) / e2e_s
+    ncol = rows.shape[1]
+
+    # roofline of the dominant kernel
+    kinds = {k: v for k, v in profile.items() if v[1] > 0}
+    dom = max(kinds, key=lambda k: kinds[k][0])
+    dom_ms = kinds[dom][0] / kinds[dom][1]
+    peak, peak_kind = _peaks()
+    achieved = BYTES_PER_PT_PASS * m / (dom_ms / 1e3) / 1e9
+    traffic = _ncu_traffic(dom)
+    launches = sum(v[1] for v in kinds.values())
+
+    if rank == 0:
+        cpu = cpu_baseline(all_cores=False)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128/f64", "data": "synthetic (seeded Gaussian start state, sin^2 pulse)",
+            "config": {"workload": "plain 2D split step, 2 electrons (1D each), 2048x2048, dx=0.3, dt=0.05, "
+                                   "VG 800 nm 5e14 W/cm^2 3-cycle sin^2, absorber 205 nodes, norm+E_pot+ZOA_FLUX_2D "
+                                   "every step",
+                       "grid": [N_EDGE, N_EDGE], "parallelism": f"replicas x{ws}",
+                       "l2": "flushed between timed steps (512 MiB write)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": (16 * m + 24 * args.steps) / args.steps,
+                    "d2h_bytes_per_step": (16 * m + 8 * ncol * args.steps) / args.steps},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_launch": BYTES_PER_PT_PASS * m,
+                         "avg_launch_ms": dom_ms},
+            "kernels_ms_per_step": {k: v[0] / args.steps for k, v in kinds.items()},
+            "hbm_gbs_step": BYTES_PER_PT_STEP * value / ws / 1e9,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference arm: the reference algorithm's CPU implementation (oracle port,
+    the reference's own build needs MPI/FFTW and the reference checkout) on all host
+    cores, same workload, metric and unit."""
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    samples = []
+    for _ in range(max(1, args.steps // 10)):
+        samples.append(cpu_baseline(all_cores=True, budget_s=10.0))
+    v = statistics.median(s["value"] for s in samples)
+    cb = dict(samples[0])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128/f64", "data": "synthetic (seeded Gaussian start state, sin^2 pulse)",
+            "config": {"workload": "plain 2D split step, 2 electrons (1D each), 2048x2048, dx=0.3, dt=0.05, "
+                                   "VG 800 nm 5e14 W/cm^2 3-cycle sin^2, absorber 205 nodes, norm+E_pot+ZOA_FLUX_2D "
+                                   "every step", "grid": [N_EDGE, N_EDGE]},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

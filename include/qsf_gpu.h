@@ -172,8 +172,45 @@ typedef struct qsf_step_desc {
   double state_accuracy;    /* IM convergence threshold (0: run all nsteps)    */
   double last_energy;       /* E before the first step of this call            */
   int energy_after_normalize; /* bit 0: epot, bit 1: ekin seen after Normalize */
+  /* diagnostics: when non-NULL, every launch is bracketed by CUDA events on the
+   * grid's stream (no graph) and its device time in ms is added to
+   * kernel_ms[QSF_K_*]; kernel_launches[QSF_K_*] counts the launches. */
+  float* kernel_ms;
+  int64_t* kernel_launches;
 } qsf_step_desc;
+/* kernel kinds of the fused step (for qsf_step_desc.kernel_ms) */
+#define QSF_K_TABLES 0
+#define QSF_K_ROW_OPEN 1
+#define QSF_K_AXIS_FWD 2
+#define QSF_K_AXIS_FPI 3
+#define QSF_K_AXIS_INV 4
+#define QSF_K_ROW_CLOSE 5
+#define QSF_K_AXIS_EKIN 6
+#define QSF_K_FINALIZE 7
+#define QSF_K_LINE_STEP 8
+#define QSF_K_COUNT 9
 int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done);
+
+/* ------------------------------------------------------------- batching */
+/* Many independent solves (grids of different sizes, each with its own step program
+ * and pulse) advanced together: solves sharing (dim, line length) form a group, and
+ * one launch per split stage covers every solve of a group; all groups' launches for
+ * one step are captured once into a CUDA graph and replayed.  Each solve stops at its
+ * own nsteps; results are identical to running it alone through qsf_step (the
+ * per-solve work and reduction order do not depend on the batch).  There is no
+ * counterpart in the reference, which runs one solve per process group. */
+typedef struct qsf_batch qsf_batch;
+int qsf_batch_create(void* stream, qsf_batch** out);
+int qsf_batch_destroy(qsf_batch* b);
+/* Adds grid g (owned by the caller; it must stay alive while in the batch) with the
+ * step program d (coupling rows are copied at this call).  d->kernel_ms is ignored. */
+int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot);
+/* Removes a member; applies its pending Normalize factor first. */
+int qsf_batch_remove(qsf_batch* b, int64_t slot);
+/* Advances every member by up to `steps` steps; *active = members with steps left. */
+int qsf_batch_run(qsf_batch* b, int64_t steps, int64_t* active);
+/* Observables rows (nsteps x (3 + nborders)) and steps done of one member. */
+int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_done);
 
 /* ------------------------------------------------------------ diagnostics */
 /* last CUDA error text seen by the library (thread-local, never NULL) */

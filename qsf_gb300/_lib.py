@@ -54,7 +54,13 @@ class StepDesc(ctypes.Structure):
         ("state_accuracy", ctypes.c_double),
         ("last_energy", ctypes.c_double),
         ("energy_after_normalize", ctypes.c_int),
+        ("kernel_ms", ctypes.POINTER(ctypes.c_float)),
+        ("kernel_launches", ctypes.POINTER(ctypes.c_int64)),
     ]
+
+
+KERNEL_KINDS = ["tables", "row_open", "axis_fwd", "axis_fpi", "axis_inv", "row_close", "axis_ekin", "finalize",
+                "line_step"]
 
 
 _lib = None
@@ -89,6 +95,12 @@ def lib():
         "qsf_add_gaussian": [vp, ctypes.c_double, ctypes.c_double],
         "qsf_step": [vp, ctypes.POINTER(StepDesc), dp, ctypes.POINTER(i64)],
         "qsf_fft_plan_radices": [i64, ip, ip],
+        "qsf_batch_create": [vp, ctypes.POINTER(vp)],
+        "qsf_batch_destroy": [vp],
+        "qsf_batch_add": [vp, vp, ctypes.POINTER(StepDesc), ctypes.POINTER(i64)],
+        "qsf_batch_remove": [vp, i64],
+        "qsf_batch_run": [vp, i64, ctypes.POINTER(i64)],
+        "qsf_batch_result": [vp, i64, dp, ctypes.POINTER(i64)],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -68,7 +68,6 @@ std::vector<KernelSet>& kernel_table();
 // kernel launch geometry
 constexpr int kMaxLine1D = 8192;        // 1D line held in shared memory (complex128)
 constexpr int kMaxTile = 4096;          // points per block in row / axis passes
-constexpr int kMaxSmemOptin = 227 * 1024;
 
 }  // namespace
 
@@ -92,6 +91,8 @@ struct qsf_grid {
   BorderNodes bn;
   std::vector<double2*> tw_owned;
   const KernelSet* ks = nullptr;  // kernels for this grid's line length
+  GridDev* dG = nullptr;          // device copy of G (step kernels read descriptors from device arrays)
+  StepDev* dS = nullptr;          // device copy of the current step descriptor
   // static tables
   double2* xs = nullptr;
   double* V = nullptr;
@@ -155,15 +156,18 @@ int init_kernel_table() {
     QSF_CU(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     return QSF_OK;
   };
+  // dynamic shared memory actually requested: tiles of kMaxTile points (row / axis
+  // passes), lines of up to 16 * kLineThreads points (line kernel, plain row FFT)
+  const int tile = kMaxTile * (int)sizeof(double2);
+  const int line = 16 * kLineThreads * (int)sizeof(double2);
   for (const KernelSet& k : t) {
-    const int tile = std::min(kMaxSmemOptin, std::max(48 * 1024, k.n * 16 * 4));
     int rc;
     if ((rc = lim((const void*)k.row_open, tile)) || (rc = lim((const void*)k.row_close, tile)) ||
         (rc = lim((const void*)k.axis_fwd, tile)) || (rc = lim((const void*)k.axis_inv, tile)) ||
         (rc = lim((const void*)k.axis_fpi, tile)) || (rc = lim((const void*)k.axis_ekin, tile)) ||
         (rc = lim((const void*)k.axis_fft_f, tile)) || (rc = lim((const void*)k.axis_fft_b, tile)) ||
-        (rc = lim((const void*)k.row_fft_f, kMaxSmemOptin)) || (rc = lim((const void*)k.row_fft_b, kMaxSmemOptin)) ||
-        (rc = lim((const void*)k.line_step, kMaxSmemOptin)))
+        (rc = lim((const void*)k.row_fft_f, line)) || (rc = lim((const void*)k.row_fft_b, line)) ||
+        (rc = lim((const void*)k.line_step, k.n * (int)sizeof(double2))))
       return rc;
   }
   done = true;
@@ -298,35 +302,332 @@ int ensure_flux(qsf_grid* g, int nb, const int* types, int64_t box) {
   g->nfpts = (int)fps.size();
   g->nfterms = (int)fts.size();
   g->nfblk = (int)std::min<long long>(64, std::max<long long>(1, (g->nfterms + 2047) / 2048));
-  if ((rc = dev_reserve(g->fpartials, g->fpmax, (size_t)g->nfblk * kMaxFluxBorders))) return rc;
   g->fl_borders = want;
   g->fl_box = box;
   g->fl_ready = true;
   return QSF_OK;
 }
 
-// one step's launches (all read the device step counter)
-int launch_step(qsf_grid* g, const StepDev& S) {
-  const GridDev& G = g->G;
-  const int D = G.dim;
-  cudaStream_t st = g->stream;
-  const KernelSet& K = *g->ks;
-  const int ntab = D * S.nmax * (G.gauge == 1 ? 3 : 1);
-  k_tables<<<std::max(1, std::min(64, (ntab + 255) / 256)), 256, 0, st>>>(G, S);
-  if (D == 1) {
-    K.line_step<<<1, kLineThreads, (size_t)G.ax[0].n * sizeof(double2), st>>>(G, S);
-  } else {
-    K.row_open<<<g->nrowblk, kRowThreads, g->row_smem, st>>>(G, S, g->row_L);
-    if (D == 3) K.axis_fwd<<<g->ax_blocks[1], kRowThreads, g->ax_smem[1], st>>>(G, S, 1, g->ax_C[1]);
-    K.axis_fpi<<<g->ax_blocks[0], kRowThreads, g->ax_smem[0], st>>>(G, S, 0, g->ax_C[0]);
-    if (D == 3) K.axis_inv<<<g->ax_blocks[1], kRowThreads, g->ax_smem[1], st>>>(G, S, 1, g->ax_C[1]);
-    K.row_close<<<g->nrowblk, kRowThreads, g->row_smem, st>>>(G, S, g->row_L);
-    if (S.obs & QSF_OBS_EKIN)
-      for (int ax = 0; ax < D - 1; ++ax)
-        K.axis_ekin<<<g->ax_blocks[ax], kRowThreads, g->ax_smem[ax], st>>>(G, S, ax, g->ax_C[ax]);
+// Optional per-launch event timing (qsf_step_desc.kernel_ms): every launch of a step
+// is bracketed by a pair of events from a pool; the pairs are read after the step's
+// work is queued and synchronised once, so timing adds no host gaps between kernels.
+struct Prof {
+  float* ms = nullptr;
+  int64_t* count = nullptr;
+  cudaStream_t st = nullptr;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kinds;
+  int used = 0;
+  int init(cudaStream_t s, int pairs) {
+    st = s;
+    ev.resize((size_t)pairs * 2);
+    for (auto& e : ev) QSF_CU(cudaEventCreate(&e));
+    return QSF_OK;
   }
-  k_finalize<<<S.nfterms > 0 ? g->nfblk : 1, 256, 0, st>>>(G, S);
-  QSF_CU(cudaGetLastError());
+  void release() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    ev.clear();
+  }
+  int begin() {
+    if (!ms) return QSF_OK;
+    if ((size_t)(used * 2 + 1) >= ev.size()) return fail(QSF_EINVAL, "profiling event pool exhausted");
+    QSF_CU(cudaEventRecord(ev[(size_t)used * 2], st));
+    return QSF_OK;
+  }
+  int end(int kind) {
+    if (!ms) return QSF_OK;
+    QSF_CU(cudaEventRecord(ev[(size_t)used * 2 + 1], st));
+    kinds.push_back(kind);
+    ++used;
+    return QSF_OK;
+  }
+  int flush() {
+    if (!ms || used == 0) return QSF_OK;
+    QSF_CU(cudaEventSynchronize(ev[(size_t)used * 2 - 1]));
+    for (int i = 0; i < used; ++i) {
+      float t = 0.f;
+      QSF_CU(cudaEventElapsedTime(&t, ev[(size_t)i * 2], ev[(size_t)i * 2 + 1]));
+      ms[kinds[(size_t)i]] += t;
+      if (count) count[kinds[(size_t)i]] += 1;
+    }
+    used = 0;
+    kinds.clear();
+    return QSF_OK;
+  }
+};
+
+// Launch geometry shared by every solve of one (dim, line length) group.
+struct Geom {
+  int dim = 1, n = 0, nmax = 0, gauge = 0;
+  int nrowblk = 1, row_L = 1;
+  size_t row_smem = 0;
+  int ax_blocks[3] = {0, 0, 0}, ax_C[3] = {1, 1, 1};
+  size_t ax_smem[3] = {0, 0, 0};
+};
+
+Geom geom_of(const qsf_grid* g) {
+  Geom q;
+  q.dim = g->G.dim;
+  q.n = g->G.ax[0].n;
+  q.nmax = g->nmax;
+  q.gauge = g->G.gauge;
+  q.nrowblk = g->nrowblk;
+  q.row_L = g->row_L;
+  q.row_smem = g->row_smem;
+  for (int k = 0; k < 3; ++k) {
+    q.ax_blocks[k] = g->ax_blocks[k];
+    q.ax_C[k] = g->ax_C[k];
+    q.ax_smem[k] = g->ax_smem[k];
+  }
+  return q;
+}
+
+// One step's launches for `count` solves sharing kernels K and geometry q; every
+// kernel reads its solve's descriptors (blockIdx.y) and step counter from device memory.
+int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const StepDev* dS, int count, bool ekin,
+                 int nfblk, cudaStream_t st, Prof* P) {
+  Prof none;
+  Prof& pf = P ? *P : none;
+  int rc;
+#define QSF_TIMED(kind, launch)             \
+  do {                                      \
+    if ((rc = pf.begin())) return rc;       \
+    launch;                                 \
+    QSF_CU(cudaGetLastError());             \
+    if ((rc = pf.end(kind))) return rc;     \
+  } while (0)
+  const int D = q.dim;
+  const int ntab = D * q.nmax * (q.gauge == 1 ? 3 : 1);
+  const dim3 gt(std::max(1, std::min(64, (ntab + 255) / 256)), count);
+  QSF_TIMED(QSF_K_TABLES, (k_tables<<<gt, 256, 0, st>>>(dG, dS)));
+  if (D == 1) {
+    QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(1, count), kLineThreads, (size_t)q.n * sizeof(double2), st>>>(dG, dS)));
+  } else {
+    const dim3 gr(q.nrowblk, count);
+    QSF_TIMED(QSF_K_ROW_OPEN, (K.row_open<<<gr, kRowThreads, q.row_smem, st>>>(dG, dS, q.row_L)));
+    if (D == 3)
+      QSF_TIMED(QSF_K_AXIS_FWD,
+                (K.axis_fwd<<<dim3(q.ax_blocks[1], count), kRowThreads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
+    QSF_TIMED(QSF_K_AXIS_FPI,
+              (K.axis_fpi<<<dim3(q.ax_blocks[0], count), kRowThreads, q.ax_smem[0], st>>>(dG, dS, 0, q.ax_C[0])));
+    if (D == 3)
+      QSF_TIMED(QSF_K_AXIS_INV,
+                (K.axis_inv<<<dim3(q.ax_blocks[1], count), kRowThreads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
+    QSF_TIMED(QSF_K_ROW_CLOSE, (K.row_close<<<gr, kRowThreads, q.row_smem, st>>>(dG, dS, q.row_L)));
+    if (ekin)
+      for (int ax = 0; ax < D - 1; ++ax)
+        QSF_TIMED(QSF_K_AXIS_EKIN,
+                  (K.axis_ekin<<<dim3(q.ax_blocks[ax], count), kRowThreads, q.ax_smem[ax], st>>>(dG, dS, ax, q.ax_C[ax])));
+  }
+  QSF_TIMED(QSF_K_FINALIZE, (k_finalize<<<dim3(nfblk, count), 256, 0, st>>>(dG, dS)));
+#undef QSF_TIMED
+  return QSF_OK;
+}
+
+int launch_step(qsf_grid* g, const StepDev& S, Prof* P = nullptr) {
+  return launch_group(*g->ks, geom_of(g), g->dG, g->dS, 1, (S.obs & QSF_OBS_EKIN) != 0,
+                      S.nfterms > 0 ? g->nfblk : 1, g->stream, P);
+}
+
+// Validates a step program and stages everything a run of it needs on the device:
+// static tables for dt/2, flux point lists, coupling rows, observables rows, control
+// words; fills the step descriptor and uploads it to g->dS.
+int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_out) {
+  if (d->mode != QSF_MODE_IM && d->mode != QSF_MODE_RE) return fail(QSF_EINVAL, "mode must be IM or RE");
+  if (d->nsteps < 1) return fail(QSF_EINVAL, "nsteps < 1");
+  if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
+  const GridDev& G = g->G;
+  int rc;
+  if ((rc = ensure_static(g, d->mode, d->dt * 0.5))) return rc;
+  const bool want_flux = (d->obs & QSF_OBS_FLUX) && d->nborders > 0;
+  if (want_flux && (rc = ensure_flux(g, d->nborders, d->border_types, d->box_size))) return rc;
+  const int nb = want_flux ? d->nborders : 0;
+  const int ncol = 3 + nb;
+  const int cstride = G.gauge == QSF_GAUGE_LENGTH ? 6 : 3;
+  if ((rc = dev_reserve(g->rows_dev, g->rows_cap, (size_t)d->nsteps * ncol))) return rc;
+  const double* coup = nullptr;
+  if (d->coupling) {
+    if ((rc = dev_reserve(g->coup_dev, g->coup_cap, (size_t)d->nsteps * cstride))) return rc;
+    QSF_CU(cudaMemcpyAsync(g->coup_dev, d->coupling, (size_t)d->nsteps * cstride * sizeof(double),
+                           cudaMemcpyHostToDevice, g->stream));
+    coup = g->coup_dev;
+  }
+  long long ctl_h[8] = {0, (long long)d->nsteps, 0, 0, 0, 0, 0, 0};
+  double en_h[2] = {d->last_energy, 0.0};
+  double sc_h[2] = {1.0, 1.0};
+  QSF_CU(cudaMemcpyAsync(g->ctl, ctl_h, sizeof(ctl_h), cudaMemcpyHostToDevice, g->stream));
+  QSF_CU(cudaMemcpyAsync(g->energy, en_h, sizeof(en_h), cudaMemcpyHostToDevice, g->stream));
+  QSF_CU(cudaMemcpyAsync(g->scale, sc_h, sizeof(sc_h), cudaMemcpyHostToDevice, g->stream));
+  StepDev S{};
+  S.mode = d->mode;
+  S.dt = d->dt;
+  S.nsteps = d->nsteps;
+  S.coupling = coup;
+  S.coup_stride = cstride;
+  S.xs = g->xs;
+  S.V = g->V;
+  S.ptab = g->ptab;
+  S.xdyn = g->xdyn;
+  S.nmax = g->nmax;
+  S.partials = g->partials;
+  S.pmax = g->pmax;
+  S.nrowblk = g->nrowblk;
+  for (int ax = 0; ax < 3; ++ax) S.naxblk[ax] = g->ax_blocks[ax];
+  S.obs = d->obs | QSF_OBS_NORM;
+  if (nb == 0) S.obs &= ~QSF_OBS_FLUX;
+  S.normalize = d->normalize;
+  S.energy_after_normalize = d->energy_after_normalize;
+  S.state_accuracy = d->mode == QSF_MODE_IM ? d->state_accuracy : 0.0;
+  S.nborders = nb;
+  if (want_flux) {
+    S.snap = g->snap;
+    S.row_ptr = g->row_ptr;
+    S.snap_idx = g->snap_idx;
+    S.fpts = g->fpts;
+    S.fterms = g->fterms;
+    S.nfterms = g->nfterms;
+  }
+  S.fpartials = g->fpartials;
+  S.ctl = g->ctl;
+  S.energy_state = g->energy;
+  S.rows = g->rows_dev;
+  S.scale = g->scale;
+  QSF_CU(cudaMemcpyAsync(g->dS, &S, sizeof(StepDev), cudaMemcpyHostToDevice, g->stream));
+  *out = S;
+  *ncol_out = ncol;
+  return QSF_OK;
+}
+
+// After a run: pending Normalize factor, observables rows and progress back to host.
+int finish_step(qsf_grid* g, int normalize, int64_t nsteps, int ncol, double* rows, int64_t* steps_done) {
+  if (normalize) {
+    k_scale<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G.psi, g->G.m, g->scale);
+    QSF_CU(cudaGetLastError());
+  }
+  long long ctl_h[8];
+  QSF_CU(cudaMemcpyAsync(ctl_h, g->ctl, sizeof(ctl_h), cudaMemcpyDeviceToHost, g->stream));
+  if (rows)
+    QSF_CU(cudaMemcpyAsync(rows, g->rows_dev, (size_t)nsteps * ncol * sizeof(double), cudaMemcpyDeviceToHost,
+                           g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  if (steps_done) *steps_done = ctl_h[2];
+  if (ctl_h[4]) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a step's reductions");
+  return QSF_OK;
+}
+
+// Captures the launches issued by `body` on `st` into an executable graph.
+template <class F>
+int capture_graph(cudaStream_t st, F&& body, cudaGraphExec_t* exec) {
+  cudaGraph_t graph = nullptr;
+  QSF_CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int rc = body();
+  cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+  return QSF_OK;
+}
+
+struct BatchMember {
+  qsf_grid* g = nullptr;
+  StepDev S{};
+  int64_t nsteps = 0;
+  int ncol = 0;
+  int normalize = 0;
+  bool scaled = false;
+};
+
+struct BatchGroup {
+  const KernelSet* ks = nullptr;
+  Geom q;
+  std::vector<int64_t> slots;
+  GridDev* dG = nullptr;
+  StepDev* dS = nullptr;
+  bool ekin = false;
+  int nfblk = 1;
+};
+
+}  // namespace
+
+struct qsf_batch {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::map<int64_t, BatchMember> members;
+  int64_t next_slot = 0;
+  bool dirty = true;
+  std::vector<BatchGroup> groups;
+  cudaGraphExec_t exec = nullptr;
+  long long* ctl_host = nullptr;  // pinned, 8 words per member
+  size_t ctl_cap = 0;
+};
+
+namespace {
+
+void free_groups(qsf_batch* b) {
+  for (BatchGroup& gr : b->groups) {
+    if (gr.dG) cudaFree(gr.dG);
+    if (gr.dS) cudaFree(gr.dS);
+  }
+  b->groups.clear();
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+}
+
+// Regroups members by (dim, line length), uploads the descriptor arrays and captures
+// one batch step (every group's launches) into a graph.
+int rebuild_batch(qsf_batch* b) {
+  free_groups(b);
+  std::map<std::pair<int, int>, BatchGroup> by;
+  for (auto& kv : b->members) {
+    const qsf_grid* g = kv.second.g;
+    BatchGroup& gr = by[{g->G.dim, g->G.ax[0].n}];
+    if (!gr.ks) {
+      gr.ks = g->ks;
+      gr.q = geom_of(g);
+    }
+    gr.q.gauge = std::max(gr.q.gauge, g->G.gauge);
+    gr.slots.push_back(kv.first);
+    gr.ekin = gr.ekin || (kv.second.S.obs & QSF_OBS_EKIN);
+    if (kv.second.S.nfterms > 0) gr.nfblk = std::max(gr.nfblk, g->nfblk);
+  }
+  for (auto& kv : by) {
+    BatchGroup gr = kv.second;
+    const size_t c = gr.slots.size();
+    std::vector<GridDev> hg(c);
+    std::vector<StepDev> hs(c);
+    for (size_t i = 0; i < c; ++i) {
+      const BatchMember& mb = b->members[gr.slots[i]];
+      hg[i] = mb.g->G;
+      hs[i] = mb.S;
+    }
+    int rc;
+    if ((rc = dev_alloc(gr.dG, c)) || (rc = dev_alloc(gr.dS, c))) return rc;
+    QSF_CU(cudaMemcpyAsync(gr.dG, hg.data(), c * sizeof(GridDev), cudaMemcpyHostToDevice, b->stream));
+    QSF_CU(cudaMemcpyAsync(gr.dS, hs.data(), c * sizeof(StepDev), cudaMemcpyHostToDevice, b->stream));
+    b->groups.push_back(gr);
+  }
+  QSF_CU(cudaStreamSynchronize(b->stream));
+  if (!b->groups.empty()) {
+    int rc = capture_graph(
+        b->stream,
+        [&]() {
+          for (const BatchGroup& gr : b->groups) {
+            const int r = launch_group(*gr.ks, gr.q, gr.dG, gr.dS, (int)gr.slots.size(), gr.ekin, gr.nfblk,
+                                       b->stream, nullptr);
+            if (r) return r;
+          }
+          return QSF_OK;
+        },
+        &b->exec);
+    if (rc) return rc;
+  }
+  b->dirty = false;
   return QSF_OK;
 }
 
@@ -466,10 +767,14 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   g->pmax = std::max({g->nrowblk, g->ax_blocks[0], g->ax_blocks[1], g->ax_blocks[2], 256});
   if ((rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)2 * D * g->nmax)) ||
       (rc = dev_alloc(g->partials, (size_t)5 * g->pmax)) || (rc = dev_alloc(g->ctl, 8)) ||
-      (rc = dev_alloc(g->energy, 2)) || (rc = dev_alloc(g->scale, 2))) {
+      (rc = dev_alloc(g->energy, 2)) || (rc = dev_alloc(g->scale, 2)) ||
+      (rc = dev_alloc(g->fpartials, (size_t)64 * kMaxFluxBorders)) || (rc = dev_alloc(g->dG, 1)) ||
+      (rc = dev_alloc(g->dS, 1))) {
     qsf_grid_destroy(g);
     return rc;
   }
+  g->fpmax = (size_t)64 * kMaxFluxBorders;
+  cudaMemcpyAsync(g->dG, &g->G, sizeof(GridDev), cudaMemcpyHostToDevice, g->stream);
   cudaMemsetAsync(g->partials, 0, sizeof(double) * 5 * g->pmax, g->stream);
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) {
     qsf_grid_destroy(g);
@@ -503,6 +808,8 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->row_ptr);
   fr(g->fpts);
   fr(g->fterms);
+  fr(g->dG);
+  fr(g->dS);
   if (g->own_stream) cudaStreamDestroy(g->stream);
   delete g;
   return QSF_OK;
@@ -641,93 +948,30 @@ int qsf_add_gaussian(qsf_grid* g, double at, double delta) {
 
 int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done) {
   if (!g || !d) return fail(QSF_EINVAL, "null argument");
-  if (d->mode != QSF_MODE_IM && d->mode != QSF_MODE_RE) return fail(QSF_EINVAL, "mode must be IM or RE");
-  if (d->nsteps < 0) return fail(QSF_EINVAL, "nsteps < 0");
-  if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
   if (steps_done) *steps_done = 0;
   if (d->nsteps == 0) return QSF_OK;
-  const GridDev& G = g->G;
-  const int D = G.dim;
-  int rc;
-  if ((rc = ensure_static(g, d->mode, d->dt * 0.5))) return rc;
-  const bool want_flux = (d->obs & QSF_OBS_FLUX) && d->nborders > 0;
-  if (want_flux && (rc = ensure_flux(g, d->nborders, d->border_types, d->box_size))) return rc;
-  const int nb = want_flux ? d->nborders : 0;
-  const int ncol = 3 + nb;
-  const int cstride = G.gauge == QSF_GAUGE_LENGTH ? 6 : 3;
-  if ((rc = dev_reserve(g->rows_dev, g->rows_cap, (size_t)d->nsteps * ncol))) return rc;
-  const double* coup = nullptr;
-  if (d->coupling) {
-    if ((rc = dev_reserve(g->coup_dev, g->coup_cap, (size_t)d->nsteps * cstride))) return rc;
-    QSF_CU(cudaMemcpyAsync(g->coup_dev, d->coupling, (size_t)d->nsteps * cstride * sizeof(double),
-                           cudaMemcpyHostToDevice, g->stream));
-    coup = g->coup_dev;
-  }
-  long long ctl_h[8] = {0, (long long)d->nsteps, 0, 0, 0, 0, 0, 0};
-  double en_h[2] = {d->last_energy, 0.0};
-  double sc_h[2] = {1.0, 1.0};
-  QSF_CU(cudaMemcpyAsync(g->ctl, ctl_h, sizeof(ctl_h), cudaMemcpyHostToDevice, g->stream));
-  QSF_CU(cudaMemcpyAsync(g->energy, en_h, sizeof(en_h), cudaMemcpyHostToDevice, g->stream));
-  QSF_CU(cudaMemcpyAsync(g->scale, sc_h, sizeof(sc_h), cudaMemcpyHostToDevice, g->stream));
-
   StepDev S{};
-  S.mode = d->mode;
-  S.dt = d->dt;
-  S.nsteps = d->nsteps;
-  S.coupling = coup;
-  S.coup_stride = cstride;
-  S.xs = g->xs;
-  S.V = g->V;
-  S.ptab = g->ptab;
-  S.xdyn = g->xdyn;
-  S.nmax = g->nmax;
-  S.partials = g->partials;
-  S.pmax = g->pmax;
-  S.nrowblk = g->nrowblk;
-  for (int ax = 0; ax < 3; ++ax) S.naxblk[ax] = g->ax_blocks[ax];
-  S.obs = d->obs | QSF_OBS_NORM;
-  if (nb == 0) S.obs &= ~QSF_OBS_FLUX;
-  S.normalize = d->normalize;
-  S.energy_after_normalize = d->energy_after_normalize;
-  S.state_accuracy = d->mode == QSF_MODE_IM ? d->state_accuracy : 0.0;
-  S.nborders = nb;
-  if (want_flux) {
-    S.snap = g->snap;
-    S.row_ptr = g->row_ptr;
-    S.snap_idx = g->snap_idx;
-    S.fpts = g->fpts;
-    S.fterms = g->fterms;
-    S.nfterms = g->nfterms;
-    S.fpartials = g->fpartials;
-  }
-  if (!S.fpartials) {
-    if ((rc = dev_reserve(g->fpartials, g->fpmax, (size_t)kMaxFluxBorders))) return rc;
-    S.fpartials = g->fpartials;
-  }
-  S.ctl = g->ctl;
-  S.energy_state = g->energy;
-  S.rows = g->rows_dev;
-  S.scale = g->scale;
-
-  if (d->nsteps < 4) {
+  int ncol = 0, rc;
+  if ((rc = prepare_step(g, d, &S, &ncol))) return rc;
+  if (d->kernel_ms) {
+    Prof P;
+    P.ms = d->kernel_ms;
+    P.count = d->kernel_launches;
+    rc = P.init(g->stream, 16);
+    for (int64_t k = 0; k < d->nsteps && rc == QSF_OK; ++k) {
+      rc = launch_step(g, S, &P);
+      if (rc == QSF_OK) rc = P.flush();
+    }
+    P.release();
+    if (rc) return rc;
+  } else if (d->nsteps < 4) {
     for (int64_t k = 0; k < d->nsteps; ++k)
       if ((rc = launch_step(g, S))) return rc;
   } else {
-    cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    QSF_CU(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
-    rc = launch_step(g, S);
-    cudaError_t ce = cudaStreamEndCapture(g->stream, &graph);
-    if (rc) {
-      if (graph) cudaGraphDestroy(graph);
-      return rc;
-    }
-    if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-    ce = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    if ((rc = capture_graph(g->stream, [&]() { return launch_step(g, S); }, &exec))) return rc;
     for (int64_t k = 0; k < d->nsteps; ++k) {
-      ce = cudaGraphLaunch(exec, g->stream);
+      const cudaError_t ce = cudaGraphLaunch(exec, g->stream);
       if (ce != cudaSuccess) {
         cudaGraphExecDestroy(exec);
         return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
@@ -735,17 +979,127 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
     }
     cudaGraphExecDestroy(exec);
   }
-  if (d->normalize) {
-    k_scale<<<grid_blocks(G.m), 256, 0, g->stream>>>(G.psi, G.m, g->scale);
+  return finish_step(g, d->normalize, d->nsteps, ncol, rows, steps_done);
+}
+
+int qsf_batch_create(void* stream, qsf_batch** out) {
+  if (!out) return fail(QSF_EINVAL, "null argument");
+  if (int rc = init_kernel_table()) return rc;
+  qsf_batch* b = new qsf_batch();
+  if (stream) {
+    b->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete b;
+      return fail(QSF_ECUDA, "cudaStreamCreate failed");
+    }
+    b->own_stream = true;
+  }
+  *out = b;
+  return QSF_OK;
+}
+
+int qsf_batch_destroy(qsf_batch* b) {
+  if (!b) return QSF_OK;
+  cudaStreamSynchronize(b->stream);
+  free_groups(b);
+  if (b->ctl_host) cudaFreeHost(b->ctl_host);
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return QSF_OK;
+}
+
+int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot) {
+  if (!b || !g || !d || !slot) return fail(QSF_EINVAL, "null argument");
+  for (auto& kv : b->members)
+    if (kv.second.g == g) return fail(QSF_ESTATE, "grid is already in the batch");
+  QSF_CU(cudaStreamSynchronize(b->stream));
+  BatchMember mb;
+  mb.g = g;
+  qsf_step_desc dd = *d;
+  dd.kernel_ms = nullptr;
+  dd.kernel_launches = nullptr;
+  int rc;
+  if ((rc = prepare_step(g, &dd, &mb.S, &mb.ncol))) return rc;
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  mb.nsteps = d->nsteps;
+  mb.normalize = d->normalize;
+  *slot = b->next_slot++;
+  b->members[*slot] = mb;
+  b->dirty = true;
+  return QSF_OK;
+}
+
+int qsf_batch_remove(qsf_batch* b, int64_t slot) {
+  if (!b) return fail(QSF_EINVAL, "null argument");
+  auto it = b->members.find(slot);
+  if (it == b->members.end()) return fail(QSF_EINVAL, "unknown slot");
+  BatchMember& mb = it->second;
+  if (mb.normalize && !mb.scaled) {
+    k_scale<<<grid_blocks(mb.g->G.m), 256, 0, b->stream>>>(mb.g->G.psi, mb.g->G.m, mb.g->scale);
     QSF_CU(cudaGetLastError());
   }
-  QSF_CU(cudaMemcpyAsync(ctl_h, g->ctl, sizeof(ctl_h), cudaMemcpyDeviceToHost, g->stream));
+  QSF_CU(cudaStreamSynchronize(b->stream));
+  b->members.erase(it);
+  b->dirty = true;
+  return QSF_OK;
+}
+
+int qsf_batch_run(qsf_batch* b, int64_t steps, int64_t* active) {
+  if (!b || steps < 0) return fail(QSF_EINVAL, "bad argument");
+  int rc;
+  if (b->dirty && (rc = rebuild_batch(b))) return rc;
+  if (b->exec)
+    for (int64_t k = 0; k < steps; ++k) {
+      const cudaError_t ce = cudaGraphLaunch(b->exec, b->stream);
+      if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
+    }
+  const size_t nm = b->members.size();
+  if (nm * 8 > b->ctl_cap) {
+    if (b->ctl_host) cudaFreeHost(b->ctl_host);
+    b->ctl_cap = std::max<size_t>(nm * 8, 64);
+    QSF_CU(cudaMallocHost((void**)&b->ctl_host, b->ctl_cap * sizeof(long long)));
+  }
+  size_t i = 0;
+  for (auto& kv : b->members) {
+    QSF_CU(cudaMemcpyAsync(b->ctl_host + i * 8, kv.second.g->ctl, 8 * sizeof(long long), cudaMemcpyDeviceToHost,
+                           b->stream));
+    ++i;
+  }
+  QSF_CU(cudaStreamSynchronize(b->stream));
+  int64_t act = 0;
+  i = 0;
+  bool bad = false;
+  for (auto& kv : b->members) {
+    const long long* c = b->ctl_host + i * 8;
+    const bool done = c[0] >= kv.second.nsteps || c[0] > c[1];
+    if (!done) ++act;
+    if (c[4]) bad = true;
+    ++i;
+  }
+  if (active) *active = act;
+  if (bad) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a batch member's reductions");
+  return QSF_OK;
+}
+
+int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_done) {
+  if (!b) return fail(QSF_EINVAL, "null argument");
+  auto it = b->members.find(slot);
+  if (it == b->members.end()) return fail(QSF_EINVAL, "unknown slot");
+  BatchMember& mb = it->second;
+  QSF_CU(cudaStreamSynchronize(b->stream));
+  long long ctl_h[8];
+  QSF_CU(cudaMemcpy(ctl_h, mb.g->ctl, sizeof(ctl_h), cudaMemcpyDeviceToHost));
+  const bool done = ctl_h[0] >= mb.nsteps || ctl_h[0] > ctl_h[1];
+  if (done && mb.normalize && !mb.scaled) {
+    k_scale<<<grid_blocks(mb.g->G.m), 256, 0, b->stream>>>(mb.g->G.psi, mb.g->G.m, mb.g->scale);
+    QSF_CU(cudaGetLastError());
+    QSF_CU(cudaStreamSynchronize(b->stream));
+    mb.scaled = true;
+  }
   if (rows)
-    QSF_CU(cudaMemcpyAsync(rows, g->rows_dev, (size_t)d->nsteps * ncol * sizeof(double), cudaMemcpyDeviceToHost,
-                           g->stream));
-  QSF_CU(cudaStreamSynchronize(g->stream));
+    QSF_CU(cudaMemcpy(rows, mb.g->rows_dev, (size_t)mb.nsteps * mb.ncol * sizeof(double), cudaMemcpyDeviceToHost));
   if (steps_done) *steps_done = ctl_h[2];
-  if (ctl_h[4]) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a step's reductions");
   return QSF_OK;
 }
 

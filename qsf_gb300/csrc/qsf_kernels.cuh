@@ -17,6 +17,9 @@
 //
 // For dim == 1 the whole step is one kernel (k_line_step) over a line held in
 // shared memory.  A device step counter lets one captured CUDA graph replay any step.
+// Step kernels read their grid and step descriptors from device arrays indexed by
+// blockIdx.y, so one launch per stage advances every solve of a batch that shares
+// the line length (a single grid is a batch of one).
 // FFT kernels are templates on the line length N (compile-time radix plan); the host
 // picks the instantiation for the grid's size.
 #pragma once
@@ -207,7 +210,9 @@ __global__ void k_build_static(GridDev g, int mode, double delta, double2* xs, d
 
 // Per-step tables: P phase per axis (velocity gauge A of this step; 1/m folded into
 // axis 0) and, in the length gauge, the x.E factors of both X halves.
-__global__ void k_tables(GridDev g, StepDev S) {
+__global__ void k_tables(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss) {
+  const GridDev& g = Gs[blockIdx.y];
+  const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   const long long step = S.ctl[0];
   const double* cp = S.coupling ? S.coupling + step * S.coup_stride : nullptr;
@@ -266,7 +271,9 @@ __device__ __forceinline__ double2 xfactor(const GridDev& g, const StepDev& S, l
 // ------------------------------------------------------------ row passes
 // Rows of the last axis: L rows of N points per block, contiguous in memory.
 template <int N>
-__global__ void __launch_bounds__(kRowThreads) k_row_open(GridDev g, StepDev S, int L) {
+__global__ void __launch_bounds__(kRowThreads) k_row_open(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss, int L) {
+  const GridDev& g = Gs[blockIdx.y];
+  const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   extern __shared__ double2 sm[];
   const AxisDev& a = g.ax[g.dim - 1];
@@ -292,7 +299,9 @@ __global__ void __launch_bounds__(kRowThreads) k_row_open(GridDev g, StepDev S, 
 }
 
 template <int N>
-__global__ void __launch_bounds__(kRowThreads) k_row_close(GridDev g, StepDev S, int L) {
+__global__ void __launch_bounds__(kRowThreads) k_row_close(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss, int L) {
+  const GridDev& g = Gs[blockIdx.y];
+  const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   extern __shared__ double2 sm[];
   __shared__ double red[32 * 3];
@@ -347,8 +356,11 @@ __global__ void __launch_bounds__(kRowThreads) k_row_close(GridDev g, StepDev S,
 // (o, c0) is psi[o * N * stride + i * stride + c0 + c].  Modes:
 //   0 forward, 1 inverse, 2 forward . P phase . inverse, 3 forward + E_kin partial
 template <int MODE, int N>
-__global__ void __launch_bounds__(kRowThreads) k_axis(GridDev g, StepDev S, int ax, int C) {
+__global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss, int ax, int C) {
+  const GridDev& g = Gs[blockIdx.y];
+  const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
+  if (MODE == 3 && !(S.obs & 4u)) return;
   extern __shared__ double2 sm[];
   __shared__ double red[32];
   __shared__ double2 pcol[64];
@@ -409,7 +421,9 @@ __global__ void __launch_bounds__(kRowThreads) k_axis(GridDev g, StepDev S, int 
 // ------------------------------------------------------------ 1D whole step
 // One block per line: X open . FFT . P . IFFT . X close . observables, line in smem.
 template <int N>
-__global__ void __launch_bounds__(kLineThreads) k_line_step(GridDev g, StepDev S) {
+__global__ void __launch_bounds__(kLineThreads) k_line_step(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss) {
+  const GridDev& g = Gs[blockIdx.y];
+  const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   extern __shared__ double2 sm[];
   __shared__ double red[32 * 3];
@@ -570,7 +584,9 @@ __global__ void __launch_bounds__(256) k_flux(GridDev g, const FluxPoint* fpts, 
 // deterministic reductions of all partials, Normalize scale and IM convergence.
 // Grid: nblk blocks; block b sums flux terms [b*chunk, (b+1)*chunk); the last block
 // to finish reduces everything in a fixed order and writes the observables row.
-__global__ void __launch_bounds__(256) k_finalize(GridDev g, StepDev S) {
+__global__ void __launch_bounds__(256) k_finalize(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss) {
+  const GridDev& g = Gs[blockIdx.y];
+  const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   __shared__ double red[32 * kMaxFluxBorders];
   __shared__ int is_last;
@@ -781,13 +797,13 @@ __global__ void k_add_gaussian(GridDev g, double at, double delta) {
 // ------------------------------------------------------------ per-size kernel table
 struct KernelSet {
   int n;
-  void (*row_open)(GridDev, StepDev, int);
-  void (*row_close)(GridDev, StepDev, int);
-  void (*axis_fwd)(GridDev, StepDev, int, int);
-  void (*axis_inv)(GridDev, StepDev, int, int);
-  void (*axis_fpi)(GridDev, StepDev, int, int);
-  void (*axis_ekin)(GridDev, StepDev, int, int);
-  void (*line_step)(GridDev, StepDev);
+  void (*row_open)(const GridDev*, const StepDev*, int);
+  void (*row_close)(const GridDev*, const StepDev*, int);
+  void (*axis_fwd)(const GridDev*, const StepDev*, int, int);
+  void (*axis_inv)(const GridDev*, const StepDev*, int, int);
+  void (*axis_fpi)(const GridDev*, const StepDev*, int, int);
+  void (*axis_ekin)(const GridDev*, const StepDev*, int, int);
+  void (*line_step)(const GridDev*, const StepDev*);
   void (*row_fft_f)(GridDev, int, double);
   void (*row_fft_b)(GridDev, int, double);
   void (*axis_fft_f)(GridDev, int, int, double);

@@ -11,7 +11,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from ._lib import GridDesc, StepDesc, MAX_BORDERS, check, lib
+from ._lib import GridDesc, KERNEL_KINDS, StepDesc, MAX_BORDERS, check, lib
 
 MODE_IM, MODE_RE = 1, 2
 REP_X, REP_P = 1, 2
@@ -132,10 +132,38 @@ class Grid:
         check(lib().qsf_add_gaussian(self._h, at, delta), "qsf_add_gaussian")
 
     # ------------------------------------------------------------ fused steps
+    def step_desc(self, mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None,
+                  obs: int = OBS_NORM, normalize: bool = False, borders: Sequence[str] = (), box_size: int = 0,
+                  state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0):
+        """A qsf_step_desc (and the coupling array it points to, which must stay alive)."""
+        d = StepDesc()
+        d.mode = mode
+        d.dt = dt
+        d.nsteps = int(nsteps)
+        cp = None
+        if coupling is not None:
+            cp = np.ascontiguousarray(coupling, dtype=np.float64)
+            d.coupling = _dp(cp)
+        d.obs = obs | (OBS_FLUX if borders else 0)
+        d.normalize = int(bool(normalize))
+        d.nborders = len(borders)
+        assert len(borders) <= MAX_BORDERS
+        for i, b in enumerate(borders):
+            d.border_types[i] = BORDERS[b]
+        d.box_size = int(box_size)
+        d.state_accuracy = state_accuracy
+        d.last_energy = last_energy
+        d.energy_after_normalize = int(energy_after_normalize)
+        return d, cp
+
     def step(self, mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None, obs: int = OBS_NORM,
              normalize: bool = False, borders: Sequence[str] = (), box_size: int = 0,
-             state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0):
-        """Run nsteps fused Strang steps; returns (rows [nsteps, 3 + nb], steps_done)."""
+             state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0,
+             profile: Optional[dict] = None):
+        """Run nsteps fused Strang steps; returns (rows [nsteps, 3 + nb], steps_done).
+
+        With `profile` (a dict), every launch is timed with CUDA events on the grid's
+        stream; per kernel kind the summed ms and launch counts are added to it."""
         d = StepDesc()
         d.mode = mode
         d.dt = dt
@@ -156,7 +184,17 @@ class Grid:
         d.energy_after_normalize = int(energy_after_normalize)
         rows = np.zeros((max(int(nsteps), 1), 3 + len(borders)), dtype=np.float64)
         done = ctypes.c_int64()
+        kms = kcnt = None
+        if profile is not None:
+            kms = (ctypes.c_float * len(KERNEL_KINDS))()
+            kcnt = (ctypes.c_int64 * len(KERNEL_KINDS))()
+            d.kernel_ms = kms
+            d.kernel_launches = kcnt
         check(lib().qsf_step(self._h, ctypes.byref(d), _dp(rows), ctypes.byref(done)), "qsf_step")
+        if profile is not None:
+            for i, k in enumerate(KERNEL_KINDS):
+                ms, cnt = profile.get(k, (0.0, 0))
+                profile[k] = (ms + float(kms[i]), cnt + int(kcnt[i]))
         del cp
         return rows[: int(nsteps)], int(done.value)
 
@@ -166,3 +204,49 @@ def fft_radices(n: int):
     c = ctypes.c_int()
     check(lib().qsf_fft_plan_radices(int(n), r, ctypes.byref(c)), "qsf_fft_plan_radices")
     return list(r)[: c.value]
+
+
+class Batch:
+    """qsf_batch: many independent grids advanced together, one launch per split stage
+    per (dim, line length) group, steps replayed from a captured CUDA graph."""
+
+    def __init__(self, stream: Optional[int] = None):
+        h = ctypes.c_void_p()
+        check(lib().qsf_batch_create(ctypes.c_void_p(stream or 0), ctypes.byref(h)), "qsf_batch_create")
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().qsf_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, grid: "Grid", mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None,
+            **kw) -> int:
+        d, cp = grid.step_desc(mode, dt, nsteps, coupling, **kw)
+        slot = ctypes.c_int64()
+        check(lib().qsf_batch_add(self._h, grid.handle, ctypes.byref(d), ctypes.byref(slot)), "qsf_batch_add")
+        self._keep[slot.value] = (grid, int(nsteps), 3 + d.nborders)
+        return slot.value
+
+    def remove(self, slot: int) -> None:
+        check(lib().qsf_batch_remove(self._h, int(slot)), "qsf_batch_remove")
+        self._keep.pop(slot, None)
+
+    def run(self, steps: int) -> int:
+        active = ctypes.c_int64()
+        check(lib().qsf_batch_run(self._h, int(steps), ctypes.byref(active)), "qsf_batch_run")
+        return int(active.value)
+
+    def result(self, slot: int):
+        grid, nsteps, ncol = self._keep[slot]
+        rows = np.zeros((nsteps, ncol), dtype=np.float64)
+        done = ctypes.c_int64()
+        check(lib().qsf_batch_result(self._h, int(slot), _dp(rows), ctypes.byref(done)), "qsf_batch_result")
+        return rows, int(done.value)
