@@ -212,6 +212,60 @@ int qsf_batch_run(qsf_batch* b, int64_t steps, int64_t* active);
 /* Observables rows (nsteps x (3 + nborders)) and steps done of one member. */
 int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_done);
 
+/* -------------------------------------------------------------- serving */
+/* A request loop with continuous batching: submitted solves wait in a queue, are
+ * admitted while a slot is free and enough HBM stays free, join the running batch
+ * between rounds of steps (their wavefunctions stay resident on the device for the
+ * whole solve), and leave it when their last step is done, returning yields, flux
+ * integrals and latencies.  No counterpart in the reference. */
+typedef struct qsf_request {
+  qsf_grid_desc grid;
+  int mode;                 /* QSF_MODE_RE or QSF_MODE_IM                               */
+  double dt;
+  int64_t nsteps;
+  const double* coupling;   /* nsteps x (3 | 6) rows as for qsf_step; copied at submit   */
+  const double* psi0;       /* initial wavefunction (host, m complex); copied at submit;
+                               NULL: gaussian(0, 1) normalised (wf/preset.h:5-10)          */
+  uint32_t obs;             /* QSF_OBS_* as for qsf_step                                  */
+  int nborders;
+  int border_types[QSF_MAX_BORDERS];
+  int64_t box_size;
+} qsf_request;
+
+typedef struct qsf_result {
+  int status;               /* QSF_OK or the error that ended the solve                   */
+  int64_t steps;            /* steps run                                                   */
+  double final_norm;        /* <psi|psi> dV after the last step                           */
+  double yield;             /* 1 - final_norm: probability absorbed at the grid edge       */
+  double final_epot;        /* <psi|V|psi> dV after the last step                          */
+  double flux_integral[QSF_MAX_BORDERS]; /* sum over steps of flux_b * dt                 */
+  double queue_s;           /* submit -> admission                                          */
+  double latency_s;         /* submit -> completion                                         */
+} qsf_result;
+
+typedef struct qsf_server_config {
+  int max_slots;            /* solves resident at once                                    */
+  double hbm_reserve_gb;    /* admission keeps at least this much device memory free      */
+  int64_t steps_per_round;  /* steps between admission / completion checks                */
+  int queue_capacity;       /* pending requests; submit returns QSF_EBUSY beyond it       */
+} qsf_server_config;
+
+typedef struct qsf_server_stats {
+  int64_t submitted, admitted, completed, queued, in_flight;
+  double grid_point_steps;  /* completed solves: sum of m * steps                          */
+} qsf_server_stats;
+
+typedef struct qsf_server qsf_server;
+int qsf_server_start(const qsf_server_config* cfg, qsf_server** out);
+int qsf_server_submit(qsf_server* s, const qsf_request* r, int64_t* ticket);
+/* non-blocking: *done = 1 and *out filled once the solve has finished */
+int qsf_server_poll(qsf_server* s, int64_t ticket, qsf_result* out, int* done);
+/* bounded wait for one solve; QSF_ETIMEDOUT when timeout_s runs out */
+int qsf_server_wait(qsf_server* s, int64_t ticket, double timeout_s, qsf_result* out);
+int qsf_server_stats_get(qsf_server* s, qsf_server_stats* out);
+/* finishes the solves in flight, drops the queued ones (status QSF_ESTATE), joins */
+int qsf_server_stop(qsf_server* s);
+
 /* ------------------------------------------------------------ diagnostics */
 /* last CUDA error text seen by the library (thread-local, never NULL) */
 const char* qsf_last_error(void);

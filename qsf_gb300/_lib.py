@@ -40,6 +40,54 @@ class GridDesc(ctypes.Structure):
     ]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [
+        ("grid", GridDesc),
+        ("mode", ctypes.c_int),
+        ("dt", ctypes.c_double),
+        ("nsteps", ctypes.c_int64),
+        ("coupling", ctypes.POINTER(ctypes.c_double)),
+        ("psi0", ctypes.POINTER(ctypes.c_double)),
+        ("obs", ctypes.c_uint32),
+        ("nborders", ctypes.c_int),
+        ("border_types", ctypes.c_int * MAX_BORDERS),
+        ("box_size", ctypes.c_int64),
+    ]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int),
+        ("steps", ctypes.c_int64),
+        ("final_norm", ctypes.c_double),
+        ("yield_", ctypes.c_double),
+        ("final_epot", ctypes.c_double),
+        ("flux_integral", ctypes.c_double * MAX_BORDERS),
+        ("queue_s", ctypes.c_double),
+        ("latency_s", ctypes.c_double),
+    ]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("max_slots", ctypes.c_int),
+        ("hbm_reserve_gb", ctypes.c_double),
+        ("steps_per_round", ctypes.c_int64),
+        ("queue_capacity", ctypes.c_int),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_int64),
+        ("admitted", ctypes.c_int64),
+        ("completed", ctypes.c_int64),
+        ("queued", ctypes.c_int64),
+        ("in_flight", ctypes.c_int64),
+        ("grid_point_steps", ctypes.c_double),
+    ]
+
+
 class StepDesc(ctypes.Structure):
     _fields_ = [
         ("mode", ctypes.c_int),
@@ -101,6 +149,12 @@ def lib():
         "qsf_batch_remove": [vp, i64],
         "qsf_batch_run": [vp, i64, ctypes.POINTER(i64)],
         "qsf_batch_result": [vp, i64, dp, ctypes.POINTER(i64)],
+        "qsf_server_start": [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)],
+        "qsf_server_submit": [vp, ctypes.POINTER(Request), ctypes.POINTER(i64)],
+        "qsf_server_poll": [vp, i64, ctypes.POINTER(Result), ip],
+        "qsf_server_wait": [vp, i64, ctypes.c_double, ctypes.POINTER(Result)],
+        "qsf_server_stats_get": [vp, ctypes.POINTER(ServerStats)],
+        "qsf_server_stop": [vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

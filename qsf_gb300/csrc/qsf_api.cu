@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -144,7 +145,9 @@ std::vector<KernelSet>& kernel_table() {
 }
 
 int init_kernel_table() {
+  static std::mutex mu;
   static bool done = false;
+  std::lock_guard<std::mutex> lk(mu);
   if (done) return QSF_OK;
   std::vector<KernelSet>& t = kernel_table();
   add_sizes_p2a(t);

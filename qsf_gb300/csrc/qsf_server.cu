@@ -1,0 +1,303 @@
+// qsf_server.cu -- request loop with continuous batching over the public C ABI.
+//
+// One worker thread owns all device work.  Each round it admits queued requests while
+// a slot is free and cudaMemGetInfo reports enough free HBM beyond the reserve
+// (creating the solve's grid, uploading or preparing its start state and adding it
+// to a qsf_batch), runs the batch for a fixed number of steps, and retires the
+// solves whose last step is done (results from their observables rows; grid freed).
+// Solves therefore join and leave the running batch between rounds while the others
+// keep their wavefunctions resident on the device.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "qsf_gpu.h"
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+
+struct Pending {
+  int64_t ticket;
+  qsf_request req;
+  std::vector<double> coupling;
+  std::vector<double> psi0;
+  clk::time_point submitted;
+};
+
+struct Running {
+  int64_t ticket;
+  qsf_grid* grid = nullptr;
+  int64_t slot = -1;
+  int64_t nsteps = 0;
+  int64_t remaining = 0;
+  int64_t m = 0;
+  int nb = 0;
+  double dt = 0.0;
+  std::vector<double> coupling;  // kept alive while in the batch
+  clk::time_point submitted, admitted;
+};
+
+int64_t grid_points(const qsf_grid_desc& d) {
+  int64_t m = 1;
+  for (int k = 0; k < d.dim; ++k) m *= d.n[k];
+  return m;
+}
+
+// device bytes a solve holds: psi, static X factor and potential, observables rows,
+// coupling rows, plus small tables
+size_t solve_bytes(const qsf_request& r) {
+  const int64_t m = grid_points(r.grid);
+  const int stride = r.grid.gauge == QSF_GAUGE_LENGTH ? 6 : 3;
+  return (size_t)m * (16 + 16 + 8) + (size_t)r.nsteps * (size_t)(3 + r.nborders + stride) * 8 + (1u << 20);
+}
+
+}  // namespace
+
+struct qsf_server {
+  qsf_server_config cfg{};
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Pending> queue;
+  std::map<int64_t, qsf_result> results;
+  std::map<int64_t, Running> running;
+  int64_t next_ticket = 1;
+  bool stopping = false;
+  std::thread worker;
+  qsf_batch* batch = nullptr;
+  qsf_server_stats stats{};
+};
+
+namespace {
+
+void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t steps) {
+  qsf_result res{};
+  res.status = status;
+  res.steps = steps;
+  if (rows && steps > 0) {
+    const int ncol = 3 + r.nb;
+    const double* last = rows + (steps - 1) * ncol;
+    res.final_norm = last[0];
+    res.final_epot = last[1];
+    res.yield = 1.0 - last[0];
+    for (int b = 0; b < r.nb; ++b) {
+      double acc = 0.0;
+      for (int64_t k = 0; k < steps; ++k) acc += rows[k * ncol + 3 + b] * r.dt;
+      res.flux_integral[b] = acc;
+    }
+  }
+  const auto now = clk::now();
+  res.queue_s = std::chrono::duration<double>(r.admitted - r.submitted).count();
+  res.latency_s = std::chrono::duration<double>(now - r.submitted).count();
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->results[r.ticket] = res;
+  s->stats.completed++;
+  s->stats.in_flight--;
+  if (status == QSF_OK) s->stats.grid_point_steps += (double)r.m * (double)steps;
+  s->cv_done.notify_all();
+}
+
+// admit one request: grid, start state, batch membership
+int admit(qsf_server* s, Pending& p, Running& r) {
+  qsf_grid* g = nullptr;
+  int rc = qsf_grid_create(&p.req.grid, nullptr, &g);
+  if (rc) return rc;
+  const int64_t m = grid_points(p.req.grid);
+  if (!p.psi0.empty()) {
+    rc = qsf_upload(g, p.psi0.data(), m);
+  } else {
+    rc = qsf_add_gaussian(g, 0.0, 1.0);
+    if (!rc) rc = qsf_normalize(g, nullptr);
+  }
+  if (rc) {
+    qsf_grid_destroy(g);
+    return rc;
+  }
+  r.ticket = p.ticket;
+  r.grid = g;
+  r.nsteps = p.req.nsteps;
+  r.remaining = p.req.nsteps;
+  r.m = m;
+  r.nb = (p.req.obs & QSF_OBS_FLUX) ? p.req.nborders : 0;
+  r.dt = p.req.dt;
+  r.coupling = std::move(p.coupling);
+  r.submitted = p.submitted;
+  r.admitted = clk::now();
+  qsf_step_desc d{};
+  d.mode = p.req.mode;
+  d.dt = p.req.dt;
+  d.nsteps = p.req.nsteps;
+  d.coupling = r.coupling.empty() ? nullptr : r.coupling.data();
+  d.obs = p.req.obs;
+  d.nborders = p.req.nborders;
+  for (int b = 0; b < QSF_MAX_BORDERS; ++b) d.border_types[b] = p.req.border_types[b];
+  d.box_size = p.req.box_size;
+  rc = qsf_batch_add(s->batch, g, &d, &r.slot);
+  if (rc) {
+    qsf_grid_destroy(g);
+    r.grid = nullptr;
+  }
+  return rc;
+}
+
+void worker_loop(qsf_server* s) {
+  std::vector<double> rows;
+  for (;;) {
+    // admission
+    std::vector<Pending> take;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      if (s->running.empty() && s->queue.empty()) {
+        if (s->stopping) break;
+        s->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+        continue;
+      }
+      size_t free_b = 0, total_b = 0;
+      cudaMemGetInfo(&free_b, &total_b);
+      const double reserve = s->cfg.hbm_reserve_gb * 1e9;
+      double budget = (double)free_b - reserve;
+      while (!s->queue.empty() && (int)(s->running.size() + take.size()) < s->cfg.max_slots) {
+        const double need = (double)solve_bytes(s->queue.front().req);
+        if (need > budget) break;
+        budget -= need;
+        take.push_back(std::move(s->queue.front()));
+        s->queue.pop_front();
+        s->stats.queued--;
+        s->stats.admitted++;
+        s->stats.in_flight++;
+      }
+    }
+    for (Pending& p : take) {
+      Running r;
+      r.ticket = p.ticket;
+      r.submitted = p.submitted;
+      r.admitted = clk::now();
+      const int rc = admit(s, p, r);
+      if (rc) {
+        finish(s, r, rc, nullptr, 0);
+        continue;
+      }
+      s->running.emplace(r.ticket, std::move(r));
+    }
+    if (s->running.empty()) continue;
+    // one round of steps for every resident solve
+    int64_t active = 0;
+    const int rc_run = qsf_batch_run(s->batch, s->cfg.steps_per_round, &active);
+    // retire finished solves
+    std::vector<int64_t> done;
+    for (auto& kv : s->running) {
+      kv.second.remaining -= s->cfg.steps_per_round;
+      if (kv.second.remaining <= 0 || rc_run) done.push_back(kv.first);
+    }
+    for (int64_t t : done) {
+      Running& r = s->running[t];
+      rows.assign((size_t)r.nsteps * (3 + r.nb), 0.0);
+      int64_t steps = 0;
+      int rc = rc_run ? rc_run : qsf_batch_result(s->batch, r.slot, rows.data(), &steps);
+      qsf_batch_remove(s->batch, r.slot);
+      qsf_grid_destroy(r.grid);
+      finish(s, r, rc, rows.data(), steps);
+      s->running.erase(t);
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int qsf_server_start(const qsf_server_config* cfg, qsf_server** out) {
+  if (!cfg || !out || cfg->max_slots < 1 || cfg->steps_per_round < 1 || cfg->queue_capacity < 1)
+    return QSF_EINVAL;
+  qsf_server* s = new qsf_server();
+  s->cfg = *cfg;
+  int rc = qsf_batch_create(nullptr, &s->batch);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  s->worker = std::thread(worker_loop, s);
+  *out = s;
+  return QSF_OK;
+}
+
+int qsf_server_submit(qsf_server* s, const qsf_request* r, int64_t* ticket) {
+  if (!s || !r || !ticket || r->nsteps < 1 || r->nborders < 0 || r->nborders > QSF_MAX_BORDERS) return QSF_EINVAL;
+  Pending p;
+  p.req = *r;
+  const int stride = r->grid.gauge == QSF_GAUGE_LENGTH ? 6 : 3;
+  if (r->coupling) p.coupling.assign(r->coupling, r->coupling + r->nsteps * stride);
+  if (r->psi0) p.psi0.assign(r->psi0, r->psi0 + 2 * grid_points(r->grid));
+  p.req.coupling = nullptr;
+  p.req.psi0 = nullptr;
+  p.submitted = clk::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stopping) return QSF_ESTATE;
+  if ((int)s->queue.size() >= s->cfg.queue_capacity) return QSF_EBUSY;
+  p.ticket = s->next_ticket++;
+  *ticket = p.ticket;
+  s->queue.push_back(std::move(p));
+  s->stats.submitted++;
+  s->stats.queued++;
+  s->cv_work.notify_one();
+  return QSF_OK;
+}
+
+int qsf_server_poll(qsf_server* s, int64_t ticket, qsf_result* out, int* done) {
+  if (!s || !out || !done) return QSF_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->results.find(ticket);
+  *done = it != s->results.end();
+  if (*done) *out = it->second;
+  return QSF_OK;
+}
+
+int qsf_server_wait(qsf_server* s, int64_t ticket, double timeout_s, qsf_result* out) {
+  if (!s || !out) return QSF_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  const auto until = clk::now() + std::chrono::duration<double>(timeout_s);
+  while (s->results.find(ticket) == s->results.end()) {
+    if (s->cv_done.wait_until(lk, until) == std::cv_status::timeout && s->results.find(ticket) == s->results.end())
+      return QSF_ETIMEDOUT;
+  }
+  *out = s->results[ticket];
+  return QSF_OK;
+}
+
+int qsf_server_stats_get(qsf_server* s, qsf_server_stats* out) {
+  if (!s || !out) return QSF_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  *out = s->stats;
+  return QSF_OK;
+}
+
+int qsf_server_stop(qsf_server* s) {
+  if (!s) return QSF_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stopping = true;
+    for (Pending& p : s->queue) {
+      qsf_result res{};
+      res.status = QSF_ESTATE;
+      s->results[p.ticket] = res;
+    }
+    s->stats.queued -= (int64_t)s->queue.size();
+    s->queue.clear();
+    s->cv_work.notify_all();
+    s->cv_done.notify_all();
+  }
+  if (s->worker.joinable()) s->worker.join();
+  qsf_batch_destroy(s->batch);
+  delete s;
+  return QSF_OK;
+}
+
+}  // extern "C"
