@@ -211,6 +211,127 @@ def cpu_baseline(all_cores: bool, budget_s: float = 20.0):
                       f"(wall clock incl. process start)"}
 
 
+# ------------------------------------------------------------------ batched / served
+BATCH_EDGES = [256, 384, 512, 768, 1024]
+SERVE_1D = [1024, 1280, 1536, 2048, 2560, 3072, 4096, 5120, 6144, 8192]
+SERVE_2D = [256, 320, 384, 512, 640, 768, 1024]
+
+
+def _gauss_state(dim, n, dx):
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    line = np.exp(-0.5 * x * x)
+    psi = line
+    for _ in range(dim - 1):
+        psi = np.multiply.outer(psi, line)
+    psi = psi.astype(np.complex128)
+    return psi / math.sqrt(float(np.sum(np.abs(psi) ** 2)) * dx ** dim)
+
+
+def _schedule(Q, dim, inten, lam, ncycles, nsteps):
+    c = Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field({1: 1, 2: 3}[dim], [Q.Pulse(field=Q.field_from_intensity(inten),
+                                                                          omega=Q.omega_from_wavelength(lam),
+                                                                          ncycles=ncycles)])])
+    rows = np.zeros((nsteps, 3))
+    timer = 0.0
+    for s in range(nsteps):
+        c.precalc(timer)
+        rows[s] = c.vector()
+        timer += DT * (1.0 * 1.0)
+    return rows
+
+
+def run_batched(steps, warmup, nsolves=256, seed=0):
+    """256 independent 2-electron solves, edges uniform over {256..1024}, intensity
+    log-uniform 1e14-1e15 W/cm^2, wavelength uniform 400-1600 nm, 3-cycle sin^2, VG,
+    advanced together through qsf_batch; grid-point-steps/s over `steps` steps."""
+    import torch
+    import qsf_gb300 as Q
+    rng = np.random.default_rng(seed)
+    edges = rng.choice(BATCH_EDGES, nsolves)
+    inten = 10.0 ** rng.uniform(14.0, 15.0, nsolves)
+    lam = rng.uniform(400.0, 1600.0, nsolves)
+    stream = torch.cuda.Stream()
+    batch = Q.Batch(stream=stream.cuda_stream)
+    grids, states = [], {}
+    total = warmup + steps
+    m_sum = 0
+    for e, I, L in zip(edges, inten, lam):
+        e = int(e)
+        g = Q.Grid(2, e, DX, nCAP=e // 10, potential=Q.POT_EBERLY, Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT,
+                   Esoft=ESOFT, gauge=Q.GAUGE_VELOCITY, n_fields=1)
+        if e not in states:
+            states[e] = _gauss_state(2, e, DX)
+        g.upload(states[e])
+        batch.add(g, Q.MODE_RE, DT, total, _schedule(Q, 2, I, L, NCYCLES, total), obs=Q.OBS_NORM | Q.OBS_EPOT,
+                  borders=Q.ZOA_FLUX_2D)
+        grids.append(g)
+        m_sum += e * e
+    batch.run(warmup)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    batch.run(steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    batch.close()
+    return {"value": m_sum * steps / (ms / 1e3), "unit": UNIT, "solves": nsolves, "steps": steps,
+            "ms_per_step": ms / steps, "grid_points": int(m_sum),
+            "workload": "batched: 256 2D solves, edges U{256,384,512,768,1024}, I log-U[1e14,1e15], "
+                        "lambda U[400,1600] nm, 3-cycle sin^2 VG, norm+E_pot+ZOA_FLUX_2D every step, seed 0"}
+
+
+def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128):
+    """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N in 1024..8192) and 2D
+    (edge in 256..1024) solves with seeded pulses; each solve runs its first
+    `steps_per_solve` steps.  Returns throughput and p50/p99 submit->completion."""
+    import qsf_gb300 as Q
+    from qsf_gb300 import serve as S
+    rng = np.random.default_rng(seed)
+    srv = S.Server(max_slots=max_slots, hbm_reserve_gb=16.0, steps_per_round=16)
+    tickets, pts = [], 0.0
+    t0 = time.perf_counter()
+    t_next = t0
+    states = {}
+    while True:
+        now = time.perf_counter()
+        if now - t0 >= duration_s:
+            break
+        if now < t_next:
+            time.sleep(min(t_next - now, 0.01))
+            continue
+        t_next += rng.exponential(1.0 / rate)
+        dim = 1 if rng.random() < 0.5 else 2
+        n = int(rng.choice(SERVE_1D if dim == 1 else SERVE_2D))
+        dx = 0.2 if dim == 1 else DX
+        inten = 10.0 ** rng.uniform(14.0, 15.0)
+        lam = rng.uniform(400.0, 1600.0)
+        gd = S.grid_desc(dim, n, dx, nCAP=n // 10, Ncharge=float(dim), gauge=Q.GAUGE_VELOCITY, n_fields=1)
+        key = (dim, n)
+        if key not in states:
+            states[key] = _gauss_state(dim, n, dx)
+        borders = ["BOX"] if dim == 1 else Q.ZOA_FLUX_2D
+        box = int(0.4 * n) if dim == 1 else 0
+        tickets.append(srv.submit(gd, Q.MODE_RE, DT, steps_per_solve,
+                                  _schedule(Q, dim, inten, lam, NCYCLES, steps_per_solve), psi0=states[key],
+                                  obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box))
+        pts += float(n ** dim) * steps_per_solve
+    lat = []
+    for t in tickets:
+        r = srv.wait(t, 3600)
+        if r["status"] == 0:
+            lat.append(r["latency_s"])
+    wall = time.perf_counter() - t0
+    srv.stop()
+    lat.sort()
+    pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
+    return {"rate_per_s": rate, "submitted": len(tickets), "completed": len(lat), "value": pts / wall, "unit": UNIT,
+            "p50_s": pct(0.50), "p99_s": pct(0.99), "wall_s": wall,
+            "workload": f"served: Poisson {rate}/s for {duration_s}s, 50/50 1D N in [1024,8192] / 2D edge in "
+                        f"[256,1024] (2^a 3^b 5^c sizes), I log-U[1e14,1e15], lambda U[400,1600] nm, "
+                        f"{steps_per_solve} steps per solve, seed {seed}"}
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args):
     ws, rank, local = _dist()
@@ -283,6 +404,9 @@ def run_gpu(args):
     traffic = _ncu_traffic(dom)
     launches = sum(v[1] for v in kinds.values())
 
+    batched = run_batched(steps=20, warmup=3)
+    served = run_served(rate=100.0, duration_s=3.0)
+
     if rank == 0:
         cpu = cpu_baseline(all_cores=False)
         line = {
@@ -306,6 +430,9 @@ def run_gpu(args):
             "hbm_gbs_step": BYTES_PER_PT_STEP * value / ws / 1e9,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "batched": batched,
+            "served": served,
+            "batched_vs_plain": batched["value"] / value * ws,
         }
         print(json.dumps(line))
     if ws > 1:
@@ -345,9 +472,21 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"])
+    ap.add_argument("--rates", default="10,30,100,300,1000")
+    ap.add_argument("--duration", type=float, default=5.0)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"metric": METRIC, **run_batched(args.steps, args.warmup)}))
+    elif args.workload == "served":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        for r in [float(v) for v in args.rates.split(",")]:
+            print(json.dumps({"metric": METRIC, **run_served(r, args.duration)}), flush=True)
     else:
         run_gpu(args)
 

@@ -1,0 +1,81 @@
+"""Run a few fused steps of one workload, for profilers (ncu) and quick timing.
+
+    python -m qsf_gb300.profile_step --workload 2d2048 --steps 3
+
+Workloads: 1d4096 (1 electron, length gauge, BOX flux), 2d2048 (2 electrons,
+velocity gauge, ZOA_FLUX_2D), 3d256 (3 electrons, length gauge, ZOA_FLUX_3D),
+2d1024.  Each starts from a normalised Gaussian and runs `steps` Strang steps with
+norm, E_pot and the workload's fluxes every step; prints the event-timed ms per step
+and the per-kernel split.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+
+import numpy as np
+
+WORKLOADS = {
+    # dim, n, dx, nCAP, Ncharge, gauge, intensity W/cm^2, wavelength nm, cycles, borders, box
+    "1d4096": (1, 4096, 0.2, 410, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 1638),
+    "2d1024": (2, 1024, 0.3, 102, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
+    "2d2048": (2, 2048, 0.3, 205, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
+    "3d256": (3, 256, 0.4, 26, 3.0, 1, 1e15, 800.0, 2.0, "ZOA_FLUX_3D", 0),
+}
+
+
+def make(workload: str):
+    import qsf_gb300 as Q
+    dim, n, dx, ncap, charge, gauge, inten, lam, cyc, borders, box = WORKLOADS[workload]
+    if isinstance(borders, str):
+        borders = getattr(Q, borders)
+    g = Q.Grid(dim, n, dx, nCAP=ncap, potential=Q.POT_EBERLY, Ncharge=charge, gauge=gauge, n_fields=1)
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    line = np.exp(-0.5 * x * x)
+    psi = line
+    for _ in range(dim - 1):
+        psi = np.multiply.outer(psi, line)
+    psi = psi.astype(np.complex128)
+    psi /= math.sqrt(float(np.sum(np.abs(psi) ** 2)) * dx ** dim)
+    g.upload(psi)
+    axis = {1: 1, 2: 3, 3: 7}[dim]
+    c = Q.Coupling(gauge, [Q.Field(axis, [Q.Pulse(field=Q.field_from_intensity(inten),
+                                                  omega=Q.omega_from_wavelength(lam), ncycles=cyc)])])
+    prop = Q.SplitPropagator(Q.MODE_RE, 0.05, 0, g, c, ["norm", "epot", ("flux", borders, box)])
+    return g, prop, borders, box
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="2d2048", choices=sorted(WORKLOADS))
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--ekin", action="store_true", help="also compute the kinetic energy every step")
+    ap.add_argument("--fourier", type=int, default=0, help="instead time this many forward+backward transforms")
+    args = ap.parse_args()
+    import time
+    import qsf_gb300 as Q
+    g, prop, borders, box = make(args.workload)
+    if args.fourier:
+        g.fourier(Q.REP_P)
+        g.fourier(Q.REP_X)
+        g.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.fourier):
+            g.fourier(Q.REP_P)
+            g.fourier(Q.REP_X)
+        g.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / args.fourier
+        print(json.dumps({"workload": args.workload, "fourier_pairs": args.fourier, "ms_per_pair": ms}))
+        return
+    obs = Q.OBS_NORM | Q.OBS_EPOT | (Q.OBS_EKIN if args.ekin else 0)
+    prof = {}
+    sched = prop._schedule(args.steps)
+    g.step(Q.MODE_RE, 0.05, args.steps, sched, obs=obs, borders=borders, box_size=box, profile=prof)
+    tot = sum(v[0] for v in prof.values())
+    print(json.dumps({"workload": args.workload, "steps": args.steps, "ms_per_step": tot / args.steps,
+                      "kernels_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[1]}}))
+
+
+if __name__ == "__main__":
+    main()
