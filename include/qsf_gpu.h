@@ -266,6 +266,22 @@ int qsf_server_stats_get(qsf_server* s, qsf_server_stats* out);
 /* finishes the solves in flight, drops the queued ones (status QSF_ESTATE), joins */
 int qsf_server_stop(qsf_server* s);
 
+/* ------------------------------------------------- norm without allocation */
+/* No counterpart in the reference.  For callers that cannot allocate device memory
+ * (a host program that hands out all device memory from its own pool, a language
+ * runtime that may only pass buffers it already owns across its foreign-function
+ * boundary): computes <psi|psi> dV of a complex128 wavefunction of m points that the
+ * caller holds on the device (psi_dev, interleaved re/im) and writes the one double
+ * into out_dev, a device buffer the caller owns.  Launches on `stream` (NULL: the
+ * default stream) and returns without waiting.  It allocates nothing: the per-block
+ * partial sums live in a fixed 64 KiB device array inside the library, which every
+ * GPU that loads the library holds until the process exits.  m may be at most
+ * 134,217,728 points; larger m returns QSF_EINVAL.  All calls share that array, so
+ * calls that overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's address (with that device current); make it
+ * before any stream capture. */
+int qsf_norm_noalloc(const double* psi_dev, int64_t m, double dV, double* out_dev, void* stream);
+
 /* ------------------------------------------------------------ diagnostics */
 /* last CUDA error text seen by the library (thread-local, never NULL) */
 const char* qsf_last_error(void);

@@ -73,6 +73,7 @@ constexpr int kMaxTile = 4096;          // points per block in row / axis passes
 }  // namespace
 
 namespace qsf {
+void set_error_message(const std::string& msg) { g_err = msg; }
 void add_sizes_p2a(std::vector<KernelSet>& out);
 void add_sizes_p2b(std::vector<KernelSet>& out);
 void add_sizes_r3(std::vector<KernelSet>& out);
