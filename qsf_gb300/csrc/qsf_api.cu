@@ -92,19 +92,28 @@ struct qsf_grid {
   bool own_stream = false;
   BorderNodes bn;
   std::vector<double2*> tw_owned;
+  std::vector<longlong2*> twx_owned;
   const KernelSet* ks = nullptr;  // kernels for this grid's line length
   GridDev* dG = nullptr;          // device copy of G (step kernels read descriptors from device arrays)
   StepDev* dS = nullptr;          // device copy of the current step descriptor
   // static tables
-  double2* xs = nullptr;
-  double* V = nullptr;
+  longlong2* xs = nullptr;
+  long long* Vx = nullptr;
   int xs_mode = 0;
   double xs_delta = 0.0;
+  int xs_exp = 0;
+  int vshift = 0;
+  double vmax = 0.0, vneg = 0.0;  // max V and max -V over the grid
   bool V_ready = false;
   // per-step tables
-  double2* ptab = nullptr;
-  double2* xdyn = nullptr;
+  longlong2* ptab = nullptr;
+  longlong2* xdyn = nullptr;
   int nmax = 0;
+  int l2m = 0;
+  double m_mant = 1.0;
+  // fixed-point pass bookkeeping: [kTexp] table exponents, [4] pass minima, [4][scmax] block exponents
+  int* ibuf = nullptr;
+  int scmax = 1;
   // reductions
   double* partials = nullptr;
   int pmax = 0;
@@ -183,10 +192,20 @@ int grid_blocks(long long m) {
   return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 16);
 }
 
+double decode_ordered(long long i) {
+  if (i < 0) i ^= 0x7fffffffffffffffLL;
+  double x;
+  std::memcpy(&x, &i, sizeof x);
+  return x;
+}
+
+// Static tables of X(delta) in fixed point.  The potential's range sets its
+// fixed-point scale (|V| * 2^vshift < 2^50) and, in imaginary time, the exponent taken
+// out of the X factor exp(-delta V) so that the stored factors stay <= 1.
 int ensure_static(qsf_grid* g, int mode, double delta) {
   const long long m = g->G.m;
-  if (!g->V) {
-    int rc = dev_alloc(g->V, (size_t)m);
+  if (!g->Vx) {
+    int rc = dev_alloc(g->Vx, (size_t)m);
     if (rc) return rc;
   }
   if (!g->xs) {
@@ -194,7 +213,37 @@ int ensure_static(qsf_grid* g, int mode, double delta) {
     if (rc) return rc;
   }
   if (g->xs_mode == mode && g->xs_delta == delta && g->V_ready) return QSF_OK;
-  k_build_static<<<grid_blocks(m), 256, 0, g->stream>>>(g->G, mode, delta, g->xs, g->V);
+  if (!g->V_ready) {
+    long long* rng = nullptr;
+    int rc = dev_alloc(rng, 2);
+    if (rc) return rc;
+    const long long init[2] = {-0x7fffffffffffffffLL - 1, -0x7fffffffffffffffLL - 1};
+    long long h[2];
+    cudaError_t ce = cudaMemcpyAsync(rng, init, sizeof init, cudaMemcpyHostToDevice, g->stream);
+    if (ce == cudaSuccess) {
+      k_vrange<<<grid_blocks(m), 256, 0, g->stream>>>(g->G, rng);
+      ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(h, rng, sizeof h, cudaMemcpyDeviceToHost, g->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(g->stream);
+    cudaFree(rng);
+    if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("potential range: ") + cudaGetErrorString(ce));
+    g->vmax = decode_ordered(h[0]);
+    g->vneg = decode_ordered(h[1]);
+    if (!std::isfinite(g->vmax) || !std::isfinite(g->vneg))
+      return fail(QSF_EINVAL, "the potential is not finite on the grid");
+    const double vabs = std::max(std::fabs(g->vmax), std::fabs(g->vneg));
+    int e = 0;
+    if (vabs > 0.0) std::frexp(vabs, &e);  // vabs < 2^e
+    g->vshift = 50 - e;
+  }
+  g->xs_exp = 0;
+  if (mode == QSF_MODE_IM && g->vneg > 0.0) {
+    const double fmax = std::exp(delta * g->vneg);
+    if (!std::isfinite(fmax)) return fail(QSF_EINVAL, "imaginary-time X factor overflows (dt * |V| too large)");
+    if (fmax > 1.0) std::frexp(fmax, &g->xs_exp);
+  }
+  k_build_static<<<grid_blocks(m), 256, 0, g->stream>>>(g->G, mode, delta, g->xs_exp, g->xs, g->Vx, g->vshift);
   QSF_CU(cudaGetLastError());
   g->xs_mode = mode;
   g->xs_delta = delta;
@@ -402,8 +451,7 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
     if ((rc = pf.end(kind))) return rc;     \
   } while (0)
   const int D = q.dim;
-  const int ntab = D * q.nmax * (q.gauge == 1 ? 3 : 1);
-  const dim3 gt(std::max(1, std::min(64, (ntab + 255) / 256)), count);
+  const dim3 gt(D * 3, count);  // one block per (kind, axis) table; X tables only in the length gauge
   QSF_TIMED(QSF_K_TABLES, (k_tables<<<gt, 256, 0, st>>>(dG, dS)));
   if (D == 1) {
     QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(1, count), kLineThreads, (size_t)q.n * sizeof(double2), st>>>(dG, dS)));
@@ -470,9 +518,17 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   S.coupling = coup;
   S.coup_stride = cstride;
   S.xs = g->xs;
-  S.V = g->V;
+  S.Vx = g->Vx;
   S.ptab = g->ptab;
   S.xdyn = g->xdyn;
+  S.xs_exp = g->xs_exp;
+  S.vshift = g->vshift;
+  S.l2m = g->l2m;
+  S.m_mant = g->m_mant;
+  S.texp = g->ibuf;
+  S.gmin = g->ibuf + kTexp;
+  S.sc = g->ibuf + kTexp + 4;
+  S.scmax = g->scmax;
   S.nmax = g->nmax;
   S.partials = g->partials;
   S.pmax = g->pmax;
@@ -693,6 +749,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     s *= d->n[k];
   }
   std::map<int64_t, double2*> tws;
+  std::map<int64_t, longlong2*> twxs;
   for (int k = 0; k < d->dim; ++k) {
     AxisDev& a = G.ax[k];
     a.n = (int)d->n[k];
@@ -706,22 +763,37 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     auto it = tws.find(a.n);
     if (it == tws.end()) {
       std::vector<double2> h((size_t)a.n);
+      std::vector<longlong2> hx((size_t)a.n);
       const long double twopi = 6.283185307179586476925286766559005768L;
+      const long double q62 = 4611686018427387904.0L;
       for (int t = 0; t < a.n; ++t) {
         const long double ang = twopi * (long double)t / (long double)a.n;
-        h[(size_t)t] = make_double2((double)cosl(ang), -(double)sinl(ang));
+        const long double c = cosl(ang), sn = -sinl(ang);
+        h[(size_t)t] = make_double2((double)c, (double)sn);
+        hx[(size_t)t] = make_longlong2(llroundl(c * q62), llroundl(sn * q62));
       }
       double2* dptr = nullptr;
+      longlong2* xptr = nullptr;
       if (int rc = dev_alloc(dptr, h.size())) {
         qsf_grid_destroy(g);
         return rc;
       }
+      if (int rc = dev_alloc(xptr, hx.size())) {
+        cudaFree(dptr);
+        qsf_grid_destroy(g);
+        return rc;
+      }
       cudaMemcpy(dptr, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice);
+      cudaMemcpy(xptr, hx.data(), hx.size() * sizeof(longlong2), cudaMemcpyHostToDevice);
       g->tw_owned.push_back(dptr);
+      g->twx_owned.push_back(xptr);
       tws[a.n] = dptr;
+      twxs[a.n] = xptr;
       a.tw = dptr;
+      a.twx = xptr;
     } else {
       a.tw = it->second;
+      a.twx = twxs[a.n];
     }
   }
   G.inv_m = 1.0 / (double)G.m;
@@ -769,7 +841,13 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   g->nmax = 0;
   for (int k = 0; k < D; ++k) g->nmax = std::max(g->nmax, G.ax[k].n);
   g->pmax = std::max({g->nrowblk, g->ax_blocks[0], g->ax_blocks[1], g->ax_blocks[2], 256});
-  if ((rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)2 * D * g->nmax)) ||
+  g->scmax = std::max({g->nrowblk, g->ax_blocks[0], g->ax_blocks[1], g->ax_blocks[2], 1});
+  // 1/m = m_mant * 2^-l2m with m_mant in (0.5, 1]
+  g->l2m = 0;
+  while ((1LL << (g->l2m + 1)) <= G.m) ++g->l2m;
+  g->m_mant = std::ldexp(1.0, g->l2m) / (double)G.m;
+  if ((rc = dev_alloc(g->ibuf, (size_t)kTexp + 4 + 4 * (size_t)g->scmax)) ||
+      (rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)2 * D * g->nmax)) ||
       (rc = dev_alloc(g->partials, (size_t)5 * g->pmax)) || (rc = dev_alloc(g->ctl, 8)) ||
       (rc = dev_alloc(g->energy, 2)) || (rc = dev_alloc(g->scale, 2)) ||
       (rc = dev_alloc(g->fpartials, (size_t)64 * kMaxFluxBorders)) || (rc = dev_alloc(g->dG, 1)) ||
@@ -796,8 +874,10 @@ int qsf_grid_destroy(qsf_grid* g) {
   };
   fr(g->G.psi);
   for (double2* t : g->tw_owned) fr(t);
+  for (longlong2* t : g->twx_owned) fr(t);
   fr(g->xs);
-  fr(g->V);
+  fr(g->Vx);
+  fr(g->ibuf);
   fr(g->ptab);
   fr(g->xdyn);
   fr(g->partials);

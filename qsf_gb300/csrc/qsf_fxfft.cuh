@@ -1,0 +1,327 @@
+// qsf_fxfft.cuh -- block-fixed-point (int64) Stockham FFT for sm_103a.
+//
+// GB300 issues about 2 FP64 instructions per clock per SM but ~128 integer
+// instructions, so the split step's FFTs run on the integer pipes: a line (or a tile
+// of lines) is held as 64-bit integers sharing one power-of-two block exponent,
+// value = int * 2^-scale.  Additions are exact; products by twiddles and butterfly
+// constants are 64 x 64 -> 128-bit products rounded back to 64 bits (constants carry
+// 62 fractional bits).  After every radix pass the block is renormalised so that its
+// largest component again uses all bits the next pass can afford (62 minus the pass's
+// growth), i.e. block floating point with a 55-60 bit mantissa at every pass.  Against
+// an exact DFT this is ~4x more accurate than an FP64 FFT (normwise relative error
+// ~5e-17 vs ~2e-16 at N = 48 .. 4096); FP64 storage of psi is unchanged.
+//
+// Radix plans, pass structure and index maps are those of qsf_fft.cuh.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qsf_fft.cuh"
+
+namespace qsf {
+
+typedef long long i64;
+typedef unsigned long long u64;
+
+// round(a * w / 2^62)
+__device__ __forceinline__ i64 mulq62(i64 a, i64 w) {
+  const i64 hi = __mul64hi(a, w);
+  const u64 lo = (u64)a * (u64)w;
+  return (i64)(((u64)hi << 2) | (lo >> 62)) + (i64)((lo >> 61) & 1ull);
+}
+// round(a * w / 2^60): phase-table factors (|w| < 4)
+__device__ __forceinline__ i64 mulq60(i64 a, i64 w) {
+  const i64 hi = __mul64hi(a, w);
+  const u64 lo = (u64)a * (u64)w;
+  return (i64)(((u64)hi << 4) | (lo >> 60)) + (i64)((lo >> 59) & 1ull);
+}
+
+__device__ __forceinline__ longlong2 fadd(longlong2 a, longlong2 b) { return make_longlong2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ longlong2 fsub(longlong2 a, longlong2 b) { return make_longlong2(a.x - b.x, a.y - b.y); }
+// a * w with w in 2^62 fixed point (|w| <= 1)
+__device__ __forceinline__ longlong2 fmul62(longlong2 a, longlong2 w) {
+  return make_longlong2(mulq62(a.x, w.x) - mulq62(a.y, w.y), mulq62(a.x, w.y) + mulq62(a.y, w.x));
+}
+// a * conj(w)
+__device__ __forceinline__ longlong2 fmul62c(longlong2 a, longlong2 w) {
+  return make_longlong2(mulq62(a.x, w.x) + mulq62(a.y, w.y), mulq62(a.y, w.x) - mulq62(a.x, w.y));
+}
+// a * w with w in 2^60 fixed point (|w| < 4)
+__device__ __forceinline__ longlong2 fmul60(longlong2 a, longlong2 w) {
+  return make_longlong2(mulq60(a.x, w.x) - mulq60(a.y, w.y), mulq60(a.x, w.y) + mulq60(a.y, w.x));
+}
+template <bool FWD> __device__ __forceinline__ longlong2 fmul_si(longlong2 a) {
+  return FWD ? make_longlong2(a.y, -a.x) : make_longlong2(-a.y, a.x);
+}
+
+// butterfly constants in 2^62 fixed point
+#define QSF_FX_SQRT1_2 3260954456333195553LL   /* round(2^62 / sqrt(2)) */
+#define QSF_FX_SQRT3_2 3993837246235628775LL   /* round(2^62 * sqrt(3)/2) */
+#define QSF_FX_HALF 2305843009213693952LL      /* 2^61 */
+#define QSF_FX_C5_1 1425089352415399811LL      /* round(2^62 * cos(2pi/5)) */
+#define QSF_FX_C5_2 (-3730932361629093763LL)   /* round(2^62 * cos(4pi/5)) */
+#define QSF_FX_S5_1 4385974038932618941LL      /* round(2^62 * sin(2pi/5)) */
+#define QSF_FX_S5_2 2710681029835013083LL      /* round(2^62 * sin(4pi/5)) */
+#define QSF_FX_C16_1 4260642322793532497LL     /* round(2^62 * cos(pi/8)) */
+#define QSF_FX_S16_1 1764815834521887442LL     /* round(2^62 * sin(pi/8)) */
+
+template <bool FWD> __device__ __forceinline__ void fbfly2(longlong2& a, longlong2& b) {
+  const longlong2 t = a;
+  a = fadd(t, b);
+  b = fsub(t, b);
+}
+template <bool FWD>
+__device__ __forceinline__ void fbfly4(longlong2& x0, longlong2& x1, longlong2& x2, longlong2& x3) {
+  const longlong2 t0 = fadd(x0, x2), t1 = fsub(x0, x2), t2 = fadd(x1, x3), t3 = fmul_si<FWD>(fsub(x1, x3));
+  x0 = fadd(t0, t2);
+  x2 = fsub(t0, t2);
+  x1 = fadd(t1, t3);
+  x3 = fsub(t1, t3);
+}
+// w8^1 * a and w8^3 * a, w8 = exp(sign 2 pi i / 8)
+template <bool FWD> __device__ __forceinline__ longlong2 fw8_1(longlong2 a) {
+  return FWD ? make_longlong2(mulq62(a.x + a.y, QSF_FX_SQRT1_2), mulq62(a.y - a.x, QSF_FX_SQRT1_2))
+             : make_longlong2(mulq62(a.x - a.y, QSF_FX_SQRT1_2), mulq62(a.x + a.y, QSF_FX_SQRT1_2));
+}
+template <bool FWD> __device__ __forceinline__ longlong2 fw8_3(longlong2 a) {
+  return FWD ? make_longlong2(mulq62(a.y - a.x, QSF_FX_SQRT1_2), -mulq62(a.x + a.y, QSF_FX_SQRT1_2))
+             : make_longlong2(-mulq62(a.x + a.y, QSF_FX_SQRT1_2), mulq62(a.x - a.y, QSF_FX_SQRT1_2));
+}
+template <bool FWD> __device__ __forceinline__ void fbfly8(longlong2* v) {
+  longlong2 a0 = fadd(v[0], v[4]), a4 = fsub(v[0], v[4]);
+  longlong2 a1 = fadd(v[1], v[5]), a5 = fsub(v[1], v[5]);
+  longlong2 a2 = fadd(v[2], v[6]), a6 = fsub(v[2], v[6]);
+  longlong2 a3 = fadd(v[3], v[7]), a7 = fsub(v[3], v[7]);
+  a5 = fw8_1<FWD>(a5);
+  a6 = fmul_si<FWD>(a6);
+  a7 = fw8_3<FWD>(a7);
+  fbfly4<FWD>(a0, a1, a2, a3);
+  fbfly4<FWD>(a4, a5, a6, a7);
+  v[0] = a0; v[4] = a2; v[2] = a1; v[6] = a3;
+  v[1] = a4; v[5] = a6; v[3] = a5; v[7] = a7;
+}
+template <bool FWD> __device__ __forceinline__ void fbfly3(longlong2* v) {
+  const longlong2 t1 = fadd(v[1], v[2]), t2 = fsub(v[1], v[2]);
+  // m1 = v0 - t1/2 ; X1 = m1 + i k t2, X2 = m1 - i k t2, k = sign * sqrt(3)/2
+  const longlong2 m1 = make_longlong2(v[0].x - mulq62(t1.x, QSF_FX_HALF), v[0].y - mulq62(t1.y, QSF_FX_HALF));
+  const i64 kx = mulq62(t2.x, QSF_FX_SQRT3_2), ky = mulq62(t2.y, QSF_FX_SQRT3_2);
+  v[0] = fadd(v[0], t1);
+  if (FWD) {  // k = -sqrt3/2
+    v[1] = make_longlong2(m1.x + ky, m1.y - kx);
+    v[2] = make_longlong2(m1.x - ky, m1.y + kx);
+  } else {
+    v[1] = make_longlong2(m1.x - ky, m1.y + kx);
+    v[2] = make_longlong2(m1.x + ky, m1.y - kx);
+  }
+}
+template <bool FWD> __device__ __forceinline__ void fbfly5(longlong2* v) {
+  const longlong2 t1 = fadd(v[1], v[4]), t2 = fadd(v[2], v[3]), t3 = fsub(v[1], v[4]), t4 = fsub(v[2], v[3]);
+  const longlong2 x0 = v[0];
+  const longlong2 a1 = make_longlong2(x0.x + mulq62(t1.x, QSF_FX_C5_1) + mulq62(t2.x, QSF_FX_C5_2),
+                                      x0.y + mulq62(t1.y, QSF_FX_C5_1) + mulq62(t2.y, QSF_FX_C5_2));
+  const longlong2 a2 = make_longlong2(x0.x + mulq62(t1.x, QSF_FX_C5_2) + mulq62(t2.x, QSF_FX_C5_1),
+                                      x0.y + mulq62(t1.y, QSF_FX_C5_2) + mulq62(t2.y, QSF_FX_C5_1));
+  // b1 = s1 t3 + s2 t4, b2 = s2 t3 - s1 t4 with s = sign * sin
+  longlong2 b1 = make_longlong2(mulq62(t3.x, QSF_FX_S5_1) + mulq62(t4.x, QSF_FX_S5_2),
+                                mulq62(t3.y, QSF_FX_S5_1) + mulq62(t4.y, QSF_FX_S5_2));
+  longlong2 b2 = make_longlong2(mulq62(t3.x, QSF_FX_S5_2) - mulq62(t4.x, QSF_FX_S5_1),
+                                mulq62(t3.y, QSF_FX_S5_2) - mulq62(t4.y, QSF_FX_S5_1));
+  if (FWD) {
+    b1 = make_longlong2(-b1.x, -b1.y);
+    b2 = make_longlong2(-b2.x, -b2.y);
+  }
+  v[0] = make_longlong2(x0.x + t1.x + t2.x, x0.y + t1.y + t2.y);
+  v[1] = make_longlong2(a1.x - b1.y, a1.y + b1.x);
+  v[4] = make_longlong2(a1.x + b1.y, a1.y - b1.x);
+  v[2] = make_longlong2(a2.x - b2.y, a2.y + b2.x);
+  v[3] = make_longlong2(a2.x + b2.y, a2.y - b2.x);
+}
+// multiply by (c + i sign s) in 2^62 fixed point
+template <bool FWD> __device__ __forceinline__ longlong2 frot(longlong2 a, i64 c, i64 s) {
+  const i64 ss = FWD ? -s : s;
+  return make_longlong2(mulq62(a.x, c) - mulq62(a.y, ss), mulq62(a.x, ss) + mulq62(a.y, c));
+}
+template <bool FWD> __device__ __forceinline__ void fbfly16(longlong2* v) {
+  longlong2 a[16];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    longlong2 x0 = v[r], x1 = v[r + 4], x2 = v[r + 8], x3 = v[r + 12];
+    fbfly4<FWD>(x0, x1, x2, x3);
+    a[r * 4 + 0] = x0;
+    a[r * 4 + 1] = x1;
+    a[r * 4 + 2] = x2;
+    a[r * 4 + 3] = x3;
+  }
+  a[1 * 4 + 1] = frot<FWD>(a[1 * 4 + 1], QSF_FX_C16_1, QSF_FX_S16_1);    // w^1
+  a[1 * 4 + 2] = fw8_1<FWD>(a[1 * 4 + 2]);                              // w^2
+  a[1 * 4 + 3] = frot<FWD>(a[1 * 4 + 3], QSF_FX_S16_1, QSF_FX_C16_1);    // w^3
+  a[2 * 4 + 1] = fw8_1<FWD>(a[2 * 4 + 1]);                              // w^2
+  a[2 * 4 + 2] = fmul_si<FWD>(a[2 * 4 + 2]);                            // w^4
+  a[2 * 4 + 3] = fw8_3<FWD>(a[2 * 4 + 3]);                              // w^6
+  a[3 * 4 + 1] = frot<FWD>(a[3 * 4 + 1], QSF_FX_S16_1, QSF_FX_C16_1);    // w^3
+  a[3 * 4 + 2] = fw8_3<FWD>(a[3 * 4 + 2]);                              // w^6
+  a[3 * 4 + 3] = frot<FWD>(a[3 * 4 + 3], -QSF_FX_C16_1, -QSF_FX_S16_1);  // w^9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    longlong2 x0 = a[0 * 4 + k1], x1 = a[1 * 4 + k1], x2 = a[2 * 4 + k1], x3 = a[3 * 4 + k1];
+    fbfly4<FWD>(x0, x1, x2, x3);
+    v[k1 + 0] = x0;
+    v[k1 + 4] = x1;
+    v[k1 + 8] = x2;
+    v[k1 + 12] = x3;
+  }
+}
+template <int R, bool FWD> __device__ __forceinline__ void fbfly(longlong2* v) {
+  if constexpr (R == 2) fbfly2<FWD>(v[0], v[1]);
+  else if constexpr (R == 3) fbfly3<FWD>(v);
+  else if constexpr (R == 4) fbfly4<FWD>(v[0], v[1], v[2], v[3]);
+  else if constexpr (R == 5) fbfly5<FWD>(v);
+  else if constexpr (R == 8) fbfly8<FWD>(v);
+  else if constexpr (R == 16) fbfly16<FWD>(v);
+}
+
+// bit length of |x| (0 for x == 0)
+__device__ __forceinline__ int fbits(i64 x) {
+  const u64 a = (u64)(x < 0 ? -x : x);
+  return 64 - __clzll((long long)a);
+}
+// x * 2^sh with rounding (sh < 0: arithmetic right shift, round half up)
+__device__ __forceinline__ i64 fshift(i64 x, int sh) {
+  if (sh >= 0) return x << sh;
+  const int r = -sh;
+  if (r >= 63) return 0;
+  return (x + ((i64)1 << (r - 1))) >> r;
+}
+// guard bits a radix-R pass needs above the block maximum (growth <= R * sqrt(2))
+__host__ __device__ constexpr int fguard(int r) { return r == 16 ? 5 : r == 8 ? 4 : r == 5 ? 4 : r == 4 ? 3 : r == 3 ? 3 : 2; }
+
+// Block-wide max of per-thread values (smem needs 32 ints); result returned to all.
+__device__ __forceinline__ int block_max_int(int v, int* red) {
+  v = __reduce_max_sync(0xffffffffu, (unsigned)v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  int m = 0;
+  for (int w = 0; w < nw; ++w) m = max(m, red[w]);
+  __syncthreads();
+  return m;
+}
+
+// One in-place Stockham pass in fixed point.  Inputs are scaled by 2^shift_in on
+// load; returns (via bits_out, valid in every thread after the call) the bit length
+// of the largest output component in the block.
+template <int R, bool FWD, int MAXB, int N, int NS>
+__device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const LineSet& L,
+                                           const longlong2* __restrict__ tw, int tid, int nth, int shift_in, int* red) {
+  constexpr int nr = N / R;
+  constexpr int twstep = N / (NS * R);
+  const int total = nr * L.nlines;
+  longlong2 v[MAXB][R];
+  int dsto[MAXB];
+#pragma unroll
+  for (int b = 0; b < MAXB; ++b) {
+    const int w = tid + b * nth;
+    dsto[b] = -1;
+    if (w < total) {
+      int line, j;
+      if (L.line_fastest) {
+        line = w % L.nlines;
+        j = w / L.nlines;
+      } else {
+        j = w % nr;
+        line = w / nr;
+      }
+      const longlong2* src = buf + line * L.ls;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        longlong2 x = src[(j + q * nr) * L.es];
+        if (shift_in) x = make_longlong2(fshift(x.x, shift_in), fshift(x.y, shift_in));
+        v[b][q] = x;
+      }
+      const int jm = j % NS;
+      if constexpr (NS > 1) {
+#pragma unroll
+        for (int q = 1; q < R; ++q) {
+          const longlong2 t = tw[jm * q * twstep];
+          v[b][q] = FWD ? fmul62(v[b][q], t) : fmul62c(v[b][q], t);
+        }
+      }
+      dsto[b] = line * L.ls + ((j - jm) * R + jm) * L.es;
+    }
+  }
+  __syncthreads();
+  int mb = 0;
+#pragma unroll
+  for (int b = 0; b < MAXB; ++b) {
+    if (dsto[b] >= 0) {
+      fbfly<R, FWD>(v[b]);
+      longlong2* dst = buf + dsto[b];
+      const int st = NS * L.es;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        dst[q * st] = v[b][q];
+        mb = max(mb, max(fbits(v[b][q].x), fbits(v[b][q].y)));
+      }
+    }
+  }
+  return block_max_int(mb, red);  // includes the barrier that ends the pass
+}
+
+// Full fixed-point transform of every line of the set, in place.  On entry the data
+// have block exponent `scale` (value = int * 2^-scale) and fit the first pass's
+// guard; on return `scale` is the exponent of the output and its largest component
+// has bit length `bits`.  Requires nlines * N <= 16 * nth.
+template <int N, bool FWD, int S = 0>
+__device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw, int tid,
+                                       int nth, int& scale, int& bits, int* red, int shift_in = 0) {
+  if constexpr (S < nstages(N)) {
+    constexpr int R = radix_at(N, S);
+    bits = fx_stockham<R, FWD, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red);
+    if constexpr (S + 1 < nstages(N)) {
+      // renormalise for the next pass: largest component < 2^(62 - guard(next))
+      const int target = 62 - fguard(radix_at(N, S + 1));
+      const int sh = bits == 0 ? 0 : target - bits;
+      scale += sh;
+      fft_fx<N, FWD, S + 1>(buf, L, tw, tid, nth, scale, bits, red, sh);
+    }
+  }
+}
+
+// Exponent bits of a double's magnitude (0 for 0 / denormals)
+__device__ __forceinline__ int dexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+
+// round(x * 2^s) as int64 using integer operations only (x finite, result < 2^63)
+__device__ __forceinline__ i64 d2fx(double x, int s) {
+  const u64 b = (u64)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0) return 0;  // zero or denormal: below any representable fixed-point step here
+  const u64 m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int sh = e - 1075 + s;  // x * 2^s = m * 2^sh
+  i64 r;
+  if (sh >= 0) r = (i64)(m << sh);
+  else if (sh <= -64) r = 0;
+  else r = (i64)((m + (1ull << (-sh - 1))) >> (-sh));
+  return (b >> 63) ? -r : r;
+}
+// x * 2^-s as a double (round to nearest even), integer operations only
+__device__ __forceinline__ double fx2d(i64 x, int s) {
+  if (x == 0) return 0.0;
+  const u64 sign = x < 0 ? 0x8000000000000000ull : 0ull;
+  u64 a = (u64)(x < 0 ? -x : x);
+  const int lz = __clzll((long long)a);
+  a <<= lz;  // top bit set: value = a * 2^(63 - lz - 63)
+  u64 mant = a >> 11;
+  const u64 rem = a & 0x7ffull;
+  int e = (63 - lz) - s + 1023;  // exponent of the leading bit
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) {
+    ++mant;
+    if (mant >> 53) {
+      mant >>= 1;
+      ++e;
+    }
+  }
+  if (e <= 0) return 0.0;  // underflow below the normal range: negligible here
+  return __longlong_as_double((long long)(sign | ((u64)e << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+}  // namespace qsf

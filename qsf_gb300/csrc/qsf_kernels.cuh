@@ -22,8 +22,18 @@
 // the line length (a single grid is a batch of one).
 // FFT kernels are templates on the line length N (compile-time radix plan); the host
 // picks the instantiation for the grid's size.
+//
+// Arithmetic: psi is stored as complex128 between steps; inside a step every pass
+// works in block fixed point (int64 components sharing one power-of-two exponent per
+// thread block, qsf_fxfft.cuh), because GB300's integer pipes issue ~64x more
+// instructions per clock than its FP64 pipe.  Intermediate passes write int64 pairs
+// into psi's own buffer together with their block exponents; the next pass aligns every
+// element to the smallest exponent of the producing pass.  Phase tables are stored in
+// 2^62 fixed point with magnitude <= 1.  Norm and E_pot partials are exact 128-bit
+// integer sums per block.
 #pragma once
 #include "qsf_fft.cuh"
+#include "qsf_fxfft.cuh"
 
 namespace qsf {
 
@@ -36,7 +46,8 @@ struct AxisDev {
   int n, n2;
   long long stride;
   double dx, xmin, dp, inv_2dx;
-  const double2* tw;  // exp(-2 pi i t / n), t < n
+  const double2* tw;     // exp(-2 pi i t / n), t < n
+  const longlong2* twx;  // the same twiddles in 2^62 fixed point
 };
 
 struct GridDev {
@@ -70,10 +81,18 @@ struct StepDev {
   long long nsteps;
   const double* coupling;  // device copy of the per-step coupling rows (may be null)
   int coup_stride;         // 3 (velocity gauge) or 6 (length gauge)
-  const double2* xs;       // static X half-step factor per point (dt/2, incl. absorber)
-  const double* V;         // potential per point
-  double2* ptab;           // [dim][nmax] P-phase tables of the current step
-  double2* xdyn;           // [2][dim][nmax] length-gauge factors: open half, close half
+  const longlong2* xs;     // static X half-step factor per point (dt/2, incl. absorber), 2^62 fixed, * 2^-xs_exp
+  const long long* Vx;     // potential per point in 2^vshift fixed point
+  longlong2* ptab;         // [dim][nmax] P-phase tables of the current step (2^62 fixed, |.| <= 1)
+  longlong2* xdyn;         // [2][dim][nmax] length-gauge factors: open half, close half
+  int xs_exp;              // exponent taken out of xs (imaginary time: factors above 1)
+  int vshift;              // Vx = round(V * 2^vshift)
+  int l2m;                 // 1/m = m_mant * 2^-l2m, m_mant in (0.5, 1] (folded into axis 0's P table)
+  double m_mant;
+  int* texp;               // [3][3] exponents taken out of the per-step tables (set by k_tables)
+  int* gmin;               // [4] minimum block exponent of each fixed-point pass of the step
+  int* sc;                 // [4][scmax] block exponents of each fixed-point pass
+  int scmax;
   int nmax;
   // reductions
   double* partials;  // [5][pmax]: norm, epot, ekin axis 0..2
@@ -188,10 +207,101 @@ __device__ __forceinline__ double2 expop(int mode, double val) {
   return make_double2(cs, sn);
 }
 
+// ------------------------------------------------------------ fixed-point helpers
+// Rows per block of the last-axis passes and columns per tile of the strided-axis
+// passes are compile-time functions of the line length (<= kMaxTile points per block),
+// so a consumer pass finds the block that produced an element with a few integer ops.
+__host__ __device__ constexpr int row_lines(int n) { return n >= 4096 ? 1 : 4096 / n; }
+__host__ __device__ constexpr int tile_cols(int n) { return (4096 / n) < 64 ? (4096 / n) : 64; }
+
+// Passes that leave the wavefunction in fixed point inside a step; each block of a
+// pass records its exponent in sc[pass][block] and the pass minimum in gmin[pass]:
+// 0 last-axis rows (open), 1 axis-1 tiles forward (3D), 2 axis-0 tiles, 3 axis-1
+// tiles inverse (3D).  The next pass aligns every element to gmin of its producer.
+template <int N>
+__device__ __forceinline__ int producer_block(int pass, int dim, long long p) {
+  if (pass == 0) return (int)((p / N) / row_lines(N));
+  if (pass == 2) {  // axis 0: a single outer index, inner = m / N
+    const long long inner = dim == 2 ? (long long)N : (long long)N * N;
+    const long long C = tile_cols(N) < inner ? tile_cols(N) : inner;
+    return (int)((p % inner) / C);
+  }
+  // axis 1 of a 3D grid: outer index i0, inner = N
+  constexpr long long C = tile_cols(N) < N ? tile_cols(N) : N;
+  constexpr long long tpo = (N + C - 1) / C;
+  const long long o = p / ((long long)N * N);
+  return (int)(o * tpo + (p % N) / C);
+}
+
+// Exponent bookkeeping of the step's fixed-point tables: every table is stored with
+// magnitude <= 1 in 2^62 fixed point; a table whose exact values exceed 1 (imaginary
+// time) is stored times 2^-e and e is added back to the block exponent.
+//   texp[0][d]: P table of axis d, texp[1][d] / texp[2][d]: length-gauge X tables of
+//   axis d (open / close half).  The static X table's exponent is StepDev::xs_exp.
+constexpr int kTexp = 9;
+
+// sum |x|^2 and sum V |x|^2 of fixed-point values, exact in 128-bit integers
+struct Acc128 {
+  unsigned long long lo;
+  long long hi;
+};
+__device__ __forceinline__ void acc_add(Acc128& a, unsigned long long lo, long long hi) {
+  const unsigned long long l = a.lo + lo;
+  a.hi += hi + (l < lo ? 1 : 0);
+  a.lo = l;
+}
+__device__ __forceinline__ double acc_value(const Acc128& a) {
+  return (double)a.hi * 18446744073709551616.0 + (double)a.lo;
+}
+
+// Norm and E_pot partial sums of a block of psi_n in fixed point (components below
+// 2^56 after the block's common shift q): |x|^2 exactly, V|x|^2 with |x|^2 >> 50 and V
+// in 2^vshift fixed point (|V| < 2^50 there).
+__device__ __forceinline__ void acc_point(Acc128& an, Acc128& av, longlong2 x, int q, const long long* Vx, long long p,
+                                          bool epot) {
+  const long long xr = q ? fshift(x.x, -q) : x.x, xi = q ? fshift(x.y, -q) : x.y;
+  const unsigned long long ar = (unsigned long long)(xr < 0 ? -xr : xr), ai = (unsigned long long)(xi < 0 ? -xi : xi);
+  const unsigned long long l1 = ar * ar, l2 = ai * ai;
+  const unsigned long long lo = l1 + l2;
+  const unsigned long long hi = __umul64hi(ar, ar) + __umul64hi(ai, ai) + (lo < l1 ? 1ull : 0ull);
+  acc_add(an, lo, (long long)hi);
+  if (epot) {
+    const long long n2 = (long long)((hi << 14) | (lo >> 50));
+    const long long v = Vx[p];
+    acc_add(av, (unsigned long long)n2 * (unsigned long long)v, __mul64hi(n2, v));
+  }
+}
+
+// 2^62 fixed point of a factor with |f| <= 1
+__device__ __forceinline__ longlong2 to_fx62(double2 f) {
+  return make_longlong2(__double2ll_rn(f.x * 4611686018427387904.0), __double2ll_rn(f.y * 4611686018427387904.0));
+}
+
+// x * f, f in 2^62 fixed point with |f| <= 1 (real f: imaginary-time X factors)
+__device__ __forceinline__ longlong2 apply_f(longlong2 x, longlong2 f, bool real_f) {
+  return real_f ? make_longlong2(mulq62(x.x, f.x), mulq62(x.y, f.x)) : fmul62(x, f);
+}
+
+// Largest exponent shift that brings a block whose largest component has `bits`
+// bits below 2^(62 - guard of the first pass of an N-point transform)
+template <int N>
+__device__ __forceinline__ int first_pass_shift(int bits) {
+  return bits == 0 ? 0 : (62 - fguard(radix_at(N, 0))) - bits;
+}
+// shift that brings `bits` to at most 61 (headroom for one complex product)
+__device__ __forceinline__ int product_headroom(int bits) { return bits > 61 ? 61 - bits : 0; }
+
 #ifdef QSF_DEFINE_KERNELS
 // ------------------------------------------------------------ tables
-// Static X factor for delta (per point): expOp(delta V) * absorb(delta)   (IM: real).
-__global__ void k_build_static(GridDev g, int mode, double delta, double2* xs, double* V) {
+// Range of the potential (for its fixed-point scale and the imaginary-time X factor
+// bound): out[0] = max over points of V (ordered-integer encoding), out[1] = max of -V.
+__device__ __forceinline__ long long ordered_bits(double x) {
+  long long i = __double_as_longlong(x);
+  return i < 0 ? i ^ 0x7fffffffffffffffLL : i;
+}
+__global__ void k_vrange(GridDev g, long long* out) {
+  __shared__ long long r0[32], r1[32];
+  long long a = LLONG_MIN, b = LLONG_MIN;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
     int idx[kMaxDim];
@@ -199,171 +309,359 @@ __global__ void k_build_static(GridDev g, int mode, double delta, double2* xs, d
     unflatten(g, p, idx);
     for (int d = 0; d < g.dim; ++d) c[d] = xpos(g.ax[d], idx[d]);
     const double v = potential_at(g, c);
-    if (V) V[p] = v;
-    if (xs) {
-      const double2 f = expop(mode, delta * v);
-      const double a = absorb_at(g, delta, idx);
-      xs[p] = make_double2(f.x * a, f.y * a);
+    a = max(a, ordered_bits(v));
+    b = max(b, ordered_bits(-v));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a = max(a, __shfl_down_sync(0xffffffffu, a, o));
+    b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r0[threadIdx.x >> 5] = a;
+    r1[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      a = max(a, r0[w]);
+      b = max(b, r1[w]);
     }
+    atomicMax(&out[0], a);
+    atomicMax(&out[1], b);
   }
 }
 
-// Per-step tables: P phase per axis (velocity gauge A of this step; 1/m folded into
-// axis 0) and, in the length gauge, the x.E factors of both X halves.
-__global__ void k_tables(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss) {
+// Static tables for X(delta): expOp(delta V) * absorb(delta) per point in 2^62 fixed
+// point times 2^-xs_exp, and the potential in 2^vshift fixed point.
+__global__ void k_build_static(GridDev g, int mode, double delta, int xs_exp, longlong2* xsx, long long* Vx,
+                               int vshift) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const double vs = ldexp(1.0, vshift), xsc = ldexp(1.0, -xs_exp);
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
+    int idx[kMaxDim];
+    double c[kMaxDim];
+    unflatten(g, p, idx);
+    for (int d = 0; d < g.dim; ++d) c[d] = xpos(g.ax[d], idx[d]);
+    const double v = potential_at(g, c);
+    Vx[p] = __double2ll_rn(v * vs);
+    const double2 f = expop(mode, delta * v);
+    const double a = absorb_at(g, delta, idx) * xsc;
+    const double2 fa = make_double2(f.x * a, f.y * a);
+    xsx[p] = to_fx62(make_double2(fmin(fmax(fa.x, -1.0), 1.0), fmin(fmax(fa.y, -1.0), 1.0)));
+  }
+}
+
+// value of one per-step table entry: kind 0 P phase (hamiltonian.h:52-58: kinetic and,
+// in the velocity gauge, A.k), kind 1 / 2 length-gauge x.E factor of the open / close
+// X half (hamiltonian.h:60-66 via DipoleCoupling)
+__device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& S, const double* cp, int kind, int d,
+                                               int i) {
+  const AxisDev& a = g.ax[d];
+  if (kind == 0) {
+    double A = 0.0;
+    if (g.gauge != 1 && cp && g.n_fields) {
+      int dd = d;
+      if (g.p_swap && g.dim >= 2 && d < 2) dd = 1 - d;
+      A = cp[dd];
+    }
+    const double k = kpos(a, i);
+    return expop(S.mode, S.dt * (0.5 * k * k + k * A));
+  }
+  const double E = (cp && g.n_fields) ? cp[(kind - 1) * 3 + d] : 0.0;
+  return expop(S.mode, (S.dt * 0.5) * (xpos(a, i) * E));
+}
+
+// Per-step tables: one block per (kind, axis) table; each block normalises its table
+// to magnitude <= 1 and records the exponent it took out.  Axis 0's P table also
+// carries the mantissa of 1/m (its power of two goes into the exponent).  Block 0
+// resets the per-pass minimum exponents of the step.
+__global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
+  __shared__ double red[32];
+  __shared__ int e_sh;
+  const int D = g.dim;
+  const int kind = blockIdx.x / D, d = blockIdx.x % D;
+  if (kind > 0 && g.gauge != 1) return;
+  if (blockIdx.x == 0 && threadIdx.x < 4) S.gmin[threadIdx.x] = 0x7fffffff;
   const long long step = S.ctl[0];
   const double* cp = S.coupling ? S.coupling + step * S.coup_stride : nullptr;
-  const int D = g.dim;
-  const int ntab = D * S.nmax;
-  const bool lg = g.gauge == 1;
-  const int total = ntab * (lg ? 3 : 1);
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    const int kind = t / ntab;  // 0: P table, 1: X open, 2: X close
-    const int d = (t % ntab) / S.nmax;
-    const int i = t % S.nmax;
-    const AxisDev& a = g.ax[d];
-    if (i >= a.n) continue;
-    if (kind == 0) {
-      // hamiltonian.h:52-58 kinetic + coupling in P (velocity gauge only)
-      double A = 0.0;
-      if (!lg && cp && g.n_fields) {
-        int dd = d;
-        if (g.p_swap && D >= 2 && d < 2) dd = 1 - d;
-        A = cp[dd];
+  const int n = g.ax[d].n;
+  const double mant = (kind == 0 && d == 0) ? S.m_mant : 1.0;
+  double mx = 0.0;
+  if (S.mode == 1) {  // imaginary time: real factors that may exceed 1
+    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, table_entry(g, S, cp, kind, d, i).x * mant);
+    // block max via the sum helper's layout
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m2 = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m2 = fmax(m2, red[w]);
+      int e = 0;
+      if (m2 > 1.0) {
+        frexp(m2, &e);  // m2 < 2^e
       }
-      const double k = kpos(a, i);
-      const double val = S.dt * (0.5 * k * k + k * A);
-      double2 f = expop(S.mode, val);
-      if (d == 0) f = cscale(f, g.inv_m);
-      S.ptab[d * S.nmax + i] = f;
-    } else {
-      const double E = (cp && g.n_fields) ? cp[(kind - 1) * 3 + d] : 0.0;
-      const double val = (S.dt * 0.5) * (xpos(a, i) * E);
-      S.xdyn[((kind - 1) * D + d) * S.nmax + i] = expop(S.mode, val);
+      e_sh = e;
+      S.texp[kind * 3 + d] = e;
     }
+    __syncthreads();
+  } else {
+    if (threadIdx.x == 0) S.texp[kind * 3 + d] = 0;
+    e_sh = 0;
+  }
+  const double sc = ldexp(mant, -e_sh);
+  longlong2* out = kind == 0 ? S.ptab + (size_t)d * S.nmax : S.xdyn + ((size_t)(kind - 1) * D + d) * S.nmax;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 f = table_entry(g, S, cp, kind, d, i);
+    out[i] = to_fx62(make_double2(fmin(fmax(f.x * sc, -1.0), 1.0), fmin(fmax(f.y * sc, -1.0), 1.0)));
   }
 }
 
 #endif  // QSF_DEFINE_KERNELS
 
-// X factor at point p (row index r, position j on the last axis); half 0 open, 1 close
-__device__ __forceinline__ double2 xfactor(const GridDev& g, const StepDev& S, long long p, long long r, int j,
-                                           int half) {
-  double2 f = __ldg(&S.xs[p]);
+// X factor (2^62 fixed point, |.| <= 1) at point p (row r of the last axis, position
+// j on it); half 0 opens the step, 1 closes it
+__device__ __forceinline__ longlong2 xfactor(const GridDev& g, const StepDev& S, long long p, long long r, int j,
+                                             int half) {
+  longlong2 f = S.xs[p];
   if (g.gauge == 1) {
     const int D = g.dim;
-    const double2* t = S.xdyn + (size_t)half * D * S.nmax;
-    double2 d = __ldg(&t[(D - 1) * S.nmax + j]);
+    const longlong2* t = S.xdyn + (size_t)half * D * S.nmax;
+    longlong2 d = t[(D - 1) * S.nmax + j];
     long long rr = r;
     for (int dd = D - 2; dd >= 0; --dd) {
       const int ii = (int)(rr % g.ax[dd].n);
       rr /= g.ax[dd].n;
-      d = cmul(d, __ldg(&t[dd * S.nmax + ii]));
+      d = fmul62(d, t[dd * S.nmax + ii]);
     }
-    f = cmul(f, d);
+    f = fmul62(f, d);
   }
   return f;
+}
+// exponent taken out of the X factor of one half
+__device__ __forceinline__ int xfactor_exp(const GridDev& g, const StepDev& S, int half) {
+  int e = S.xs_exp;
+  if (g.gauge == 1)
+    for (int d = 0; d < g.dim; ++d) e += S.texp[(1 + half) * 3 + d];
+  return e;
+}
+
+// psi (double) -> fixed point: the block exponent from the largest biased exponent
+// em of the block leaves two bits for the pending Normalize factor and the first pass
+template <int N>
+__device__ __forceinline__ int scale_from_exponent(int em) {
+  return (62 - 1 - fguard(radix_at(N, 0))) - (em - 1022);
+}
+
+// pending Normalize factor s = F 2^-62 * 2^k with F in [2^61, 2^62)
+__device__ __forceinline__ void split_scale(double s, long long& F, int& k) {
+  int e;
+  const double f = frexp(s, &e);
+  F = __double2ll_rn(f * 4611686018427387904.0);
+  k = e;
+}
+
+// Loads psi (double) of `cnt` contiguous points at `base` into smx as fixed point
+// times the pending Normalize factor and the opening X factor; returns the block
+// exponent and (in bits) the bit length of the largest component.
+template <int N>
+__device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, longlong2* smx, long long base, int cnt,
+                                          long long row0, int* red, int& bits) {
+  const bool real_f = S.mode == 1 && g.gauge != 1;
+  int em = 0;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const double2 v = g.psi[base + e];
+    em = max(em, max(dexp(v.x), dexp(v.y)));
+  }
+  em = block_max_int(em, red);
+  const int s_in = scale_from_exponent<N>(em);
+  int scale = s_in;
+  long long F = 0;
+  int k = 0;
+  const bool use_s = S.normalize && *S.scale != 1.0;
+  if (use_s) {
+    split_scale(*S.scale, F, k);
+    scale -= k;
+  }
+  int mb = 0;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const long long p = base + e;
+    const double2 v = g.psi[p];
+    longlong2 x = make_longlong2(d2fx(v.x, s_in), d2fx(v.y, s_in));
+    if (use_s) x = make_longlong2(mulq62(x.x, F), mulq62(x.y, F));
+    x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 0), real_f);
+    smx[e] = x;
+    mb = max(mb, max(fbits(x.x), fbits(x.y)));
+  }
+  bits = block_max_int(mb, red);
+  return scale - xfactor_exp(g, S, 0);
+}
+
+// psi_n from the block after the last inverse transform: closing X factor, 1/m's
+// power of two, store as double, norm / E_pot partial sums (exact integers).  On
+// return smx holds psi_n in fixed point with exponent `scale` and bit length `bits`.
+template <int N>
+__device__ __forceinline__ void close_block(const GridDev& g, const StepDev& S, longlong2* smx, long long base, int cnt,
+                                            long long row0, int* red, int& scale, int& bits, double* dacc) {
+  const bool real_f = S.mode == 1 && g.gauge != 1;
+  const int pre = product_headroom(bits);
+  int mb = 0;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const long long p = base + e;
+    longlong2 x = smx[e];
+    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+    x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 1), real_f);
+    smx[e] = x;
+    mb = max(mb, max(fbits(x.x), fbits(x.y)));
+  }
+  scale += pre - xfactor_exp(g, S, 1) + S.l2m;
+  bits = block_max_int(mb, red);
+  const int q = bits > 56 ? bits - 56 : 0;
+  Acc128 an{0ull, 0ll}, av{0ull, 0ll};
+  const bool epot = (S.obs & 2u) != 0;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const long long p = base + e;
+    const longlong2 x = smx[e];
+    g.psi[p] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
+    acc_point(an, av, x, q, S.Vx, p, epot);
+  }
+  dacc[0] = acc_value(an);
+  dacc[1] = acc_value(av);
+  // block-uniform exponents of the two sums
+  dacc[3] = (double)(2 * q - 2 * scale);
+  dacc[4] = (double)(2 * q - 2 * scale + 50 - S.vshift);
+}
+
+// E_kin part of the last axis: forward transform of psi_n (in smx) and sum k^2 |.|^2
+template <int N>
+__device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, const LineSet& ls, int cnt, int scale,
+                                            int bits, int* red) {
+  const int sh = first_pass_shift<N>(bits);
+  int sc = scale + sh, b = 0;
+  fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, sc, b, red, sh);
+  double ek = 0.0;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const double kk = kpos(a, e % N);
+    const longlong2 x = smx[e];
+    const double xr = fx2d(x.x, sc), xi = fx2d(x.y, sc);
+    ek = fma(kk * kk, fma(xr, xr, xi * xi), ek);
+  }
+  return ek;
 }
 
 // ------------------------------------------------------------ row passes
 // Rows of the last axis: L rows of N points per block, contiguous in memory.
+// Open: psi (double) . [Normalize] . X half . forward FFT -> fixed point (pass 0).
 template <int N>
-__global__ void __launch_bounds__(kRowThreads) k_row_open(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss, int L) {
+__global__ void __launch_bounds__(kRowThreads) k_row_open(const GridDev* __restrict__ Gs,
+                                                          const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
-  extern __shared__ double2 sm[];
-  const AxisDev& a = g.ax[g.dim - 1];
+  extern __shared__ longlong2 smx[];
+  __shared__ int red[32];
   const long long row0 = (long long)blockIdx.x * L;
-  const long long nrows = g.m / N;
-  const int Lh = (int)min((long long)L, nrows - row0);
+  const int Lh = (int)min((long long)L, g.m / N - row0);
   const long long base = row0 * N;
   const int cnt = Lh * N;
-  const double s = (S.normalize && S.scale) ? *S.scale : 1.0;
-  const bool use_s = S.normalize && s != 1.0;
-  const bool realx = S.mode == 1 && g.gauge != 1;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const long long p = base + e;
-    double2 v = g.psi[p];
-    if (use_s) v = cscale(v, s);
-    const double2 f = xfactor(g, S, p, row0 + e / N, e % N, 0);
-    sm[e] = realx ? cscale(v, f.x) : cmul(v, f);
-  }
-  __syncthreads();
+  int bits = 0;
+  int scale = open_block<N>(g, S, smx, base, cnt, row0, red, bits);
+  const int sh = first_pass_shift<N>(bits);
+  scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_static<N, true>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) g.psi[base + e] = sm[e];
+  fft_fx<N, true>(smx, ls, g.ax[g.dim - 1].twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  longlong2* out = reinterpret_cast<longlong2*>(g.psi);
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
+  if (threadIdx.x == 0) {
+    S.sc[blockIdx.x] = scale;
+    atomicMin(&S.gmin[0], scale);
+  }
 }
 
+// Loads the elements [obase + i * inner + c] (i < N, c < Ch) of a fixed-point pass
+// output into smx[i * ldc + c] aligned to the pass minimum exponent; returns the
+// block's common exponent and the bit length of its largest component.
 template <int N>
-__global__ void __launch_bounds__(kRowThreads) k_row_close(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss, int L) {
+__device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, int in_pass, longlong2* smx,
+                                            long long obase, long long inner, int rows, int Ch, int ldc, int* red,
+                                            int& bits) {
+  const int gm = S.gmin[in_pass];
+  const int* sc = S.sc + (size_t)in_pass * S.scmax;
+  const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
+  const int cnt = rows * Ch;
+  int mb = 0;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const int i = e / Ch, c = e % Ch;
+    const long long p = obase + (long long)i * inner + c;
+    longlong2 x = in[p];
+    const int d = gm - sc[producer_block<N>(in_pass, g.dim, p)];
+    if (d) x = make_longlong2(fshift(x.x, d), fshift(x.y, d));
+    smx[i * ldc + c] = x;
+    mb = max(mb, max(fbits(x.x), fbits(x.y)));
+  }
+  bits = block_max_int(mb, red);
+  return gm;
+}
+
+// Close: (fixed point, produced by the last strided-axis pass) inverse FFT . X half
+// -> psi_n (double), norm / E_pot partials, flux snapshot, E_kin part of the last axis.
+template <int N>
+__global__ void __launch_bounds__(kRowThreads) k_row_close(const GridDev* __restrict__ Gs,
+                                                           const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
-  extern __shared__ double2 sm[];
-  __shared__ double red[32 * 3];
+  extern __shared__ longlong2 smx[];
+  __shared__ int red[32];
+  __shared__ double dred[32 * 3];
   const AxisDev& a = g.ax[g.dim - 1];
   const long long row0 = (long long)blockIdx.x * L;
-  const long long nrows = g.m / N;
-  const int Lh = (int)min((long long)L, nrows - row0);
+  const int Lh = (int)min((long long)L, g.m / N - row0);
   const long long base = row0 * N;
   const int cnt = Lh * N;
-  const bool realx = S.mode == 1 && g.gauge != 1;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) sm[e] = g.psi[base + e];
-  __syncthreads();
+  int bits = 0;
+  // rows are contiguous: treat the block as one "column" of cnt elements
+  int scale = load_aligned<N>(g, S, g.dim == 3 ? 3 : 2, smx, base, 1, cnt, 1, 1, red, bits);
+  const int sh = first_pass_shift<N>(bits);
+  scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_static<N, false>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-  double acc[3] = {0.0, 0.0, 0.0};
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const long long p = base + e;
-    const double2 f = xfactor(g, S, p, row0 + e / N, e % N, 1);
-    const double2 v = realx ? cscale(sm[e], f.x) : cmul(sm[e], f);
-    sm[e] = v;
-    g.psi[p] = v;
-    const double nrm = fma(v.x, v.x, v.y * v.y);
-    acc[0] += nrm;
-    if (S.obs & 2u) acc[1] = fma(nrm, __ldg(&S.V[p]), acc[1]);
-  }
+  fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  double dacc[5];
+  close_block<N>(g, S, smx, base, cnt, row0, red, scale, bits, dacc);
   __syncthreads();
-  // flux snapshot of psi_n for the entries of these rows (psi_n is still in smem)
   if (S.row_ptr) {
     const int e0 = S.row_ptr[row0], e1 = S.row_ptr[row0 + Lh];
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = sm[S.snap_idx[e] - base];
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = g.psi[S.snap_idx[e]];
   }
-  __syncthreads();
-  // E_kin part of the last axis: forward FFT of psi_n rows, sum k^2 |.|^2
-  if (S.obs & 4u) {
-    fft_static<N, true>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-      const double k = kpos(a, e % N);
-      const double2 v = sm[e];
-      acc[2] = fma(k * k, fma(v.x, v.x, v.y * v.y), acc[2]);
-    }
-  }
-  block_sum<3>(acc, red);
+  dacc[2] = (S.obs & 4u) ? ekin_rows<N>(a, smx, ls, cnt, scale, bits, red) : 0.0;
+  const double e_n = dacc[3], e_v = dacc[4];
+  block_sum<3>(dacc, dred);
   if (threadIdx.x == 0) {
-    S.partials[0 * S.pmax + blockIdx.x] = acc[0];
-    S.partials[1 * S.pmax + blockIdx.x] = acc[1];
-    S.partials[(2 + g.dim - 1) * S.pmax + blockIdx.x] = acc[2];
+    S.partials[0 * S.pmax + blockIdx.x] = ldexp(dacc[0], (int)e_n);
+    S.partials[1 * S.pmax + blockIdx.x] = ldexp(dacc[1], (int)e_v);
+    S.partials[(2 + g.dim - 1) * S.pmax + blockIdx.x] = dacc[2];
   }
 }
 
 // ------------------------------------------------------------ strided axes
 // Axis `ax` (not the last): tiles of C adjacent columns; element (i, c) of tile
 // (o, c0) is psi[o * N * stride + i * stride + c0 + c].  Modes:
-//   0 forward, 1 inverse, 2 forward . P phase . inverse, 3 forward + E_kin partial
+//   0 forward (3D axis 1: pass 0 -> 1), 1 inverse (3D axis 1: pass 2 -> 3),
+//   2 forward . P phase . inverse (axis 0: pass 0 (2D) or 1 (3D) -> 2),
+//   3 forward of psi_n (double) + E_kin partial
 template <int MODE, int N>
-__global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss, int ax, int C) {
+__global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
+                                                      int ax, int C) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   if (MODE == 3 && !(S.obs & 4u)) return;
-  extern __shared__ double2 sm[];
-  __shared__ double red[32];
-  __shared__ double2 pcol[64];
+  extern __shared__ longlong2 smx[];
+  __shared__ int red[32];
+  __shared__ double dred[32];
+  __shared__ longlong2 pcol[64];
   const AxisDev& a = g.ax[ax];
   const long long inner = a.stride;
   const long long tiles_per_outer = (inner + C - 1) / C;
@@ -372,134 +670,176 @@ __global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict_
   const int Ch = (int)min((long long)C, inner - c0);
   const long long obase = o * (long long)N * inner + c0;
   const int cnt = N * Ch;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int i = e / Ch, c = e % Ch;
-    sm[i * C + c] = g.psi[obase + (long long)i * inner + c];
-  }
-  if (MODE == 2 && threadIdx.x < Ch) {
-    // per-column factor: product of the P tables of the axes after `ax`
-    long long cc = c0 + threadIdx.x;
-    double2 f = make_double2(1.0, 0.0);
-    for (int d = g.dim - 1; d > ax; --d) {
-      const int i = (int)(cc % g.ax[d].n);
-      cc /= g.ax[d].n;
-      f = cmul(f, __ldg(&S.ptab[d * S.nmax + i]));
-    }
-    pcol[threadIdx.x] = f;
-  }
-  __syncthreads();
   const LineSet ls{Ch, 1, C, true};
-  if (MODE == 1) fft_static<N, false>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-  else fft_static<N, true>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-  if (MODE == 2) {
+  int scale = 0, bits = 0;
+  if (MODE == 3) {
+    int em = 0;
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int i = e / Ch, c = e % Ch;
-      const double2 f = cmul(__ldg(&S.ptab[ax * S.nmax + i]), pcol[c]);
-      sm[i * C + c] = S.mode == 1 ? cscale(sm[i * C + c], f.x) : cmul(sm[i * C + c], f);
+      const double2 v = g.psi[obase + (long long)i * inner + c];
+      em = max(em, max(dexp(v.x), dexp(v.y)));
+    }
+    em = block_max_int(em, red);
+    scale = (62 - fguard(radix_at(N, 0))) - (em - 1022);
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int i = e / Ch, c = e % Ch;
+      const double2 v = g.psi[obase + (long long)i * inner + c];
+      smx[i * C + c] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
     }
     __syncthreads();
-    fft_static<N, false>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-  }
-  if (MODE == 3) {
+    fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
     double acc = 0.0;
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int i = e / Ch, c = e % Ch;
       const double k = kpos(a, i);
-      const double2 v = sm[i * C + c];
-      acc = fma(k * k, fma(v.x, v.x, v.y * v.y), acc);
+      const longlong2 x = smx[i * C + c];
+      const double xr = fx2d(x.x, scale), xi = fx2d(x.y, scale);
+      acc = fma(k * k, fma(xr, xr, xi * xi), acc);
     }
-    block_sum<1>(&acc, red);
+    block_sum<1>(&acc, dred);
     if (threadIdx.x == 0) S.partials[(2 + ax) * S.pmax + blockIdx.x] = acc;
     return;
   }
+  const int in_pass = MODE == 0 ? 0 : MODE == 1 ? 2 : (g.dim == 3 ? 1 : 0);
+  const int out_pass = MODE == 0 ? 1 : MODE == 1 ? 3 : 2;
+  scale = load_aligned<N>(g, S, in_pass, smx, obase, inner, N, Ch, C, red, bits);
+  if (MODE == 2 && threadIdx.x < Ch) {
+    // per-column factor: product of the P tables of the axes after `ax`
+    long long cc = c0 + threadIdx.x;
+    longlong2 f = make_longlong2(4611686018427387904LL, 0LL);  // 1.0
+    for (int d2 = g.dim - 1; d2 > ax; --d2) {
+      const int i = (int)(cc % g.ax[d2].n);
+      cc /= g.ax[d2].n;
+      f = fmul62(f, S.ptab[(size_t)d2 * S.nmax + i]);
+    }
+    pcol[threadIdx.x] = f;
+  }
+  int sh = first_pass_shift<N>(bits);
+  scale += sh;
+  if (MODE == 1) fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  else fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  if (MODE == 2) {
+    const bool real_f = S.mode == 1;
+    const int pre = product_headroom(bits);
+    int mb = 0;
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int i = e / Ch, c = e % Ch;
+      longlong2 x = smx[i * C + c];
+      if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+      x = apply_f(x, fmul62(S.ptab[(size_t)ax * S.nmax + i], pcol[c]), real_f);
+      smx[i * C + c] = x;
+      mb = max(mb, max(fbits(x.x), fbits(x.y)));
+    }
+    int pe = 0;
+    for (int d = 0; d < g.dim; ++d) pe += S.texp[d];
+    scale += pre - pe;
+    bits = block_max_int(mb, red);
+    sh = first_pass_shift<N>(bits);
+    scale += sh;
+    fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  }
+  longlong2* out = reinterpret_cast<longlong2*>(g.psi);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
-    g.psi[obase + (long long)i * inner + c] = sm[i * C + c];
+    out[obase + (long long)i * inner + c] = smx[i * C + c];
+  }
+  if (threadIdx.x == 0) {
+    S.sc[(size_t)out_pass * S.scmax + blockIdx.x] = scale;
+    atomicMin(&S.gmin[out_pass], scale);
   }
 }
 
 // ------------------------------------------------------------ 1D whole step
 // One block per line: X open . FFT . P . IFFT . X close . observables, line in smem.
 template <int N>
-__global__ void __launch_bounds__(kLineThreads) k_line_step(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss) {
+__global__ void __launch_bounds__(kLineThreads) k_line_step(const GridDev* __restrict__ Gs,
+                                                            const StepDev* __restrict__ Ss) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
-  extern __shared__ double2 sm[];
-  __shared__ double red[32 * 3];
+  extern __shared__ longlong2 smx[];
+  __shared__ int red[32];
+  __shared__ double dred[32 * 3];
   const AxisDev& a = g.ax[0];
-  const double s = (S.normalize && S.scale) ? *S.scale : 1.0;
-  const bool use_s = S.normalize && s != 1.0;
-  const bool realx = S.mode == 1 && g.gauge != 1;
-  for (int e = threadIdx.x; e < N; e += blockDim.x) {
-    double2 v = g.psi[e];
-    if (use_s) v = cscale(v, s);
-    const double2 f = xfactor(g, S, e, 0, e, 0);
-    sm[e] = realx ? cscale(v, f.x) : cmul(v, f);
-  }
-  __syncthreads();
+  int bits = 0;
+  int scale = open_block<N>(g, S, smx, 0, N, 0, red, bits);
+  int sh = first_pass_shift<N>(bits);
+  scale += sh;
   const LineSet ls{1, N, 1, false};
-  fft_static<N, true>(sm, ls, a.tw, threadIdx.x, blockDim.x);
+  fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  const bool real_f = S.mode == 1;
+  const int pre = product_headroom(bits);
+  int mb = 0;
   for (int e = threadIdx.x; e < N; e += blockDim.x) {
-    const double2 f = __ldg(&S.ptab[e]);
-    sm[e] = S.mode == 1 ? cscale(sm[e], f.x) : cmul(sm[e], f);
+    longlong2 x = smx[e];
+    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+    x = apply_f(x, S.ptab[e], real_f);
+    smx[e] = x;
+    mb = max(mb, max(fbits(x.x), fbits(x.y)));
   }
-  __syncthreads();
-  fft_static<N, false>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-  double acc[3] = {0.0, 0.0, 0.0};
-  for (int e = threadIdx.x; e < N; e += blockDim.x) {
-    const double2 f = xfactor(g, S, e, 0, e, 1);
-    const double2 v = realx ? cscale(sm[e], f.x) : cmul(sm[e], f);
-    sm[e] = v;
-    g.psi[e] = v;
-    const double nrm = fma(v.x, v.x, v.y * v.y);
-    acc[0] += nrm;
-    if (S.obs & 2u) acc[1] = fma(nrm, __ldg(&S.V[e]), acc[1]);
-  }
+  scale += pre - S.texp[0];
+  bits = block_max_int(mb, red);
+  sh = first_pass_shift<N>(bits);
+  scale += sh;
+  fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  double dacc[5];
+  close_block<N>(g, S, smx, 0, N, 0, red, scale, bits, dacc);
   __syncthreads();
   if (S.row_ptr) {
     const int e1 = S.row_ptr[1];
-    for (int e = threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = sm[S.snap_idx[e]];
+    for (int e = threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = g.psi[S.snap_idx[e]];
   }
-  __syncthreads();
-  if (S.obs & 4u) {
-    fft_static<N, true>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-    for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      const double k = kpos(a, e);
-      const double2 v = sm[e];
-      acc[2] = fma(k * k, fma(v.x, v.x, v.y * v.y), acc[2]);
-    }
-  }
-  block_sum<3>(acc, red);
+  dacc[2] = (S.obs & 4u) ? ekin_rows<N>(a, smx, ls, N, scale, bits, red) : 0.0;
+  const double e_n = dacc[3], e_v = dacc[4];
+  block_sum<3>(dacc, dred);
   if (threadIdx.x == 0) {
-    S.partials[0 * S.pmax] = acc[0];
-    S.partials[1 * S.pmax] = acc[1];
-    S.partials[2 * S.pmax] = acc[2];
+    S.partials[0 * S.pmax] = ldexp(dacc[0], (int)e_n);
+    S.partials[1 * S.pmax] = ldexp(dacc[1], (int)e_v);
+    S.partials[2 * S.pmax] = dacc[2];
   }
 }
 
 // ------------------------------------------------------------ plain FFT passes
-// fourier<R>() without phases (qsf_fourier): rows of the last axis, and strided axes
+// fourier<R>() without phases (qsf_fourier), in block fixed point: each block takes
+// its exponent from the largest double it loads, converts with integer operations,
+// runs the fixed-point passes and converts back (times post_scale).
 template <int N, bool FWD>
 __global__ void __launch_bounds__(kLineThreads) k_row_fft(GridDev g, int L, double post_scale) {
-  extern __shared__ double2 sm[];
+  extern __shared__ longlong2 smx[];
+  __shared__ int red[32];
   const AxisDev& a = g.ax[g.dim - 1];
   const long long row0 = (long long)blockIdx.x * L;
   const long long nrows = g.m / N;
   const int Lh = (int)min((long long)L, nrows - row0);
   const long long base = row0 * N;
   const int cnt = Lh * N;
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) sm[e] = g.psi[base + e];
+  int em = 0;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const double2 v = g.psi[base + e];
+    em = max(em, max(dexp(v.x), dexp(v.y)));
+  }
+  em = block_max_int(em, red);
+  int scale = (62 - fguard(radix_at(N, 0))) - (em - 1022);
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const double2 v = g.psi[base + e];
+    smx[e] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
+  }
   __syncthreads();
   const LineSet ls{Lh, N, 1, false};
-  fft_static<N, FWD>(sm, ls, a.tw, threadIdx.x, blockDim.x);
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x)
-    g.psi[base + e] = post_scale == 1.0 ? sm[e] : cscale(sm[e], post_scale);
+  int bits = 0;
+  fft_fx<N, FWD>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const longlong2 x = smx[e];
+    double2 v = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
+    if (post_scale != 1.0) v = cscale(v, post_scale);
+    g.psi[base + e] = v;
+  }
 }
 
 template <int N, bool FWD>
 __global__ void __launch_bounds__(kRowThreads) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
-  extern __shared__ double2 sm[];
+  extern __shared__ longlong2 smx[];
+  __shared__ int red[32];
   const AxisDev& a = g.ax[ax];
   const long long inner = a.stride;
   const long long tiles_per_outer = (inner + C - 1) / C;
@@ -508,17 +848,29 @@ __global__ void __launch_bounds__(kRowThreads) k_axis_fft(GridDev g, int ax, int
   const int Ch = (int)min((long long)C, inner - c0);
   const long long obase = o * (long long)N * inner + c0;
   const int cnt = N * Ch;
+  int em = 0;
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
-    sm[i * C + c] = g.psi[obase + (long long)i * inner + c];
+    const double2 v = g.psi[obase + (long long)i * inner + c];
+    em = max(em, max(dexp(v.x), dexp(v.y)));
+  }
+  em = block_max_int(em, red);
+  int scale = (62 - fguard(radix_at(N, 0))) - (em - 1022);
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const int i = e / Ch, c = e % Ch;
+    const double2 v = g.psi[obase + (long long)i * inner + c];
+    smx[i * C + c] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
   }
   __syncthreads();
   const LineSet ls{Ch, 1, C, true};
-  fft_static<N, FWD>(sm, ls, a.tw, threadIdx.x, blockDim.x);
+  int bits = 0;
+  fft_fx<N, FWD>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
-    const double2 v = sm[i * C + c];
-    g.psi[obase + (long long)i * inner + c] = post_scale == 1.0 ? v : cscale(v, post_scale);
+    const longlong2 x = smx[i * C + c];
+    double2 v = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
+    if (post_scale != 1.0) v = cscale(v, post_scale);
+    g.psi[obase + (long long)i * inner + c] = v;
   }
 }
 
