@@ -38,18 +38,23 @@ __device__ __forceinline__ i64 mulq60(i64 a, i64 w) {
 
 __device__ __forceinline__ longlong2 fadd(longlong2 a, longlong2 b) { return make_longlong2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ longlong2 fsub(longlong2 a, longlong2 b) { return make_longlong2(a.x - b.x, a.y - b.y); }
-// a * w with w in 2^62 fixed point (|w| <= 1)
+__device__ __forceinline__ longlong2 fconj(longlong2 a) { return make_longlong2(a.x, -a.y); }
+// a * w with w in 2^62 fixed point (|w| <= 1, components of a below 2^62): three
+// rounded products (Gauss / Karatsuba): re = c(a+b) - b(c+d), im = c(a+b) + a(d-c)
 __device__ __forceinline__ longlong2 fmul62(longlong2 a, longlong2 w) {
-  return make_longlong2(mulq62(a.x, w.x) - mulq62(a.y, w.y), mulq62(a.x, w.y) + mulq62(a.y, w.x));
-}
-// a * conj(w)
-__device__ __forceinline__ longlong2 fmul62c(longlong2 a, longlong2 w) {
-  return make_longlong2(mulq62(a.x, w.x) + mulq62(a.y, w.y), mulq62(a.y, w.x) - mulq62(a.x, w.y));
+  const i64 k1 = mulq62(a.x + a.y, w.x);
+  const i64 k2 = mulq62(a.x, w.y - w.x);
+  const i64 k3 = mulq62(a.y, w.x + w.y);
+  return make_longlong2(k1 - k3, k1 + k2);
 }
 // a * w with w in 2^60 fixed point (|w| < 4)
 __device__ __forceinline__ longlong2 fmul60(longlong2 a, longlong2 w) {
   return make_longlong2(mulq60(a.x, w.x) - mulq60(a.y, w.y), mulq60(a.x, w.y) + mulq60(a.y, w.x));
 }
+// OR of the component magnitudes (x ^ (x >> 63) is |x| or |x| - 1): its bit length is
+// the block maximum's bit length, or one less when that maximum is a negative power of two
+__device__ __forceinline__ u64 fmag(longlong2 x) { return (u64)(x.x ^ (x.x >> 63)) | (u64)(x.y ^ (x.y >> 63)); }
+__device__ __forceinline__ int bitlen(u64 v) { return 64 - __clzll((long long)v); }
 template <bool FWD> __device__ __forceinline__ longlong2 fmul_si(longlong2 a) {
   return FWD ? make_longlong2(a.y, -a.x) : make_longlong2(-a.y, a.x);
 }
@@ -136,10 +141,9 @@ template <bool FWD> __device__ __forceinline__ void fbfly5(longlong2* v) {
   v[2] = make_longlong2(a2.x - b2.y, a2.y + b2.x);
   v[3] = make_longlong2(a2.x + b2.y, a2.y - b2.x);
 }
-// multiply by (c + i sign s) in 2^62 fixed point
+// multiply by (c + i sign s) in 2^62 fixed point (three products)
 template <bool FWD> __device__ __forceinline__ longlong2 frot(longlong2 a, i64 c, i64 s) {
-  const i64 ss = FWD ? -s : s;
-  return make_longlong2(mulq62(a.x, c) - mulq62(a.y, ss), mulq62(a.x, ss) + mulq62(a.y, c));
+  return fmul62(a, make_longlong2(c, FWD ? -s : s));
 }
 template <bool FWD> __device__ __forceinline__ void fbfly16(longlong2* v) {
   longlong2 a[16];
@@ -207,10 +211,11 @@ __device__ __forceinline__ int block_max_int(int v, int* red) {
   return m;
 }
 
-// One in-place Stockham pass in fixed point.  Inputs are scaled by 2^shift_in on
-// load; returns (via bits_out, valid in every thread after the call) the bit length
-// of the largest output component in the block.
-template <int R, bool FWD, int MAXB, int N, int NS>
+// One in-place forward Stockham pass in fixed point (an inverse transform is the
+// forward one between two conjugations).  Inputs are scaled by 2^shift_in on load;
+// returns, valid in every thread after the call, the bit length of the block's
+// largest output component (see fmag).
+template <int R, int MAXB, int N, int NS>
 __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const LineSet& L,
                                            const longlong2* __restrict__ tw, int tid, int nth, int shift_in, int* red) {
   constexpr int nr = N / R;
@@ -241,48 +246,46 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
       const int jm = j % NS;
       if constexpr (NS > 1) {
 #pragma unroll
-        for (int q = 1; q < R; ++q) {
-          const longlong2 t = tw[jm * q * twstep];
-          v[b][q] = FWD ? fmul62(v[b][q], t) : fmul62c(v[b][q], t);
-        }
+        for (int q = 1; q < R; ++q) v[b][q] = fmul62(v[b][q], tw[jm * q * twstep]);
       }
       dsto[b] = line * L.ls + ((j - jm) * R + jm) * L.es;
     }
   }
   __syncthreads();
-  int mb = 0;
+  u64 mag = 0;
 #pragma unroll
   for (int b = 0; b < MAXB; ++b) {
     if (dsto[b] >= 0) {
-      fbfly<R, FWD>(v[b]);
+      fbfly<R, true>(v[b]);
       longlong2* dst = buf + dsto[b];
       const int st = NS * L.es;
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         dst[q * st] = v[b][q];
-        mb = max(mb, max(fbits(v[b][q].x), fbits(v[b][q].y)));
+        mag |= fmag(v[b][q]);
       }
     }
   }
-  return block_max_int(mb, red);  // includes the barrier that ends the pass
+  return block_max_int(bitlen(mag), red);  // includes the barrier that ends the pass
 }
 
-// Full fixed-point transform of every line of the set, in place.  On entry the data
-// have block exponent `scale` (value = int * 2^-scale) and fit the first pass's
-// guard; on return `scale` is the exponent of the output and its largest component
-// has bit length `bits`.  Requires nlines * N <= 16 * nth.
-template <int N, bool FWD, int S = 0>
+// Full forward fixed-point transform of every line of the set, in place.  On entry
+// the data have block exponent `scale` (value = int * 2^-scale) and, after the shift
+// 2^shift_in applied on load, fit the first pass's guard; on return `scale` is the
+// exponent of the output and its largest component has bit length `bits`.
+// Requires nlines * N <= 16 * nth.
+template <int N, int S = 0>
 __device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw, int tid,
                                        int nth, int& scale, int& bits, int* red, int shift_in = 0) {
   if constexpr (S < nstages(N)) {
     constexpr int R = radix_at(N, S);
-    bits = fx_stockham<R, FWD, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red);
+    bits = fx_stockham<R, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red);
     if constexpr (S + 1 < nstages(N)) {
-      // renormalise for the next pass: largest component < 2^(62 - guard(next))
+      // renormalise for the next pass: largest component below 2^(62 - guard(next))
       const int target = 62 - fguard(radix_at(N, S + 1));
       const int sh = bits == 0 ? 0 : target - bits;
       scale += sh;
-      fft_fx<N, FWD, S + 1>(buf, L, tw, tid, nth, scale, bits, red, sh);
+      fft_fx<N, S + 1>(buf, L, tw, tid, nth, scale, bits, red, sh);
     }
   }
 }

@@ -41,6 +41,10 @@ constexpr int kMaxDim = 3;
 constexpr int kRowThreads = 256;
 constexpr int kLineThreads = 512;
 constexpr int kMaxFluxBorders = 16;
+// resident blocks per SM the FFT kernels are compiled for (caps registers per thread)
+#ifndef QSF_FFT_MIN_BLOCKS
+#define QSF_FFT_MIN_BLOCKS 2
+#endif
 
 struct AxisDev {
   int n, n2;
@@ -463,16 +467,20 @@ __device__ __forceinline__ void split_scale(double s, long long& F, int& k) {
   k = e;
 }
 
-// Loads psi (double) of `cnt` contiguous points at `base` into smx as fixed point
-// times the pending Normalize factor and the opening X factor; returns the block
-// exponent and (in bits) the bit length of the largest component.
+// Loads psi (double) of `cnt` contiguous points at `base` into smx (one global read,
+// staged in smem as doubles, converted in place) as fixed point times the pending
+// Normalize factor and the opening X factor; returns the block exponent and (in bits)
+// the bit length of the largest component.
 template <int N>
 __device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, longlong2* smx, long long base, int cnt,
                                           long long row0, int* red, int& bits) {
   const bool real_f = S.mode == 1 && g.gauge != 1;
+  double2* sd = reinterpret_cast<double2*>(smx);
   int em = 0;
+#pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const double2 v = g.psi[base + e];
+    sd[e] = v;
     em = max(em, max(dexp(v.x), dexp(v.y)));
   }
   em = block_max_int(em, red);
@@ -485,42 +493,48 @@ __device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, lo
     split_scale(*S.scale, F, k);
     scale -= k;
   }
-  int mb = 0;
+  u64 mag = 0;
+#pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const long long p = base + e;
-    const double2 v = g.psi[p];
+    const double2 v = sd[e];  // written by this thread
     longlong2 x = make_longlong2(d2fx(v.x, s_in), d2fx(v.y, s_in));
     if (use_s) x = make_longlong2(mulq62(x.x, F), mulq62(x.y, F));
     x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 0), real_f);
     smx[e] = x;
-    mb = max(mb, max(fbits(x.x), fbits(x.y)));
+    mag |= fmag(x);
   }
-  bits = block_max_int(mb, red);
+  bits = block_max_int(bitlen(mag), red);
   return scale - xfactor_exp(g, S, 0);
 }
 
-// psi_n from the block after the last inverse transform: closing X factor, 1/m's
-// power of two, store as double, norm / E_pot partial sums (exact integers).  On
-// return smx holds psi_n in fixed point with exponent `scale` and bit length `bits`.
+// psi_n from the block after the last inverse transform (held conjugated in smx when
+// conj_in): closing X factor, 1/m's power of two, store as double, norm / E_pot
+// partial sums (exact integers).  On return smx holds psi_n in fixed point with
+// exponent `scale` and bit length `bits`.
 template <int N>
 __device__ __forceinline__ void close_block(const GridDev& g, const StepDev& S, longlong2* smx, long long base, int cnt,
-                                            long long row0, int* red, int& scale, int& bits, double* dacc) {
+                                            long long row0, int* red, int& scale, int& bits, double* dacc,
+                                            bool conj_in) {
   const bool real_f = S.mode == 1 && g.gauge != 1;
   const int pre = product_headroom(bits);
-  int mb = 0;
+  u64 mag = 0;
+#pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const long long p = base + e;
     longlong2 x = smx[e];
+    if (conj_in) x = fconj(x);
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
     x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 1), real_f);
     smx[e] = x;
-    mb = max(mb, max(fbits(x.x), fbits(x.y)));
+    mag |= fmag(x);
   }
   scale += pre - xfactor_exp(g, S, 1) + S.l2m;
-  bits = block_max_int(mb, red);
+  bits = block_max_int(bitlen(mag), red);
   const int q = bits > 56 ? bits - 56 : 0;
   Acc128 an{0ull, 0ll}, av{0ull, 0ll};
   const bool epot = (S.obs & 2u) != 0;
+#pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const long long p = base + e;
     const longlong2 x = smx[e];
@@ -540,7 +554,7 @@ __device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, co
                                             int bits, int* red) {
   const int sh = first_pass_shift<N>(bits);
   int sc = scale + sh, b = 0;
-  fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, sc, b, red, sh);
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, sc, b, red, sh);
   double ek = 0.0;
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const double kk = kpos(a, e % N);
@@ -555,7 +569,7 @@ __device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, co
 // Rows of the last axis: L rows of N points per block, contiguous in memory.
 // Open: psi (double) . [Normalize] . X half . forward FFT -> fixed point (pass 0).
 template <int N>
-__global__ void __launch_bounds__(kRowThreads) k_row_open(const GridDev* __restrict__ Gs,
+__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_open(const GridDev* __restrict__ Gs,
                                                           const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -571,8 +585,9 @@ __global__ void __launch_bounds__(kRowThreads) k_row_open(const GridDev* __restr
   const int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_fx<N, true>(smx, ls, g.ax[g.dim - 1].twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N>(smx, ls, g.ax[g.dim - 1].twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
+#pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
   if (threadIdx.x == 0) {
     S.sc[blockIdx.x] = scale;
@@ -580,35 +595,39 @@ __global__ void __launch_bounds__(kRowThreads) k_row_open(const GridDev* __restr
   }
 }
 
-// Loads the elements [obase + i * inner + c] (i < N, c < Ch) of a fixed-point pass
-// output into smx[i * ldc + c] aligned to the pass minimum exponent; returns the
-// block's common exponent and the bit length of its largest component.
+// Loads the elements [obase + i * inner + c] (i < rows, c < Ch) of a fixed-point pass
+// output into smx[i * ldc + c] aligned to the pass minimum exponent (conjugated when
+// conj); returns the block's common exponent and the bit length of its largest
+// component.
 template <int N>
 __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, int in_pass, longlong2* smx,
                                             long long obase, long long inner, int rows, int Ch, int ldc, int* red,
-                                            int& bits) {
+                                            int& bits, bool conj) {
   const int gm = S.gmin[in_pass];
   const int* sc = S.sc + (size_t)in_pass * S.scmax;
   const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
   const int cnt = rows * Ch;
-  int mb = 0;
+  u64 mag = 0;
+#pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
     const long long p = obase + (long long)i * inner + c;
     longlong2 x = in[p];
     const int d = gm - sc[producer_block<N>(in_pass, g.dim, p)];
     if (d) x = make_longlong2(fshift(x.x, d), fshift(x.y, d));
+    if (conj) x = fconj(x);
     smx[i * ldc + c] = x;
-    mb = max(mb, max(fbits(x.x), fbits(x.y)));
+    mag |= fmag(x);
   }
-  bits = block_max_int(mb, red);
+  bits = block_max_int(bitlen(mag), red);
   return gm;
 }
 
 // Close: (fixed point, produced by the last strided-axis pass) inverse FFT . X half
 // -> psi_n (double), norm / E_pot partials, flux snapshot, E_kin part of the last axis.
+// The inverse transform is the forward one on conjugated data.
 template <int N>
-__global__ void __launch_bounds__(kRowThreads) k_row_close(const GridDev* __restrict__ Gs,
+__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(const GridDev* __restrict__ Gs,
                                                            const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -623,13 +642,13 @@ __global__ void __launch_bounds__(kRowThreads) k_row_close(const GridDev* __rest
   const int cnt = Lh * N;
   int bits = 0;
   // rows are contiguous: treat the block as one "column" of cnt elements
-  int scale = load_aligned<N>(g, S, g.dim == 3 ? 3 : 2, smx, base, 1, cnt, 1, 1, red, bits);
+  int scale = load_aligned<N>(g, S, g.dim == 3 ? 3 : 2, smx, base, 1, cnt, 1, 1, red, bits, true);
   const int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
-  close_block<N>(g, S, smx, base, cnt, row0, red, scale, bits, dacc);
+  close_block<N>(g, S, smx, base, cnt, row0, red, scale, bits, dacc, true);
   __syncthreads();
   if (S.row_ptr) {
     const int e0 = S.row_ptr[row0], e1 = S.row_ptr[row0 + Lh];
@@ -645,14 +664,40 @@ __global__ void __launch_bounds__(kRowThreads) k_row_close(const GridDev* __rest
   }
 }
 
+// P phase between the forward and the inverse transform of axis `ax` (element (i, c)
+// of the tile at smx[i * ldc + c]), written conjugated so that the inverse transform
+// runs as a forward one; returns the exponent change and the new bit length.
+__device__ __forceinline__ int p_phase(const GridDev& g, const StepDev& S, longlong2* smx, int ax, int rows, int Ch,
+                                       int ldc, const longlong2* pcol, int* red, int& bits) {
+  const bool real_f = S.mode == 1;
+  const int pre = product_headroom(bits);
+  const int cnt = rows * Ch;
+  u64 mag = 0;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const int i = e / Ch, c = e % Ch;
+    longlong2 x = smx[i * ldc + c];
+    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+    const longlong2 f = pcol ? fmul62(S.ptab[(size_t)ax * S.nmax + i], pcol[c]) : S.ptab[(size_t)ax * S.nmax + i];
+    x = fconj(apply_f(x, f, real_f));
+    smx[i * ldc + c] = x;
+    mag |= fmag(x);
+  }
+  int pe = 0;
+  for (int d = 0; d < g.dim; ++d) pe += S.texp[d];
+  bits = block_max_int(bitlen(mag), red);
+  return pre - pe;
+}
+
 // ------------------------------------------------------------ strided axes
 // Axis `ax` (not the last): tiles of C adjacent columns; element (i, c) of tile
 // (o, c0) is psi[o * N * stride + i * stride + c0 + c].  Modes:
 //   0 forward (3D axis 1: pass 0 -> 1), 1 inverse (3D axis 1: pass 2 -> 3),
 //   2 forward . P phase . inverse (axis 0: pass 0 (2D) or 1 (3D) -> 2),
 //   3 forward of psi_n (double) + E_kin partial
+// Inverse transforms run as forward ones on conjugated data.
 template <int MODE, int N>
-__global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
+__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
                                                       int ax, int C) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -673,21 +718,23 @@ __global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict_
   const LineSet ls{Ch, 1, C, true};
   int scale = 0, bits = 0;
   if (MODE == 3) {
+    double2* sd = reinterpret_cast<double2*>(smx);
     int em = 0;
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int i = e / Ch, c = e % Ch;
       const double2 v = g.psi[obase + (long long)i * inner + c];
+      sd[i * C + c] = v;
       em = max(em, max(dexp(v.x), dexp(v.y)));
     }
     em = block_max_int(em, red);
     scale = (62 - fguard(radix_at(N, 0))) - (em - 1022);
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int i = e / Ch, c = e % Ch;
-      const double2 v = g.psi[obase + (long long)i * inner + c];
+      const double2 v = sd[i * C + c];
       smx[i * C + c] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
     }
     __syncthreads();
-    fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+    fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
     double acc = 0.0;
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int i = e / Ch, c = e % Ch;
@@ -702,8 +749,9 @@ __global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict_
   }
   const int in_pass = MODE == 0 ? 0 : MODE == 1 ? 2 : (g.dim == 3 ? 1 : 0);
   const int out_pass = MODE == 0 ? 1 : MODE == 1 ? 3 : 2;
-  scale = load_aligned<N>(g, S, in_pass, smx, obase, inner, N, Ch, C, red, bits);
-  if (MODE == 2 && threadIdx.x < Ch) {
+  scale = load_aligned<N>(g, S, in_pass, smx, obase, inner, N, Ch, C, red, bits, MODE == 1);
+  const bool multi_col = MODE == 2 && ax + 1 < g.dim;
+  if (multi_col && threadIdx.x < Ch) {
     // per-column factor: product of the P tables of the axes after `ax`
     long long cc = c0 + threadIdx.x;
     longlong2 f = make_longlong2(4611686018427387904LL, 0LL);  // 1.0
@@ -716,32 +764,20 @@ __global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict_
   }
   int sh = first_pass_shift<N>(bits);
   scale += sh;
-  if (MODE == 1) fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
-  else fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   if (MODE == 2) {
-    const bool real_f = S.mode == 1;
-    const int pre = product_headroom(bits);
-    int mb = 0;
-    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-      const int i = e / Ch, c = e % Ch;
-      longlong2 x = smx[i * C + c];
-      if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-      x = apply_f(x, fmul62(S.ptab[(size_t)ax * S.nmax + i], pcol[c]), real_f);
-      smx[i * C + c] = x;
-      mb = max(mb, max(fbits(x.x), fbits(x.y)));
-    }
-    int pe = 0;
-    for (int d = 0; d < g.dim; ++d) pe += S.texp[d];
-    scale += pre - pe;
-    bits = block_max_int(mb, red);
+    scale += p_phase(g, S, smx, ax, N, Ch, C, multi_col ? pcol : nullptr, red, bits);
     sh = first_pass_shift<N>(bits);
     scale += sh;
-    fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+    fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   }
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
+  const bool conj_out = MODE != 0;
+#pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
-    out[obase + (long long)i * inner + c] = smx[i * C + c];
+    const longlong2 x = smx[i * C + c];
+    out[obase + (long long)i * inner + c] = conj_out ? fconj(x) : x;
   }
   if (threadIdx.x == 0) {
     S.sc[(size_t)out_pass * S.scmax + blockIdx.x] = scale;
@@ -752,7 +788,7 @@ __global__ void __launch_bounds__(kRowThreads) k_axis(const GridDev* __restrict_
 // ------------------------------------------------------------ 1D whole step
 // One block per line: X open . FFT . P . IFFT . X close . observables, line in smem.
 template <int N>
-__global__ void __launch_bounds__(kLineThreads) k_line_step(const GridDev* __restrict__ Gs,
+__global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_line_step(const GridDev* __restrict__ Gs,
                                                             const StepDev* __restrict__ Ss) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -766,24 +802,13 @@ __global__ void __launch_bounds__(kLineThreads) k_line_step(const GridDev* __res
   int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{1, N, 1, false};
-  fft_fx<N, true>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
-  const bool real_f = S.mode == 1;
-  const int pre = product_headroom(bits);
-  int mb = 0;
-  for (int e = threadIdx.x; e < N; e += blockDim.x) {
-    longlong2 x = smx[e];
-    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    x = apply_f(x, S.ptab[e], real_f);
-    smx[e] = x;
-    mb = max(mb, max(fbits(x.x), fbits(x.y)));
-  }
-  scale += pre - S.texp[0];
-  bits = block_max_int(mb, red);
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  scale += p_phase(g, S, smx, 0, N, 1, 1, nullptr, red, bits);
   sh = first_pass_shift<N>(bits);
   scale += sh;
-  fft_fx<N, false>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
-  close_block<N>(g, S, smx, 0, N, 0, red, scale, bits, dacc);
+  close_block<N>(g, S, smx, 0, N, 0, red, scale, bits, dacc, true);
   __syncthreads();
   if (S.row_ptr) {
     const int e1 = S.row_ptr[1];
@@ -801,10 +826,11 @@ __global__ void __launch_bounds__(kLineThreads) k_line_step(const GridDev* __res
 
 // ------------------------------------------------------------ plain FFT passes
 // fourier<R>() without phases (qsf_fourier), in block fixed point: each block takes
-// its exponent from the largest double it loads, converts with integer operations,
-// runs the fixed-point passes and converts back (times post_scale).
+// its exponent from the largest double it loads (one global read, staged in smem),
+// converts with integer operations, runs the fixed-point passes (an inverse is the
+// forward transform between two conjugations) and converts back (times post_scale).
 template <int N, bool FWD>
-__global__ void __launch_bounds__(kLineThreads) k_row_fft(GridDev g, int L, double post_scale) {
+__global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_row_fft(GridDev g, int L, double post_scale) {
   extern __shared__ longlong2 smx[];
   __shared__ int red[32];
   const AxisDev& a = g.ax[g.dim - 1];
@@ -813,23 +839,26 @@ __global__ void __launch_bounds__(kLineThreads) k_row_fft(GridDev g, int L, doub
   const int Lh = (int)min((long long)L, nrows - row0);
   const long long base = row0 * N;
   const int cnt = Lh * N;
+  double2* sd = reinterpret_cast<double2*>(smx);
   int em = 0;
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const double2 v = g.psi[base + e];
+    sd[e] = v;
     em = max(em, max(dexp(v.x), dexp(v.y)));
   }
   em = block_max_int(em, red);
   int scale = (62 - fguard(radix_at(N, 0))) - (em - 1022);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const double2 v = g.psi[base + e];
-    smx[e] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
+    const double2 v = sd[e];
+    const longlong2 x = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
+    smx[e] = FWD ? x : fconj(x);
   }
   __syncthreads();
   const LineSet ls{Lh, N, 1, false};
   int bits = 0;
-  fft_fx<N, FWD>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const longlong2 x = smx[e];
+    const longlong2 x = FWD ? smx[e] : fconj(smx[e]);
     double2 v = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
     if (post_scale != 1.0) v = cscale(v, post_scale);
     g.psi[base + e] = v;
@@ -837,7 +866,7 @@ __global__ void __launch_bounds__(kLineThreads) k_row_fft(GridDev g, int L, doub
 }
 
 template <int N, bool FWD>
-__global__ void __launch_bounds__(kRowThreads) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
+__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
   extern __shared__ longlong2 smx[];
   __shared__ int red[32];
   const AxisDev& a = g.ax[ax];
@@ -848,26 +877,29 @@ __global__ void __launch_bounds__(kRowThreads) k_axis_fft(GridDev g, int ax, int
   const int Ch = (int)min((long long)C, inner - c0);
   const long long obase = o * (long long)N * inner + c0;
   const int cnt = N * Ch;
+  double2* sd = reinterpret_cast<double2*>(smx);
   int em = 0;
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
     const double2 v = g.psi[obase + (long long)i * inner + c];
+    sd[i * C + c] = v;
     em = max(em, max(dexp(v.x), dexp(v.y)));
   }
   em = block_max_int(em, red);
   int scale = (62 - fguard(radix_at(N, 0))) - (em - 1022);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
-    const double2 v = g.psi[obase + (long long)i * inner + c];
-    smx[i * C + c] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
+    const double2 v = sd[i * C + c];
+    const longlong2 x = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
+    smx[i * C + c] = FWD ? x : fconj(x);
   }
   __syncthreads();
   const LineSet ls{Ch, 1, C, true};
   int bits = 0;
-  fft_fx<N, FWD>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
-    const longlong2 x = smx[i * C + c];
+    const longlong2 x = FWD ? smx[i * C + c] : fconj(smx[i * C + c]);
     double2 v = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
     if (post_scale != 1.0) v = cscale(v, post_scale);
     g.psi[obase + (long long)i * inner + c] = v;
