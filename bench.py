@@ -231,13 +231,8 @@ def _schedule(Q, dim, inten, lam, ncycles, nsteps):
     c = Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field({1: 1, 2: 3}[dim], [Q.Pulse(field=Q.field_from_intensity(inten),
                                                                           omega=Q.omega_from_wavelength(lam),
                                                                           ncycles=ncycles)])])
-    rows = np.zeros((nsteps, 3))
-    timer = 0.0
-    for s in range(nsteps):
-        c.precalc(timer)
-        rows[s] = c.vector()
-        timer += DT * (1.0 * 1.0)
-    return rows
+    from qsf_gb300.propagator import coupling_schedule
+    return coupling_schedule(c, DT, nsteps)[0]
 
 
 def run_batched(steps, warmup, nsolves=256, seed=0):

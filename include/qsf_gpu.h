@@ -8,7 +8,10 @@
  * the propagator (include/propagator.h).  This ABI replaces those members with calls
  * that run hand-written CUDA kernels on one GPU; every entry point below names the
  * reference member it stands in for.  The wavefunction lives in device memory owned
- * by a qsf_grid handle.  All arithmetic is FP64 / complex128.
+ * by a qsf_grid handle and is exchanged as complex128.  Inside a step the transforms
+ * and phase products run in block fixed point (int64 components sharing one
+ * power-of-two exponent per thread block, 55 or more significant bits), which is more
+ * accurate than an FP64 FFT and runs on GB300's integer pipes.
  *
  * Conventions
  *  - Arrays of complex numbers are interleaved doubles (re, im), C order, last axis
@@ -154,7 +157,15 @@ int qsf_add_gaussian(qsf_grid* g, double at, double delta);
  * (propagator.h:304-309): after the first step whose |E_n - E_{n-1}| <= accuracy
  * exactly one more step runs and the call returns; *steps_done says how many ran.
  * E_n = epot + ekin; bit 0 of energy_after_normalize divides epot, bit 1 divides ekin
- * by the step's norm (the observables declared after OPERATION<Normalize>). */
+ * by the step's norm (the observables declared after OPERATION<Normalize>).
+ *
+ * substeps = K > 1 is MultiProductSplit<Split3Base<X,P,X>, K> (splitting.h:63-91,
+ * propagator.h:331-413).  As the reference completes its chains, a step's result is
+ * its last chain: K Strang sub-steps of dt / K with the inner X halves joined.  The
+ * coupling then holds nsteps * K rows, one per sub-step, as that chain evaluates them
+ * (velocity gauge: A at each P sub-step; length gauge: E at the sub-step's opening
+ * and closing X half, the closing one equal to the next sub-step's opening one);
+ * observables, Normalize and the convergence test apply once per step. */
 #define QSF_OBS_NORM 1u
 #define QSF_OBS_EPOT 2u
 #define QSF_OBS_EKIN 4u
@@ -177,6 +188,7 @@ typedef struct qsf_step_desc {
    * kernel_ms[QSF_K_*]; kernel_launches[QSF_K_*] counts the launches. */
   float* kernel_ms;
   int64_t* kernel_launches;
+  int substeps;             /* MultiProductSplit order K (0 or 1: plain Strang) */
 } qsf_step_desc;
 /* kernel kinds of the fused step (for qsf_step_desc.kernel_ms) */
 #define QSF_K_TABLES 0
@@ -265,6 +277,42 @@ int qsf_server_wait(qsf_server* s, int64_t ticket, double timeout_s, qsf_result*
 int qsf_server_stats_get(qsf_server* s, qsf_server_stats* out);
 /* finishes the solves in flight, drops the queued ones (status QSF_ESTATE), joins */
 int qsf_server_stop(qsf_server* s);
+
+/* ------------------------------------------------------ wavefunction files */
+/* .psi files with the layout of the reference's LocalGrid (grid.h:1025-1035):
+ * dim u8 | rep u8 | complex u8 | downscale i64 | n[dim] i64 | dx[dim] f64 |
+ * bounded[dim] u8 | payload.  Paths are relative to the process's working directory,
+ * as in the reference. */
+typedef struct qsf_dump_format { /* DUMP_FORMAT, enums.h:157-164 */
+  int rep;            /* QSF_REP_X or QSF_REP_P (P: centred by the (-1)^(i0+i1+..) shift) */
+  int complex_values; /* 1: complex128 payload; 0: |psi|^2 (float64) */
+  int64_t downscale;  /* >= 1 and dividing every axis; > 1 stores |psi|^2 block sums */
+  int evo_backup;     /* 1: raw psi, no name suffixes (evolution backups) */
+} qsf_dump_format;
+/* save / _save_centered / _save / coarse (grid.h:955-1114): writes
+ * base[_scale<d>]_rep{X,P}<ext> (no suffixes for evo_backup) and returns the path in
+ * path_out (may be NULL).  A P-representation save transforms psi and back, as the
+ * reference does. */
+int qsf_save(qsf_grid* g, const char* base, const qsf_dump_format* df, const char* ext, char* path_out,
+             size_t path_cap);
+/* load / _load (grid.h:789-859): reads base<ext> into psi.  A file of the wrong
+ * dimensionality is QSF_EINVAL.  warnings (may be NULL) gets bit 0: n differs,
+ * bit 1: dx differs, bit 2: file holds |psi|^2 (each element becomes its modulus, as
+ * the reference reads it), bit 3: file shorter than the grid.  norm (may be NULL)
+ * gets <psi|psi> dV after loading. */
+int qsf_load(qsf_grid* g, const char* base, const char* ext, int* warnings, double* norm);
+/* orthogonalizeWith (grid.h:909-946): psi -= <psi_f|psi> dV psi_f for the complex
+ * wavefunction psi_f in base<ext>; overlap2 (may be NULL) gets <psi_f|psi> dV as
+ * (re, im), norm the norm afterwards.  The payload is read after the header the file
+ * actually has (the reference's offset arithmetic is 3 bytes short, grid.h:917-918). */
+int qsf_orthogonalize_with(qsf_grid* g, const char* base, const char* ext, double* overlap2, double* norm);
+/* _backup (grid.h:1116-1126): backup.info (int64 step) and backup<ext> (raw psi) */
+int qsf_backup(qsf_grid* g, int64_t step, const char* ext);
+/* restore (grid.h:949-953) plus the step read from backup.info (propagator.h:424-428);
+ * step may be NULL */
+int qsf_restore(qsf_grid* g, const char* ext, int64_t* step);
+/* remove_backups (grid.h:1128-1132) */
+int qsf_remove_backups(const char* ext);
 
 /* ------------------------------------------------- norm without allocation */
 /* No counterpart in the reference.  For callers that cannot allocate device memory

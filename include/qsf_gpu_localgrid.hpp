@@ -258,8 +258,49 @@ struct LocalGrid<Hamiltonian, GPU::CAP<D>, Components, MPI_GC, MPI::Slices, fals
     bo.template store<M, COMP>(1.0);
   }
   void postCompute() {}
-  void restore() {}
-  void remove_backups() {}
+
+  // .psi files (grid.h:948-1153), written and read by the library
+  static qsf_dump_format dump_of(const DUMP_FORMAT& df) {
+    return qsf_dump_format{df.rep == REP::P ? QSF_REP_P : QSF_REP_X, df.complex ? 1 : 0, (int64_t)df.downscale,
+                           df.evo_backup ? 1 : 0};
+  }
+  IO::path save(IO::path file_sub_path = "", DUMP_FORMAT df = {.dim = DIM}) {
+    push();
+    const qsf_dump_format f = dump_of(df);
+    char out[4096];
+    GPU::check(qsf_save(grid(), file_sub_path.c_str(), &f, IO::psi_ext, out, sizeof out), "qsf_save");
+    return std::filesystem::current_path() / out;
+  }
+  void load(IO::path input_path) {
+    push();
+    GPU::check(qsf_load(grid(), input_path.c_str(), IO::psi_ext, nullptr, nullptr), "qsf_load");
+  }
+  void backup(const ind step) {
+    push();
+    GPU::check(qsf_backup(grid(), step, IO::psi_ext), "qsf_backup");
+  }
+  void restore() {
+    push();
+    GPU::check(qsf_restore(grid(), IO::psi_ext, nullptr), "qsf_restore");
+  }
+  void remove_backups() { GPU::check(qsf_remove_backups(IO::psi_ext), "qsf_remove_backups"); }
+  void snapshot(std::string extra_info, DUMP_FORMAT df = {.dim = DIM}) {
+    static ind x_count = 0;
+    static ind p_count = 0;
+    ind& count = df.rep == REP::X ? x_count : p_count;
+    push();
+    const qsf_dump_format f = dump_of(df);
+    const std::string ext = std::string(IO::psi_ext) + std::to_string(MPI::region);
+    GPU::check(qsf_save(grid(), ("snapshot_" + std::to_string(count) + extra_info).c_str(), &f, ext.c_str(),
+                        nullptr, 0),
+               "qsf_save");
+    count++;
+  }
+  void orthogonalizeWith(IO::path input_path, std::string ext = IO::psi_ext) {
+    push();
+    GPU::check(qsf_orthogonalize_with(grid(), input_path.c_str(), ext.c_str(), nullptr, nullptr),
+               "qsf_orthogonalize_with");
+  }
 
   // addUsingCoordinateFunction (grid.h:775-778): psi += f(x...) on the host copy
   template <class F, REP R = REP::X> void addUsingCoordinateFunction(F&& f) {

@@ -304,11 +304,34 @@ class Propagator:
             return self.step <= self.max_steps
         return abs(self.dif_energy) > self.state_accuracy and self.step != self.max_steps
 
-    # propagator.h:311-346
-    def make_step(self):
+    order: int = 1  # MultiProductSplit<Split3Base<X,P,X>, order>
+
+    @staticmethod
+    def chain_mults(chain: int) -> List[float]:
+        """_SplitChain::pack for Split3Base with `chain` coefficients 1/chain, joined X
+        sub-steps (splitting.h:43-58): X, then (P, X) `chain` times."""
+        c = 1.0 / chain
+        arr = [0.0] * (2 * chain + 1)
+        for j in range(chain):
+            for k, mult in enumerate((0.5, 1.0, 0.5)):
+                arr[2 * j + k] += mult * c
+        return arr
+
+    @staticmethod
+    def chain_value(chain: int, order: int) -> float:
+        """MultiProductSplit::Chain::value (splitting.h:82-85)."""
+        v = 1.0
+        for j in range(1, order + 1):
+            v *= (float(chain * chain) / (float(chain * chain) - float(j * j))) if j != chain else 1.0
+        return v
+
+    # propagator.h:311-328 chainEvolve
+    def _chain_evolve(self, chain: int):
         g = self.grid
         c = g.coupling
-        for si, (rep, mult) in enumerate(((REP_X, 0.5), (REP_P, 1.0), (REP_X, 0.5))):
+        mults = self.chain_mults(chain)
+        for si, mult in enumerate(mults):
+            rep = REP_X if si % 2 == 0 else REP_P
             if si > 0:
                 g.fourier(rep)
             if rep == c.couples_in:
@@ -317,6 +340,29 @@ class Propagator:
             g.evolve(self.mode, rep, self.dt * mult, cv)
             if rep == c.couples_in:
                 self.timer += self.dt * (mult * 1.0)
+
+    # propagator.h:331-343 makeStep with chainBackup / chainRestore / chainComplete
+    # (propagator.h:369-413) for order > 1, restated as written: the last chain is
+    # completed at `chain == ChainCount - 1`, so for order >= 2 the result of the step
+    # is the last chain's wavefunction alone.
+    def make_step(self):
+        g = self.grid
+        K = self.order
+        if K > 1:
+            psi_copy = g.psi.copy()
+            psi_acc = np.zeros_like(g.psi)
+            timer_copy = self.timer
+        for chain in range(1, K + 1):
+            if K > 1 and chain > 1:
+                self.timer = timer_copy
+                g.psi[...] = psi_copy
+            self._chain_evolve(chain)
+            if K > 1:
+                v = self.chain_value(chain, K)
+                if chain == K - 1:
+                    g.psi[...] = v * g.psi + psi_acc
+                else:
+                    psi_acc += v * g.psi
         self.step += 1
 
     # propagator.h:275-300 (+ 259-265 flux, 249-257 velocity-gauge correction)

@@ -7,7 +7,9 @@
 // against the single-rank MPI and FFTW stand-ins in oracle/ref/shim/.
 //
 // Usage: qsf_ref <case> <outdir> key=value ...
-//   cases: prim2d, prim3d, c1 (1D IM + RE), c2 (2D IM + RE VG), c3 (3D RE LG)
+//   cases: prim2d, prim3d, c1 (1D IM + RE), c2 (2D IM + RE VG), c3 (3D RE LG),
+//          io1 / io2 / io3 (.psi save / load / backup / orthogonalizeWith / snapshot),
+//          mp (1D real time with MultiProductSplit of order 2 and 3, VG and LG)
 #include "QSF.h"
 
 #include <map>
@@ -228,6 +230,83 @@ static void c3(const std::string& out) {
                                                        DipoleCoupling<VelocityGauge, F>(F(Sin2(field_cfg()))));
 }
 
+
+// ---------------------------------------------------------------- .psi I/O
+// Writes the reference's .psi files (grid.h:948-1153) from a seeded state: X and P
+// representation, complex and probability (doubles) payloads, downscale 2, the
+// evolution backup, a snapshot; then loads files back into fresh grids and runs
+// orthogonalizeWith, dumping the resulting wavefunctions.
+template <DIMS D> static void io(const std::string& out) {
+  using Ham = Schrodinger::Spin0<CapGrid<D>, Eberly>;
+  Ham wf(make_grid<D>(), make_pot());
+  const ind m = wf.m_l;
+  g_state = (uint64_t)par("seed", 3);
+  std::vector<cxd> psi0((size_t)m), psi1((size_t)m);
+  for (ind i = 0; i < m; i++) psi0[(size_t)i] = cxd(urand(), urand());
+  for (ind i = 0; i < m; i++) psi1[(size_t)i] = cxd(urand(), urand());
+  auto set = [&](Ham& w, const std::vector<cxd>& v) {
+    for (ind i = 0; i < m; i++) w[i] = v[(size_t)i];
+  };
+  set(wf, psi0);
+  dump(out + "/psi_in.bin", psi0.data(), m);
+  dump(out + "/psi_b.bin", psi1.data(), m);
+  wf.save("sx");
+  wf.save("sp", DUMP_FORMAT{.dim = D, .rep = REP::P});
+  dump(out + "/psi_after_sp.bin", &wf[0], m);
+  set(wf, psi0);
+  wf.save("sd", DUMP_FORMAT{.dim = D, .rep = REP::X, .complex = true, .downscale = 2});
+  wf.save("sdp", DUMP_FORMAT{.dim = D, .rep = REP::P, .complex = true, .downscale = 2});
+  set(wf, psi0);
+  wf.save("sn", DUMP_FORMAT{.dim = D, .rep = REP::X, .complex = false});
+  wf.backup(7);
+  wf.snapshot("_a");
+  {
+    Ham w2(make_grid<D>(), make_pot());
+    set(w2, psi1);
+    w2.load("sx_repX");
+    dump(out + "/psi_load_sx.bin", &w2[0], m);
+  }
+  {
+    Ham w3(make_grid<D>(), make_pot());
+    set(w3, psi1);
+    w3.load("sn_repX");
+    dump(out + "/psi_load_sn.bin", &w3[0], m);
+  }
+  {
+    Ham w4(make_grid<D>(), make_pot());
+    set(w4, psi1);
+    w4.orthogonalizeWith("sx_repX");
+    dump(out + "/psi_orth.bin", &w4[0], m);
+  }
+}
+
+
+// ---------------------------------------------------------------- multi-product
+// Real-time 1D runs from the field-free Gaussian with MultiProductSplit<Split3Base, K>
+// (splitting.h:63-91, propagator.h:331-413): final psi and the .dat rows.
+template <size_t K, class Coupling>
+static void mp_run(const std::string& out, const std::string& tag, Coupling&& c) {
+  using Ham = Schrodinger::Spin0<CapGrid<1>, Eberly, std::decay_t<Coupling>>;
+  using SplitK = MultiProductSplit<Split3Base<REP::X, REP::P, REP::X>, K>;
+  Ham wf(make_grid<1>(), make_pot(), std::forward<Coupling>(c));
+  wf.addUsingCoordinateFunction([](auto... x) { return gaussian(0.0, 1.0, x...); });
+  const ind m = wf.m_l;
+  dump(out + "/" + tag + "_psi0.bin", &wf[0], m);
+  SplitPropagator<MODE::RE, SplitK, Ham> re(
+      PropagatorBase{.dt = par("re_dt", 0.05), .max_steps = 0, .state_accuracy = 0}, std::move(wf), tag);
+  using Outs = BufferedBinaryOutputs<VALUE<Step, Time>, AVG<Identity>, AVG<PotentialEnergy>>;
+  re.run(Outs(BufferedOutputsBase{1, 1}), [&](WHEN when, ind, uind, auto& w) {
+    if (when == WHEN::AT_END) dump(out + "/" + tag + "_psi.bin", &w[0], m);
+  });
+}
+static void mp(const std::string& out) {
+  using F = Field<AXIS::X, Sin2>;
+  mp_run<2>(out, "MP2VG", DipoleCoupling<VelocityGauge, F>(F(Sin2(field_cfg()))));
+  mp_run<3>(out, "MP3VG", DipoleCoupling<VelocityGauge, F>(F(Sin2(field_cfg()))));
+  mp_run<2>(out, "MP2LG", DipoleCoupling<LengthGauge, F>(F(Sin2(field_cfg()))));
+  mp_run<3>(out, "MP3LG", DipoleCoupling<LengthGauge, F>(F(Sin2(field_cfg()))));
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) {
     fprintf(stderr, "usage: %s <case> <outdir> key=value...\n", argv[0]);
@@ -253,6 +332,10 @@ int main(int argc, char** argv) {
     else { fprintf(stderr, "box size %d not instantiated\n", b); return 2; }
   } else if (cs == "c2") c2(out);
   else if (cs == "c3") c3(out);
+  else if (cs == "mp") mp(out);
+  else if (cs == "io1") io<1>(out);
+  else if (cs == "io2") io<2>(out);
+  else if (cs == "io3") io<3>(out);
   else { fprintf(stderr, "unknown case %s\n", cs.c_str()); return 2; }
   return 0;
 }

@@ -104,6 +104,16 @@ class StepDesc(ctypes.Structure):
         ("energy_after_normalize", ctypes.c_int),
         ("kernel_ms", ctypes.POINTER(ctypes.c_float)),
         ("kernel_launches", ctypes.POINTER(ctypes.c_int64)),
+        ("substeps", ctypes.c_int),
+    ]
+
+
+class DumpFormat(ctypes.Structure):
+    _fields_ = [
+        ("rep", ctypes.c_int),
+        ("complex_values", ctypes.c_int),
+        ("downscale", ctypes.c_int64),
+        ("evo_backup", ctypes.c_int),
     ]
 
 
@@ -155,6 +165,13 @@ def lib():
         "qsf_server_wait": [vp, i64, ctypes.c_double, ctypes.POINTER(Result)],
         "qsf_server_stats_get": [vp, ctypes.POINTER(ServerStats)],
         "qsf_server_stop": [vp],
+        "qsf_save": [vp, ctypes.c_char_p, ctypes.POINTER(DumpFormat), ctypes.c_char_p, ctypes.c_char_p,
+                     ctypes.c_size_t],
+        "qsf_load": [vp, ctypes.c_char_p, ctypes.c_char_p, ip, dp],
+        "qsf_orthogonalize_with": [vp, ctypes.c_char_p, ctypes.c_char_p, dp, dp],
+        "qsf_backup": [vp, i64, ctypes.c_char_p],
+        "qsf_restore": [vp, ctypes.c_char_p, ctypes.POINTER(i64)],
+        "qsf_remove_backups": [ctypes.c_char_p],
     }
     for name, args in sig.items():
         f = getattr(L, name)

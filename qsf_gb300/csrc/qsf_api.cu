@@ -13,48 +13,22 @@
 #include <string>
 #include <vector>
 
-#include "qsf_gpu.h"
-#include "qsf_borders.h"
 #define QSF_DEFINE_KERNELS
-#include "qsf_kernels.cuh"
+#include "qsf_internal.h"
 
 using namespace qsf;
 
+namespace qsf {
 namespace {
-
 thread_local std::string g_err;
-
+}  // namespace
 int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+}  // namespace qsf
 
-#define QSF_CU(call)                                                                       \
-  do {                                                                                     \
-    cudaError_t e_ = (call);                                                               \
-    if (e_ != cudaSuccess) return fail(QSF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-template <class T>
-int dev_alloc(T*& p, size_t count) {
-  if (p) cudaFree(p);
-  p = nullptr;
-  if (count == 0) return QSF_OK;
-  if (cudaMalloc((void**)&p, count * sizeof(T)) != cudaSuccess) {
-    cudaGetLastError();
-    p = nullptr;
-    return fail(QSF_ENOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed");
-  }
-  return QSF_OK;
-}
-template <class T>
-int dev_reserve(T*& p, size_t& cap, size_t count) {
-  if (count <= cap && p) return QSF_OK;
-  size_t c = std::max(count, cap * 2);
-  int rc = dev_alloc(p, c);
-  cap = rc == QSF_OK ? c : 0;
-  return rc;
-}
+namespace {
 
 // the compile-time radix plan of qsf_fft.cuh, for reporting
 bool plan_radices(int64_t n, std::vector<int>& r) {
@@ -73,7 +47,7 @@ constexpr int kMaxTile = 4096;          // points per block in row / axis passes
 }  // namespace
 
 namespace qsf {
-void set_error_message(const std::string& msg) { g_err = msg; }
+void set_error_message(const std::string& msg) { fail(0, msg); }
 void add_sizes_p2a(std::vector<KernelSet>& out);
 void add_sizes_p2b(std::vector<KernelSet>& out);
 void add_sizes_r3(std::vector<KernelSet>& out);
@@ -85,65 +59,6 @@ const KernelSet* kernels_for(int n) {
 }
 }  // namespace qsf
 
-struct qsf_grid {
-  qsf_grid_desc desc{};
-  GridDev G{};
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  BorderNodes bn;
-  std::vector<double2*> tw_owned;
-  std::vector<longlong2*> twx_owned;
-  const KernelSet* ks = nullptr;  // kernels for this grid's line length
-  GridDev* dG = nullptr;          // device copy of G (step kernels read descriptors from device arrays)
-  StepDev* dS = nullptr;          // device copy of the current step descriptor
-  // static tables
-  longlong2* xs = nullptr;
-  long long* Vx = nullptr;
-  int xs_mode = 0;
-  double xs_delta = 0.0;
-  int xs_exp = 0;
-  int vshift = 0;
-  double vmax = 0.0, vneg = 0.0;  // max V and max -V over the grid
-  bool V_ready = false;
-  // per-step tables
-  longlong2* ptab = nullptr;
-  longlong2* xdyn = nullptr;
-  int nmax = 0;
-  int l2m = 0;
-  double m_mant = 1.0;
-  // fixed-point pass bookkeeping: [kTexp] table exponents, [4] pass minima, [4][scmax] block exponents
-  int* ibuf = nullptr;
-  int scmax = 1;
-  // reductions
-  double* partials = nullptr;
-  int pmax = 0;
-  double* fpartials = nullptr;
-  size_t fpmax = 0;
-  long long* ctl = nullptr;
-  double* energy = nullptr;
-  double* scale = nullptr;
-  double* rows_dev = nullptr;
-  size_t rows_cap = 0;
-  double* coup_dev = nullptr;
-  size_t coup_cap = 0;
-  // flux structures
-  std::vector<int> fl_borders;
-  int64_t fl_box = -1;
-  bool fl_ready = false;
-  double2* snap = nullptr;
-  long long* snap_idx = nullptr;
-  int* row_ptr = nullptr;
-  FluxPoint* fpts = nullptr;
-  FluxTerm* fterms = nullptr;
-  int nsnap = 0, nfterms = 0, nfpts = 0, nfblk = 1;
-  // launch geometry
-  int row_L = 1;
-  int nrowblk = 1;
-  size_t row_smem = 0;
-  int ax_C[3] = {1, 1, 1};
-  int ax_blocks[3] = {0, 0, 0};
-  size_t ax_smem[3] = {0, 0, 0};
-};
 
 namespace {
 
@@ -451,8 +366,10 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
     if ((rc = pf.end(kind))) return rc;     \
   } while (0)
   const int D = q.dim;
-  const dim3 gt(D * 3, count);  // one block per (kind, axis) table; X tables only in the length gauge
-  QSF_TIMED(QSF_K_TABLES, (k_tables<<<gt, 256, 0, st>>>(dG, dS)));
+  // (kind, axis) tables (X tables only in the length gauge), ~128 entries per block
+  const int tb = std::max(1, std::min(64, q.nmax / 128));
+  const dim3 gt(D * 3 * tb, count);
+  QSF_TIMED(QSF_K_TABLES, (k_tables<<<gt, 256, 0, st>>>(dG, dS, tb)));
   if (D == 1) {
     QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(1, count), kLineThreads, (size_t)q.n * sizeof(double2), st>>>(dG, dS)));
   } else {
@@ -489,9 +406,13 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   if (d->mode != QSF_MODE_IM && d->mode != QSF_MODE_RE) return fail(QSF_EINVAL, "mode must be IM or RE");
   if (d->nsteps < 1) return fail(QSF_EINVAL, "nsteps < 1");
   if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
+  if (d->substeps < 0 || d->substeps > 64) return fail(QSF_EINVAL, "substeps must be in [0, 64]");
   const GridDev& G = g->G;
+  const int K = std::max(1, d->substeps);
+  const int64_t total = d->nsteps * K;  // sub-steps
+  const double dt_sub = d->dt / K;
   int rc;
-  if ((rc = ensure_static(g, d->mode, d->dt * 0.5))) return rc;
+  if ((rc = ensure_static(g, d->mode, dt_sub * 0.5))) return rc;
   const bool want_flux = (d->obs & QSF_OBS_FLUX) && d->nborders > 0;
   if (want_flux && (rc = ensure_flux(g, d->nborders, d->border_types, d->box_size))) return rc;
   const int nb = want_flux ? d->nborders : 0;
@@ -500,12 +421,12 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   if ((rc = dev_reserve(g->rows_dev, g->rows_cap, (size_t)d->nsteps * ncol))) return rc;
   const double* coup = nullptr;
   if (d->coupling) {
-    if ((rc = dev_reserve(g->coup_dev, g->coup_cap, (size_t)d->nsteps * cstride))) return rc;
-    QSF_CU(cudaMemcpyAsync(g->coup_dev, d->coupling, (size_t)d->nsteps * cstride * sizeof(double),
+    if ((rc = dev_reserve(g->coup_dev, g->coup_cap, (size_t)total * cstride))) return rc;
+    QSF_CU(cudaMemcpyAsync(g->coup_dev, d->coupling, (size_t)total * cstride * sizeof(double),
                            cudaMemcpyHostToDevice, g->stream));
     coup = g->coup_dev;
   }
-  long long ctl_h[8] = {0, (long long)d->nsteps, 0, 0, 0, 0, 0, 0};
+  long long ctl_h[8] = {0, (long long)total, 0, 0, 0, 0, 0, 0};
   double en_h[2] = {d->last_energy, 0.0};
   double sc_h[2] = {1.0, 1.0};
   QSF_CU(cudaMemcpyAsync(g->ctl, ctl_h, sizeof(ctl_h), cudaMemcpyHostToDevice, g->stream));
@@ -513,8 +434,9 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   QSF_CU(cudaMemcpyAsync(g->scale, sc_h, sizeof(sc_h), cudaMemcpyHostToDevice, g->stream));
   StepDev S{};
   S.mode = d->mode;
-  S.dt = d->dt;
-  S.nsteps = d->nsteps;
+  S.dt = dt_sub;
+  S.nsteps = total;
+  S.substeps = K;
   S.coupling = coup;
   S.coup_stride = cstride;
   S.xs = g->xs;
@@ -1042,19 +964,19 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
     P.ms = d->kernel_ms;
     P.count = d->kernel_launches;
     rc = P.init(g->stream, 16);
-    for (int64_t k = 0; k < d->nsteps && rc == QSF_OK; ++k) {
+    for (int64_t k = 0; k < S.nsteps && rc == QSF_OK; ++k) {
       rc = launch_step(g, S, &P);
       if (rc == QSF_OK) rc = P.flush();
     }
     P.release();
     if (rc) return rc;
-  } else if (d->nsteps < 4) {
-    for (int64_t k = 0; k < d->nsteps; ++k)
+  } else if (S.nsteps < 4) {
+    for (int64_t k = 0; k < S.nsteps; ++k)
       if ((rc = launch_step(g, S))) return rc;
   } else {
     cudaGraphExec_t exec = nullptr;
     if ((rc = capture_graph(g->stream, [&]() { return launch_step(g, S); }, &exec))) return rc;
-    for (int64_t k = 0; k < d->nsteps; ++k) {
+    for (int64_t k = 0; k < S.nsteps; ++k) {
       const cudaError_t ce = cudaGraphLaunch(exec, g->stream);
       if (ce != cudaSuccess) {
         cudaGraphExecDestroy(exec);
@@ -1095,6 +1017,7 @@ int qsf_batch_destroy(qsf_batch* b) {
 
 int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot) {
   if (!b || !g || !d || !slot) return fail(QSF_EINVAL, "null argument");
+  if (d->substeps > 1) return fail(QSF_EINVAL, "batched solves run plain Strang steps (substeps <= 1)");
   for (auto& kv : b->members)
     if (kv.second.g == g) return fail(QSF_ESTATE, "grid is already in the batch");
   QSF_CU(cudaStreamSynchronize(b->stream));

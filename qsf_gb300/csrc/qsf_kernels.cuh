@@ -116,8 +116,10 @@ struct StepDev {
   const FluxTerm* fterms;
   int nfterms;
   double* fpartials;  // [nblk][kMaxFluxBorders]
-  // control (device): ctl[0] step within call, ctl[1] stop-after step (or nsteps),
-  // ctl[2] steps done, ctl[3] finalize block counter, ctl[4] NaN flag
+  // control (device): ctl[0] sub-step within call, ctl[1] stop after this sub-step
+  // (or nsteps), ctl[2] steps done, ctl[3] finalize block counter, ctl[4] NaN flag.
+  // nsteps counts sub-steps: steps * substeps (MultiProductSplit order).
+  int substeps;
   long long* ctl;
   double* energy_state;  // [0] last E
   double* rows;          // [nsteps][3 + nborders]
@@ -375,28 +377,31 @@ __device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& 
   return expop(S.mode, (S.dt * 0.5) * (xpos(a, i) * E));
 }
 
-// Per-step tables: one block per (kind, axis) table; each block normalises its table
-// to magnitude <= 1 and records the exponent it took out.  Axis 0's P table also
-// carries the mantissa of 1/m (its power of two goes into the exponent).  Block 0
-// resets the per-pass minimum exponents of the step.
-__global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss) {
+// Per-step tables: `tb` blocks per (kind, axis) table, each storing a contiguous slice.
+// A table whose exact values exceed 1 (imaginary time) is stored times 2^-e, e from
+// its maximum (every block of the table evaluates that maximum, so the slices agree),
+// and e is recorded in texp.  Axis 0's P table also carries the mantissa of 1/m (its
+// power of two goes into the exponent).  Block 0 resets the per-pass minimum
+// exponents of the step.
+__global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
+                                                int tb) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   __shared__ double red[32];
   __shared__ int e_sh;
   const int D = g.dim;
-  const int kind = blockIdx.x / D, d = blockIdx.x % D;
+  const int table = blockIdx.x / tb, part = blockIdx.x % tb;
+  const int kind = table / D, d = table % D;
   if (kind > 0 && g.gauge != 1) return;
   if (blockIdx.x == 0 && threadIdx.x < 4) S.gmin[threadIdx.x] = 0x7fffffff;
   const long long step = S.ctl[0];
   const double* cp = S.coupling ? S.coupling + step * S.coup_stride : nullptr;
   const int n = g.ax[d].n;
   const double mant = (kind == 0 && d == 0) ? S.m_mant : 1.0;
-  double mx = 0.0;
   if (S.mode == 1) {  // imaginary time: real factors that may exceed 1
+    double mx = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, table_entry(g, S, cp, kind, d, i).x * mant);
-    // block max via the sum helper's layout
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
@@ -404,20 +409,21 @@ __global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, 
       double m2 = 0.0;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m2 = fmax(m2, red[w]);
       int e = 0;
-      if (m2 > 1.0) {
-        frexp(m2, &e);  // m2 < 2^e
-      }
+      if (m2 > 1.0) frexp(m2, &e);  // m2 < 2^e
       e_sh = e;
-      S.texp[kind * 3 + d] = e;
+      if (part == 0) S.texp[kind * 3 + d] = e;
     }
     __syncthreads();
   } else {
-    if (threadIdx.x == 0) S.texp[kind * 3 + d] = 0;
-    e_sh = 0;
+    if (part == 0 && threadIdx.x == 0) S.texp[kind * 3 + d] = 0;
+    if (threadIdx.x == 0) e_sh = 0;
+    __syncthreads();
   }
   const double sc = ldexp(mant, -e_sh);
   longlong2* out = kind == 0 ? S.ptab + (size_t)d * S.nmax : S.xdyn + ((size_t)(kind - 1) * D + d) * S.nmax;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  const int chunk = (n + tb - 1) / tb;
+  const int i1 = min(n, (part + 1) * chunk);
+  for (int i = part * chunk + threadIdx.x; i < i1; i += blockDim.x) {
     const double2 f = table_entry(g, S, cp, kind, d, i);
     out[i] = to_fx62(make_double2(fmin(fmax(f.x * sc, -1.0), 1.0), fmin(fmax(f.y * sc, -1.0), 1.0)));
   }
@@ -974,10 +980,13 @@ __global__ void __launch_bounds__(256) k_finalize(const GridDev* __restrict__ Gs
   if (!step_active(S)) return;
   __shared__ double red[32 * kMaxFluxBorders];
   __shared__ int is_last;
-  const long long step = S.ctl[0];
+  const long long sub = S.ctl[0];
+  // observables, Normalize and the convergence test once per step (its last sub-step)
+  const bool step_end = (sub + 1) % S.substeps == 0;
+  const long long step = sub / S.substeps;
   const int nb = S.nborders;
-  if (S.nfterms > 0) {
-    const double* A = (g.gauge == 0 && S.coupling && g.n_fields) ? S.coupling + step * S.coup_stride : nullptr;
+  if (S.nfterms > 0 && step_end) {
+    const double* A = (g.gauge == 0 && S.coupling && g.n_fields) ? S.coupling + sub * S.coup_stride : nullptr;
     const int chunk = (S.nfterms + gridDim.x - 1) / gridDim.x;
     const int t0 = blockIdx.x * chunk, t1 = min(S.nfterms, t0 + chunk);
     flux_block(g, S.fpts, S.fterms, t0, t1, S.snap, A, nb, red, S.fpartials + blockIdx.x * kMaxFluxBorders);
@@ -991,6 +1000,14 @@ __global__ void __launch_bounds__(256) k_finalize(const GridDev* __restrict__ Gs
   __syncthreads();
   if (!is_last) return;
   __threadfence();
+  if (!step_end) {
+    if (threadIdx.x == 0) {
+      if (S.normalize) *S.scale = 1.0;  // no Normalize between sub-steps
+      S.ctl[3] = 0;
+      S.ctl[0] = sub + 1;
+    }
+    return;
+  }
   // last block: deterministic sums in a fixed order
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < S.nrowblk; i += blockDim.x) {
@@ -1029,11 +1046,12 @@ __global__ void __launch_bounds__(256) k_finalize(const GridDev* __restrict__ Gs
       const double E = epot * se + ekin * sk;
       const double dE = E - S.energy_state[0];
       S.energy_state[0] = E;
-      if (S.ctl[1] >= S.nsteps && fabs(dE) <= S.state_accuracy) S.ctl[1] = step + 1;
+      // converged: one more step runs (its last sub-step is sub + substeps)
+      if (S.ctl[1] >= S.nsteps && fabs(dE) <= S.state_accuracy) S.ctl[1] = sub + S.substeps;
     }
     S.ctl[2] = step + 1;
     S.ctl[3] = 0;
-    S.ctl[0] = step + 1;
+    S.ctl[0] = sub + 1;
   }
 }
 

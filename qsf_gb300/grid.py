@@ -11,13 +11,14 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from ._lib import GridDesc, KERNEL_KINDS, StepDesc, MAX_BORDERS, check, lib
+from ._lib import DumpFormat, GridDesc, KERNEL_KINDS, StepDesc, MAX_BORDERS, check, lib
 
 MODE_IM, MODE_RE = 1, 2
 REP_X, REP_P = 1, 2
 OP_IDENTITY, OP_POTENTIAL, OP_KINETIC = 0, 1, 2
 POT_EBERLY, POT_ECKHARDT_SACHA, POT_COULOMB, POT_NONE = 0, 1, 2, 3
 OBS_NORM, OBS_EPOT, OBS_EKIN, OBS_FLUX = 1, 2, 4, 8
+PSI_EXT = ".psi"  # io.h:25
 
 BORDERS = {
     "BOX": 0, "S2CAP": 1, "D2CAP": 2, "N2S": 3, "N2D": 4, "N2D_SYM": 5, "N2D_ASYM": 6,
@@ -131,6 +132,59 @@ class Grid:
     def add_gaussian(self, at: float = 0.0, delta: float = 1.0) -> None:
         check(lib().qsf_add_gaussian(self._h, at, delta), "qsf_add_gaussian")
 
+    # ------------------------------------------------------------ .psi files
+    # Paths are relative to the working directory, as in the reference.
+    _snapshot_counts = {}
+
+    def save(self, path: str = "", rep: int = REP_X, complex: bool = True, downscale: int = 1,
+             evo_backup: bool = False, ext: str = PSI_EXT) -> str:
+        """save / _save_centered / _save (grid.h:1087-1114, 994-1071); returns the path written."""
+        df = DumpFormat(rep, 1 if complex else 0, int(downscale), 1 if evo_backup else 0)
+        buf = ctypes.create_string_buffer(4096)
+        check(lib().qsf_save(self._h, path.encode(), ctypes.byref(df), ext.encode(), buf, 4096), "qsf_save")
+        return buf.value.decode()
+
+    def load(self, path: str, ext: str = PSI_EXT) -> float:
+        """load / _load (grid.h:789-859); returns the norm after loading.  self.load_warnings
+        holds the reader's warning bits (1: n differs, 2: dx differs, 4: |psi|^2 file,
+        8: file shorter than the grid)."""
+        w = ctypes.c_int(0)
+        nrm = ctypes.c_double(0.0)
+        check(lib().qsf_load(self._h, path.encode(), ext.encode(), ctypes.byref(w), ctypes.byref(nrm)), "qsf_load")
+        self.load_warnings = int(w.value)
+        return float(nrm.value)
+
+    def orthogonalize_with(self, path: str, ext: str = PSI_EXT):
+        """orthogonalizeWith (grid.h:909-946); returns (<psi_file|psi> dV, norm after)."""
+        ov = (ctypes.c_double * 2)()
+        nrm = ctypes.c_double(0.0)
+        check(lib().qsf_orthogonalize_with(self._h, path.encode(), ext.encode(), ov, ctypes.byref(nrm)),
+              "qsf_orthogonalize_with")
+        return complex(ov[0], ov[1]), float(nrm.value)
+
+    def backup(self, step: int, ext: str = PSI_EXT) -> None:
+        """_backup (grid.h:1116-1127): backup.info and backup<ext>."""
+        check(lib().qsf_backup(self._h, int(step), ext.encode()), "qsf_backup")
+
+    def restore(self, ext: str = PSI_EXT) -> int:
+        """restore (grid.h:949-953); returns the step stored in backup.info."""
+        st = ctypes.c_int64(0)
+        check(lib().qsf_restore(self._h, ext.encode(), ctypes.byref(st)), "qsf_restore")
+        return int(st.value)
+
+    @staticmethod
+    def remove_backups(ext: str = PSI_EXT) -> None:
+        check(lib().qsf_remove_backups(ext.encode()), "qsf_remove_backups")
+
+    def snapshot(self, extra_info: str = "", rep: int = REP_X, complex: bool = True, downscale: int = 1) -> str:
+        """snapshot (grid.h:1133-1152): snapshot_<count><extra_info>_rep{X,P}.psi0, one
+        counter per (dimension, representation) like the reference's function statics."""
+        key = (self.dim, rep)
+        cnt = Grid._snapshot_counts.get(key, 0)
+        Grid._snapshot_counts[key] = cnt + 1
+        return self.save("snapshot_" + str(cnt) + extra_info, rep=rep, complex=complex, downscale=downscale,
+                         ext=PSI_EXT + "0")
+
     # ------------------------------------------------------------ fused steps
     def step_desc(self, mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None,
                   obs: int = OBS_NORM, normalize: bool = False, borders: Sequence[str] = (), box_size: int = 0,
@@ -159,15 +213,18 @@ class Grid:
     def step(self, mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None, obs: int = OBS_NORM,
              normalize: bool = False, borders: Sequence[str] = (), box_size: int = 0,
              state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0,
-             profile: Optional[dict] = None):
+             profile: Optional[dict] = None, substeps: int = 1):
         """Run nsteps fused Strang steps; returns (rows [nsteps, 3 + nb], steps_done).
 
+        substeps = K > 1 runs each step as MultiProductSplit<Split3Base, K> does (K
+        sub-steps of dt / K; coupling then has nsteps * K rows, one per sub-step).
         With `profile` (a dict), every launch is timed with CUDA events on the grid's
         stream; per kernel kind the summed ms and launch counts are added to it."""
         d = StepDesc()
         d.mode = mode
         d.dt = dt
         d.nsteps = int(nsteps)
+        d.substeps = int(substeps)
         cp = None
         if coupling is not None:
             cp = np.ascontiguousarray(coupling, dtype=np.float64)

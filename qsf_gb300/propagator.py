@@ -16,6 +16,8 @@ the normalised wavefunction, as in computeEach.
 """
 from __future__ import annotations
 
+import os
+import struct
 from typing import List, Optional
 
 import numpy as np
@@ -29,9 +31,59 @@ def _is_flux(o) -> bool:
     return isinstance(o, tuple) and o[0] == "flux"
 
 
+def chain_mults(chain: int) -> List[float]:
+    """_SplitChain::pack for Split3Base with `chain` coefficients 1/chain (splitting.h:43-58):
+    X, then (P, X) `chain` times, the inner X halves joined."""
+    c = 1.0 / chain
+    arr = [0.0] * (2 * chain + 1)
+    for j in range(chain):
+        for k, mult in enumerate((0.5, 1.0, 0.5)):
+            arr[2 * j + k] += mult * c
+    return arr
+
+
+def coupling_schedule(coupling: Coupling, dt: float, nsteps: int, timer: float = 0.0, order: int = 1):
+    """Coupling rows of nsteps makeStep()s from `timer` on, as qsf_step takes them, and the
+    timer afterwards; advances the coupling's state (propagator.h:311-346, 369-413).
+
+    One row per sub-step (order rows per step).  Velocity gauge: A at each P sub-step;
+    length gauge: E at the sub-step's opening and closing X half.  Every chain of a
+    multi-product step evaluates the coupling at its sub-steps with the timer restored
+    to the step's start but the coupling state (the PromoteFieldToA integral) carried
+    over; only the last chain's values are kept, as only the last chain's wavefunction
+    survives the step."""
+    lg = coupling.couples_in_x
+    K = int(order)
+    rows = np.zeros((nsteps * K, 6 if lg else 3))
+    for s in range(nsteps):
+        t_start = timer
+        t = t_start
+        for chain in range(1, K + 1):
+            t = t_start
+            vals = []
+            for si, mult in enumerate(chain_mults(chain)):
+                if (si % 2 == 0) == lg:
+                    coupling.precalc(t)
+                    vals.append(list(coupling.vector()))
+                    t += dt * (mult * 1.0)
+            if chain == K:
+                for k in range(K):
+                    if lg:
+                        rows[s * K + k, 0:3] = vals[k]
+                        rows[s * K + k, 3:6] = vals[k + 1]
+                    else:
+                        rows[s * K + k, 0:3] = vals[k]
+        timer = t
+    return rows, timer
+
+
 class SplitPropagator:
     def __init__(self, mode: int, dt: float, max_steps: int, grid: Grid, coupling: Coupling, outputs: list,
-                 state_accuracy: float = 0.0):
+                 state_accuracy: float = 0.0, order: int = 1):
+        """SplitPropagator<M, MultiProductSplit<Split3Base<X,P,X>, order>, Spin0<...>>."""
+        self.order = int(order)
+        if not 1 <= self.order <= 64:
+            raise ValueError("order must be in [1, 64]")
         self.mode = mode
         self.dt = dt
         self.grid = grid
@@ -52,27 +104,11 @@ class SplitPropagator:
         self.flux_spec = next((o for o in self.outputs if _is_flux(o)), None)
 
     # ------------------------------------------------------------ schedule
-    def _schedule(self, nsteps: int) -> np.ndarray:
-        """Coupling rows for the next nsteps steps; advances timer and coupling state.
+    chain_mults = staticmethod(chain_mults)
 
-        Velocity gauge: A at the P sub-step (precalc at the step's start time, then the
-        timer advances by dt).  Length gauge: E at the first X half, timer += dt/2,
-        E at the second X half, timer += dt/2 (propagator.h:319-329)."""
-        c = self.coupling
-        lg = c.couples_in_x
-        rows = np.zeros((nsteps, 6 if lg else 3))
-        for s in range(nsteps):
-            if lg:
-                c.precalc(self.timer)
-                rows[s, 0:3] = c.vector()
-                self.timer += self.dt * (0.5 * 1.0)
-                c.precalc(self.timer)
-                rows[s, 3:6] = c.vector()
-                self.timer += self.dt * (0.5 * 1.0)
-            else:
-                c.precalc(self.timer)
-                rows[s, 0:3] = c.vector()
-                self.timer += self.dt * (1.0 * 1.0)
+    def _schedule(self, nsteps: int) -> np.ndarray:
+        """Coupling rows for the next nsteps steps; advances timer and coupling state."""
+        rows, self.timer = coupling_schedule(self.coupling, self.dt, nsteps, self.timer, self.order)
         return rows
 
     # ------------------------------------------------------------ outputs
@@ -156,7 +192,7 @@ class SplitPropagator:
         rows, done = self.grid.step(self.mode, self.dt, nsteps, sched if self.coupling.size else None,
                                     obs=self._obs_mask(), normalize="normalize" in self.outputs, borders=borders,
                                     box_size=box, state_accuracy=acc, last_energy=self._last_change,
-                                    energy_after_normalize=self._energy_after_normalize())
+                                    energy_after_normalize=self._energy_after_normalize(), substeps=self.order)
         if done < nsteps:
             # the schedule ran ahead of the device: replay the host state to `done` steps
             self.timer = timer0
@@ -171,25 +207,42 @@ class SplitPropagator:
         return done
 
     def _times(self, t0: float, n: int) -> List[float]:
+        """Timer after each of n steps: the last chain's increments (incrementBy,
+        propagator.h:327-330) over the sub-steps of the coupling's representation."""
+        lg = self.coupling.couples_in_x
+        incs = [m for si, m in enumerate(chain_mults(self.order)) if (si % 2 == 0) == lg]
         out = []
         t = t0
         for _ in range(n):
-            if self.coupling.couples_in_x:
-                t += self.dt * (0.5 * 1.0)
-                t += self.dt * (0.5 * 1.0)
-            else:
-                t += self.dt * (1.0 * 1.0)
+            for m in incs:
+                t += self.dt * (m * 1.0)
             out.append(t)
         return out
 
-    def run(self) -> List[dict]:
-        self.rows.append(self.compute_at_start())
+    def run(self, restore: bool = False) -> List[dict]:
+        """SplitPropagator::run (propagator.h:420-462).  With restore, the step stored in
+        backup.info is read, the timer and coupling are fast-forwarded to it without
+        evolving (makeFakeStep, propagator.h:362-366) and the backed-up psi is loaded;
+        the AT_START outputs are then skipped.  At the end backup.info and the backup
+        file are removed, as the reference does."""
+        if restore:
+            with open("backup.info", "rb") as f:
+                atstep = struct.unpack("<q", f.read(8))[0]
+            if atstep > self.step:
+                self._schedule(atstep - self.step)
+                self.step = atstep
+            self.grid.restore()
+        else:
+            self.rows.append(self.compute_at_start())
         if self.mode == MODE_RE:
             # loop while step <= max_steps, then the final step (propagator.h:443-451)
-            self.run_steps(self.max_steps + 2)
+            self.run_steps(max(0, self.max_steps + 1 - self.step) + 1)
         else:
-            if not (abs(self.dif_energy) > self.state_accuracy):
+            if not (abs(self.dif_energy) > self.state_accuracy) or self.step == self.max_steps:
                 self.run_steps(1)
             else:
-                self.run_steps(self.max_steps + 1, stop_on_convergence=self.state_accuracy > 0.0)
+                self.run_steps(self.max_steps + 1 - self.step, stop_on_convergence=self.state_accuracy > 0.0)
+        if os.path.exists("backup.info"):
+            os.remove("backup.info")
+        self.grid.remove_backups()
         return self.rows

@@ -25,6 +25,14 @@ int main(int argc, char** argv) {
   using IMOuts = BufferedBinaryOutputs<VALUE<Step>, AVG<Identity>, OPERATION<Normalize>, AVG<PotentialEnergy>,
                                       AVG<KineticEnergy>, ENERGY_TOTAL, ENERGY_DIFFERENCE>;
   im.run(IMOuts(BufferedOutputsBase{1, 1}));
+  // .psi files of the ground state: X and centred P representation, a snapshot, an
+  // evolution backup read back, and a projection onto the saved state
+  im.wf.save("ground");
+  im.wf.save("ground", DUMP_FORMAT{.dim = 2, .rep = REP::P});
+  im.wf.snapshot("_ground");
+  im.wf.backup(0);
+  im.wf.restore();
+  im.wf.remove_backups();
   _FieldConfig fc{.field = 0.1, .omega = 1.0, .ncycles = 1.0, .FWHM_percent = 0, .phase_in_pi_units = 0,
                   .delay_in_cycles = 0};
   using C = DipoleCoupling<VelocityGauge, F>;
@@ -35,6 +43,7 @@ int main(int argc, char** argv) {
   for (ind i = 0; i < re.wf.localSize(); ++i) re.wf[i] = im.wf[i];
   using REOuts = BufferedBinaryOutputs<VALUE<Step, Time>, AVG<Identity>, AVG<PotentialEnergy>, ZOA_FLUX_2D>;
   re.run(REOuts(BufferedOutputsBase{1, 1}));
+  re.wf.orthogonalizeWith("ground_repX");
   printf("norm after the pulse: %.12f\n", re.wf.template average<REP::X, Identity>());
   return 0;
 }

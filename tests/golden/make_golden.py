@@ -38,7 +38,18 @@ CASES = {
     "c3_lg": ("c3", dict(n=16, dx=0.4, nCAP=2, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=20,
                          re_dt=0.05, F0=0.1688, omega=1.5, ncycles=1, phase=0.0, p_NS=4, p_SD=3, p_DT=2, p_CAP=6,
                          lg=1), 6, 13, 3),
+    # .psi files written by the reference's own save / backup / snapshot, and the
+    # wavefunctions its load / orthogonalizeWith produce (grid.h:789-1153)
+    # MultiProductSplit<Split3Base, K> real-time runs, K = 2, 3, both gauges
+    "mp": ("mp", dict(n=256, dx=0.2, nCAP=25, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, re_dt=0.05, F0=0.05,
+                      omega=0.5, ncycles=1, phase=0.0), 0, 4, 1),
+    "io1": ("io1", dict(n=16, dx=0.3, nCAP=2, seed=3), 0, 0, 1),
+    "io2": ("io2", dict(n=8, dx=0.5, nCAP=1, seed=5), 0, 0, 2),
+    "io3": ("io3", dict(n=8, dx=0.4, nCAP=1, seed=9), 0, 0, 3),
 }
+
+IO_FILES = ("sx_repX.psi", "sp_repP.psi", "sd_scale2_repX.psi", "sdp_scale2_repP.psi", "sn_repX.psi",
+            "backup.psi", "backup.info", "snapshot_0_a_repX.psi0")
 
 
 def _read_psi(path, shape):
@@ -52,7 +63,17 @@ def make(name):
         args = [REF, case, tmp] + [f"{k}={v}" for k, v in params.items()]
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL)
         out = {"params": json.dumps(params), "case": case, "dim": dim}
-        if case.startswith("prim"):
+        if case == "mp":
+            for tag in ("MP2VG", "MP3VG", "MP2LG", "MP3LG"):
+                out[tag + "_psi0"] = _read_psi(os.path.join(tmp, tag + "_psi0.bin"), shape)
+                out[tag + "_psi"] = _read_psi(os.path.join(tmp, tag + "_psi.bin"), shape)
+                out[tag + "_rows"] = np.fromfile(os.path.join(tmp, tag + ".dat"), dtype=np.float64).reshape(-1, re_cols)
+        elif case.startswith("io"):
+            for f in ("psi_in", "psi_b", "psi_after_sp", "psi_load_sx", "psi_load_sn", "psi_orth"):
+                out[f] = _read_psi(os.path.join(tmp, f + ".bin"), shape)
+            for f in IO_FILES:
+                out["file:" + f] = np.fromfile(os.path.join(tmp, f), dtype=np.uint8)
+        elif case.startswith("prim"):
             for f in ("psi_in", "psi_xre", "psi_xim", "psi_p", "psi_back", "psi_pvg", "psi_norm"):
                 out[f] = _read_psi(os.path.join(tmp, f + ".bin"), shape)
             out["scalars"] = np.fromfile(os.path.join(tmp, "prim.bin"), dtype=np.float64)

@@ -17,9 +17,8 @@ def _req(Q, S, dim, n, F0, omega, gauge=0):
                     border_nodes=(6, 4, 3, 12))
     c = Q.Coupling(gauge, [Q.Field({1: 1, 2: 3, 3: 7}[dim], [Q.Pulse(field=F0, omega=omega, ncycles=1.0)])])
     steps = int(c.max_pulse_duration() / 0.05 + 1) + 2
-    prop = Q.SplitPropagator.__new__(Q.SplitPropagator)
-    prop.coupling, prop.dt, prop.timer = c, 0.05, 0.0
-    sched = Q.SplitPropagator._schedule(prop, steps)
+    from qsf_gb300.propagator import coupling_schedule
+    sched, _ = coupling_schedule(c, 0.05, steps)
     borders = [] if dim == 1 else (Q.ZOA_FLUX_2D if dim == 2 else Q.ZOA_FLUX_3D)
     return dict(gdesc=d, mode=Q.MODE_RE, dt=0.05, nsteps=steps, coupling=sched, obs=Q.OBS_NORM | Q.OBS_EPOT,
                 borders=borders)
