@@ -4,12 +4,13 @@
 // instructions, so the split step's FFTs run on the integer pipes: a line (or a tile
 // of lines) is held as 64-bit integers sharing one power-of-two block exponent,
 // value = int * 2^-scale.  Additions are exact; products by twiddles and butterfly
-// constants are 64 x 64 -> 128-bit products rounded back to 64 bits (constants carry
-// 62 fractional bits).  After every radix pass the block is renormalised so that its
-// largest component again uses all bits the next pass can afford (62 minus the pass's
-// growth), i.e. block floating point with a 55-60 bit mantissa at every pass.  Against
-// an exact DFT this is ~4x more accurate than an FP64 FFT (normwise relative error
-// ~5e-17 vs ~2e-16 at N = 48 .. 4096); FP64 storage of psi is unchanged.
+// constants (62 fractional bits) keep the top 64 bits of the 124-bit product to within
+// 2.5 units, from three 32 x 32 -> 64-bit partial products.  After every radix pass the
+// block is renormalised so that its largest component again uses all bits the next
+// pass can afford (62 minus the pass's growth), i.e. block floating point with a 55-60
+// bit mantissa at every pass.  Against an exact DFT this is ~2.5x more accurate than an
+// FP64 FFT (normwise relative error ~9e-17 vs ~2.3e-16 at N = 48 .. 2048); FP64
+// storage of psi is unchanged.
 //
 // Radix plans, pass structure and index maps are those of qsf_fft.cuh.
 #pragma once
@@ -23,17 +24,17 @@ namespace qsf {
 typedef long long i64;
 typedef unsigned long long u64;
 
-// round(a * w / 2^62)
+// a * w / 2^62 for w in 2^62 fixed point, from three 32 x 32 -> 64-bit partial
+// products (IMAD.WIDE): the low x low product is dropped and the result centred, so it
+// lies within 2.5 units of the exact quotient.  Needs |a|, |w| < 2^62.5.
 __device__ __forceinline__ i64 mulq62(i64 a, i64 w) {
-  const i64 hi = __mul64hi(a, w);
-  const u64 lo = (u64)a * (u64)w;
-  return (i64)(((u64)hi << 2) | (lo >> 62)) + (i64)((lo >> 61) & 1ull);
-}
-// round(a * w / 2^60): phase-table factors (|w| < 4)
-__device__ __forceinline__ i64 mulq60(i64 a, i64 w) {
-  const i64 hi = __mul64hi(a, w);
-  const u64 lo = (u64)a * (u64)w;
-  return (i64)(((u64)hi << 4) | (lo >> 60)) + (i64)((lo >> 59) & 1ull);
+  const int ah = (int)(a >> 32), wh = (int)(w >> 32);
+  const unsigned al = (unsigned)a, wl = (unsigned)w;
+  const i64 hh = (i64)ah * (i64)wh;
+  // signed x unsigned: unsigned wide product, corrected for a negative signed factor
+  const i64 m1 = (i64)((u64)(unsigned)ah * (u64)wl) - (ah < 0 ? (i64)((u64)wl << 32) : 0);
+  const i64 m2 = (i64)((u64)(unsigned)wh * (u64)al) - (wh < 0 ? (i64)((u64)al << 32) : 0);
+  return (hh << 2) + (((m1 >> 1) + (m2 >> 1) + (3LL << 28)) >> 29);
 }
 
 __device__ __forceinline__ longlong2 fadd(longlong2 a, longlong2 b) { return make_longlong2(a.x + b.x, a.y + b.y); }
@@ -46,10 +47,6 @@ __device__ __forceinline__ longlong2 fmul62(longlong2 a, longlong2 w) {
   const i64 k2 = mulq62(a.x, w.y - w.x);
   const i64 k3 = mulq62(a.y, w.x + w.y);
   return make_longlong2(k1 - k3, k1 + k2);
-}
-// a * w with w in 2^60 fixed point (|w| < 4)
-__device__ __forceinline__ longlong2 fmul60(longlong2 a, longlong2 w) {
-  return make_longlong2(mulq60(a.x, w.x) - mulq60(a.y, w.y), mulq60(a.x, w.y) + mulq60(a.y, w.x));
 }
 // OR of the component magnitudes (x ^ (x >> 63) is |x| or |x| - 1): its bit length is
 // the block maximum's bit length, or one less when that maximum is a negative power of two
