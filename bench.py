@@ -213,7 +213,7 @@ def cpu_baseline(all_cores: bool, budget_s: float = 20.0):
 
 # ------------------------------------------------------------------ batched / served
 BATCH_EDGES = [256, 384, 512, 768, 1024]
-SERVE_1D = [1024, 1280, 1536, 2048, 2560, 3072, 4096, 5120, 6144, 8192]
+SERVE_1D = [1024, 1280, 1536, 2048, 2560, 3072, 4096, 5120, 6144, 8192, 10240, 12288, 16384]
 SERVE_2D = [256, 320, 384, 512, 640, 768, 1024]
 
 
@@ -277,7 +277,7 @@ def run_batched(steps, warmup, nsolves=256, seed=0):
 
 
 def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128):
-    """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N in 1024..8192) and 2D
+    """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N in 1024..16384) and 2D
     (edge in 256..1024) solves with seeded pulses; each solve runs its first
     `steps_per_solve` steps.  Returns throughput and p50/p99 submit->completion."""
     import qsf_gb300 as Q
@@ -322,7 +322,7 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128):
     pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
     return {"rate_per_s": rate, "submitted": len(tickets), "completed": len(lat), "value": pts / wall, "unit": UNIT,
             "p50_s": pct(0.50), "p99_s": pct(0.99), "wall_s": wall,
-            "workload": f"served: Poisson {rate}/s for {duration_s}s, 50/50 1D N in [1024,8192] / 2D edge in "
+            "workload": f"served: Poisson {rate}/s for {duration_s}s, 50/50 1D N in [1024,16384] / 2D edge in "
                         f"[256,1024] (2^a 3^b 5^c sizes), I log-U[1e14,1e15], lambda U[400,1600] nm, "
                         f"{steps_per_solve} steps per solve, seed {seed}"}
 

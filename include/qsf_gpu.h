@@ -278,6 +278,17 @@ int qsf_server_stats_get(qsf_server* s, qsf_server_stats* out);
 /* finishes the solves in flight, drops the queued ones (status QSF_ESTATE), joins */
 int qsf_server_stop(qsf_server* s);
 
+/* ------------------------------------------------- other LocalGrid members */
+/* average_der<X, dir, PotentialEnergy> (grid.h:443-465), the AVG<DERIVATIVE<dir,
+ * PotentialEnergy>> output (computations.h:73, propagator.h:242-247):
+ * sum |psi|^2 (V(x + dx e_dir) - V(x - dx e_dir)) dV / (2 dx_dir). */
+int qsf_average_der(qsf_grid* g, int dir, double* out);
+/* operation<M, R, AntiSymmetrize<particles>> (grid.h:611-723) on one rank:
+ * particles 2 in 2D: psi(x, y) -= psi(y, x); particles 2 in 3D: the same for the last
+ * two coordinates, psi(x, y, y) = 0; particles 3 in 3D: the full antisymmetrisation,
+ * zero wherever two coordinates coincide.  Other combinations leave psi unchanged. */
+int qsf_antisymmetrize(qsf_grid* g, int particles);
+
 /* ------------------------------------------------------ wavefunction files */
 /* .psi files with the layout of the reference's LocalGrid (grid.h:1025-1035):
  * dim u8 | rep u8 | complex u8 | downscale i64 | n[dim] i64 | dx[dim] f64 |

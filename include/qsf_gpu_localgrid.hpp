@@ -238,12 +238,29 @@ struct LocalGrid<Hamiltonian, GPU::CAP<D>, Components, MPI_GC, MPI::Slices, fals
     return out;
   }
 
-  // operation<M, R, Op>() (grid.h:599-606): Normalize
+  // operation<M, R, Op>() (grid.h:599-723): Normalize, AntiSymmetrize<2|3>
   template <MODE M, REP R, class Op> void operation() {
     if constexpr (std::is_same_v<Op, Normalize>) {
       push();
       GPU::check(qsf_normalize(grid(), nullptr), "qsf_normalize");
     }
+    if constexpr (std::is_same_v<Op, AntiSymmetrize<2>>) {
+      push();
+      GPU::check(qsf_antisymmetrize(grid(), 2), "qsf_antisymmetrize");
+    }
+    if constexpr (std::is_same_v<Op, AntiSymmetrize<3>>) {
+      push();
+      GPU::check(qsf_antisymmetrize(grid(), 3), "qsf_antisymmetrize");
+    }
+  }
+
+  // average_der<R, dir, Op>() (grid.h:443-465) for the potential
+  template <REP R, uind dir, class Op> double average_der() {
+    static_assert(std::is_same_v<Op, PotentialEnergy>, "derivative observables are built for the potential");
+    push();
+    double out = 0.0;
+    GPU::check(qsf_average_der(grid(), (int)dir, &out), "qsf_average_der");
+    return out;
   }
 
   void maskRegion() {

@@ -72,6 +72,10 @@ def lib():
         L.orc_fourier.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
         L.orc_average.argtypes = [ctypes.c_void_p, dp, ctypes.c_int, ctypes.c_int]
         L.orc_average.restype = ctypes.c_double
+        L.orc_average_der.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
+        L.orc_average_der.restype = ctypes.c_double
+        L.orc_antisymmetrize.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
+        L.orc_antisymmetrize.restype = None
         L.orc_normalize.argtypes = [ctypes.c_void_p, dp]
         L.orc_normalize.restype = ctypes.c_double
         L.orc_current_map.argtypes = [ctypes.c_void_p, dp, dp, dp]
@@ -243,6 +247,14 @@ class Grid:
     def mask_region(self, bounded):
         b = (ctypes.c_int * 3)(*(list(bounded) + [1] * (3 - len(bounded))))
         lib().orc_mask_region(self._buf, self._p(), b)
+
+    def average_der(self, direction: int) -> float:
+        """average_der<X, direction, PotentialEnergy> (grid.h:443-465)."""
+        return lib().orc_average_der(self._buf, self._p(), int(direction))
+
+    def antisymmetrize(self, particles: int):
+        """operation<M, R, AntiSymmetrize<particles>> (grid.h:611-723)."""
+        lib().orc_antisymmetrize(self._buf, self._p(), int(particles))
 
 
 def border_vector(border: str, dim: int, ci, box_size: int = 0) -> List[float]:

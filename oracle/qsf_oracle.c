@@ -393,6 +393,87 @@ double orc_average(const orc_grid* g, const double* psi_d, int rep, int op) {
   return res * (rep == ORC_REP_X ? g->dV : g->dVm);
 }
 
+/* average_der_<X, dir, Op> (grid.h:443-465) with Op = PotentialEnergy (hamiltonian.h:81-90):
+ * sum_i |psi_i|^2 (V(x_i + dx e_dir) - V(x_i - dx e_dir)) dV / (2 dx_dir), positions one
+ * node past either edge taken from the same linear formula (coords.h:132-135) */
+double orc_average_der(const orc_grid* g, const double* psi_d, int dir) {
+  const orc_cx* psi = (const orc_cx*)psi_d;
+  long idx[3] = {0, 0, 0};
+  double cp[3], cm[3];
+  double res = 0.0;
+  for (long i = 0; i < g->m; ++i) {
+    long r = i;
+    for (int d = g->dim - 1; d >= 0; --d) { idx[d] = r % g->n[d]; r /= g->n[d]; }
+    for (int d = 0; d < g->dim; ++d) {
+      cp[d] = pos(g, ORC_REP_X, d, idx[d] + (d == dir ? 1 : 0));
+      cm[d] = pos(g, ORC_REP_X, d, idx[d] + (d == dir ? -1 : 0));
+    }
+    res += (psi[i].re * psi[i].re + psi[i].im * psi[i].im) * (potential(g, cp) - potential(g, cm));
+  }
+  return res * g->dV * g->inv_2dx[dir];
+}
+
+/* operation<M, R, AntiSymmetrize<particles>> on one rank (grid.h:611-723).
+ * particles 2, dim 2: psi(i,j) -= psi_copy(j,i).
+ * particles 2, dim 3 (partial, axes 1 and 2): for k < j: psi(i,j,k) -= psi(i,k,j),
+ *   psi(i,k,j) = -psi(i,j,k); psi(i,j,j) = 0.
+ * particles 3, dim 3: for i > j > k the even permutations get
+ *   psi(i,j,k) + psi(j,k,i) + psi(k,i,j) - psi(j,i,k) - psi(i,k,j) - psi(k,j,i), the odd
+ *   ones its negative; every point with two equal indices becomes 0.
+ * Other (particles, dim) combinations leave psi unchanged, as the reference does. */
+void orc_antisymmetrize(const orc_grid* g, double* psi_d, int particles) {
+  orc_cx* psi = (orc_cx*)psi_d;
+  const long n = g->n[0];
+  if (particles == 2 && g->dim == 2) {
+    orc_cx* copy = (orc_cx*)malloc(sizeof(orc_cx) * (size_t)g->m);
+    memcpy(copy, psi, sizeof(orc_cx) * (size_t)g->m);
+    for (long i = 0; i < n; ++i)
+      for (long j = 0; j < n; ++j) {
+        psi[i * n + j].re -= copy[j * n + i].re;
+        psi[i * n + j].im -= copy[j * n + i].im;
+      }
+    free(copy);
+  } else if (particles == 2 && g->dim == 3) {
+    for (long i = 0; i < n; ++i)
+      for (long j = 0; j < n; ++j) {
+        for (long k = 0; k < j; ++k) {
+          orc_cx* a = &psi[(i * n + j) * n + k];
+          orc_cx* b = &psi[(i * n + k) * n + j];
+          a->re -= b->re;
+          a->im -= b->im;
+          b->re = -a->re;
+          b->im = -a->im;
+        }
+        psi[(i * n + j) * n + j].re = 0.0;
+        psi[(i * n + j) * n + j].im = 0.0;
+      }
+  } else if (particles == 3 && g->dim == 3) {
+#define AT(a, b, c) psi[((a) * n + (b)) * n + (c)]
+    for (long i = 0; i < n; ++i) {
+      for (long j = 0; j < i; ++j)
+        for (long k = 0; k < j; ++k) {
+          orc_cx s;
+          s.re = AT(j, k, i).re + AT(k, i, j).re - AT(j, i, k).re - AT(i, k, j).re - AT(k, j, i).re;
+          s.im = AT(j, k, i).im + AT(k, i, j).im - AT(j, i, k).im - AT(i, k, j).im - AT(k, j, i).im;
+          AT(i, j, k).re += s.re;
+          AT(i, j, k).im += s.im;
+          const orc_cx v = AT(i, j, k);
+          AT(j, k, i) = v;
+          AT(k, i, j) = v;
+          AT(j, i, k).re = -v.re; AT(j, i, k).im = -v.im;
+          AT(i, k, j).re = -v.re; AT(i, k, j).im = -v.im;
+          AT(k, j, i).re = -v.re; AT(k, j, i).im = -v.im;
+        }
+      for (long j = 0; j < n; ++j) {
+        AT(i, j, j).re = AT(i, j, j).im = 0.0;
+        AT(j, i, j).re = AT(j, i, j).im = 0.0;
+        AT(j, j, i).re = AT(j, j, i).im = 0.0;
+      }
+    }
+#undef AT
+  }
+}
+
 /* grid.h:601-606 (operation<Normalize>); returns the norm it divided by */
 double orc_normalize(const orc_grid* g, double* psi_d) {
   double res = orc_average(g, psi_d, ORC_REP_X, ORC_OP_IDENTITY);

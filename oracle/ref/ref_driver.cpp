@@ -9,7 +9,8 @@
 // Usage: qsf_ref <case> <outdir> key=value ...
 //   cases: prim2d, prim3d, c1 (1D IM + RE), c2 (2D IM + RE VG), c3 (3D RE LG),
 //          io1 / io2 / io3 (.psi save / load / backup / orthogonalizeWith / snapshot),
-//          mp (1D real time with MultiProductSplit of order 2 and 3, VG and LG)
+//          mp (1D real time with MultiProductSplit of order 2 and 3, VG and LG),
+//          as2 / as3 (average_der of the potential, AntiSymmetrize<2> and <3>)
 #include "QSF.h"
 
 #include <map>
@@ -307,6 +308,44 @@ static void mp(const std::string& out) {
   mp_run<3>(out, "MP3LG", DipoleCoupling<LengthGauge, F>(F(Sin2(field_cfg()))));
 }
 
+
+// ---------------------------------------------------------------- other members
+// average_der<X, d, PotentialEnergy> (grid.h:443-465) on a seeded state, then
+// operation<IM, X, AntiSymmetrize<2>> and, in 3D, AntiSymmetrize<3> (grid.h:611-723)
+template <DIMS D> static void as_case(const std::string& out) {
+  using Ham = Schrodinger::Spin0<CapGrid<D>, Eberly>;
+  Ham wf(make_grid<D>(), make_pot());
+  const ind m = wf.m_l;
+  g_state = (uint64_t)par("seed", 5);
+  std::vector<cxd> psi0((size_t)m);
+  for (ind i = 0; i < m; i++) psi0[(size_t)i] = cxd(urand(), urand());
+  auto set = [&]() {
+    for (ind i = 0; i < m; i++) wf[i] = psi0[(size_t)i];
+  };
+  set();
+  dump(out + "/psi_in.bin", psi0.data(), m);
+  FILE* fo = fopen((out + "/der.bin").c_str(), "wb");
+  double v;
+  v = wf.template average_der<REP::X, 0, PotentialEnergy>();
+  fwrite(&v, sizeof v, 1, fo);
+  if constexpr (D >= 2) {
+    v = wf.template average_der<REP::X, 1, PotentialEnergy>();
+    fwrite(&v, sizeof v, 1, fo);
+  }
+  if constexpr (D >= 3) {
+    v = wf.template average_der<REP::X, 2, PotentialEnergy>();
+    fwrite(&v, sizeof v, 1, fo);
+  }
+  fclose(fo);
+  wf.template operation<MODE::IM, REP::X, AntiSymmetrize<2>>();
+  dump(out + "/psi_as2.bin", &wf[0], m);
+  if constexpr (D == 3) {
+    set();
+    wf.template operation<MODE::IM, REP::X, AntiSymmetrize<3>>();
+    dump(out + "/psi_as3.bin", &wf[0], m);
+  }
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) {
     fprintf(stderr, "usage: %s <case> <outdir> key=value...\n", argv[0]);
@@ -333,6 +372,8 @@ int main(int argc, char** argv) {
   } else if (cs == "c2") c2(out);
   else if (cs == "c3") c3(out);
   else if (cs == "mp") mp(out);
+  else if (cs == "as2") as_case<2>(out);
+  else if (cs == "as3") as_case<3>(out);
   else if (cs == "io1") io<1>(out);
   else if (cs == "io2") io<2>(out);
   else if (cs == "io3") io<3>(out);

@@ -172,6 +172,8 @@ def lib():
         "qsf_backup": [vp, i64, ctypes.c_char_p],
         "qsf_restore": [vp, ctypes.c_char_p, ctypes.POINTER(i64)],
         "qsf_remove_backups": [ctypes.c_char_p],
+        "qsf_average_der": [vp, ctypes.c_int, dp],
+        "qsf_antisymmetrize": [vp, ctypes.c_int],
     }
     for name, args in sig.items():
         f = getattr(L, name)

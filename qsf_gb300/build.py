@@ -54,7 +54,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             print(r.stderr, file=sys.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, sources))
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
         cmd = [nvcc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]

@@ -41,7 +41,7 @@ bool plan_radices(int64_t n, std::vector<int>& r) {
 std::vector<KernelSet>& kernel_table();
 
 // kernel launch geometry
-constexpr int kMaxLine1D = 8192;        // 1D line held in shared memory (complex128)
+constexpr int kMaxLine1D = 16384;       // 1D line in shared memory (one CTA up to 8192, a cluster pair above)
 constexpr int kMaxTile = 4096;          // points per block in row / axis passes
 
 }  // namespace
@@ -52,6 +52,7 @@ void add_sizes_p2a(std::vector<KernelSet>& out);
 void add_sizes_p2b(std::vector<KernelSet>& out);
 void add_sizes_r3(std::vector<KernelSet>& out);
 void add_sizes_r5(std::vector<KernelSet>& out);
+void add_sizes_long(std::vector<KernelSet>& out);
 const KernelSet* kernels_for(int n) {
   for (const KernelSet& k : kernel_table())
     if (k.n == n) return &k;
@@ -79,6 +80,7 @@ int init_kernel_table() {
   add_sizes_p2b(t);
   add_sizes_r3(t);
   add_sizes_r5(t);
+  add_sizes_long(t);
   auto lim = [](const void* f, int bytes) -> int {
     if (!f) return QSF_OK;
     QSF_CU(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -95,7 +97,7 @@ int init_kernel_table() {
         (rc = lim((const void*)k.axis_fpi, tile)) || (rc = lim((const void*)k.axis_ekin, tile)) ||
         (rc = lim((const void*)k.axis_fft_f, tile)) || (rc = lim((const void*)k.axis_fft_b, tile)) ||
         (rc = lim((const void*)k.row_fft_f, line)) || (rc = lim((const void*)k.row_fft_b, line)) ||
-        (rc = lim((const void*)k.line_step, k.n * (int)sizeof(double2))))
+        (rc = lim((const void*)k.line_step, k.n / k.line_ctas * (int)sizeof(double2))))
       return rc;
   }
   done = true;
@@ -368,10 +370,11 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
   const int D = q.dim;
   // (kind, axis) tables (X tables only in the length gauge), ~128 entries per block
   const int tb = std::max(1, std::min(64, q.nmax / 128));
-  const dim3 gt(D * 3 * tb, count);
+  const dim3 gt(D * 4 * tb, count);
   QSF_TIMED(QSF_K_TABLES, (k_tables<<<gt, 256, 0, st>>>(dG, dS, tb)));
   if (D == 1) {
-    QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(1, count), kLineThreads, (size_t)q.n * sizeof(double2), st>>>(dG, dS)));
+    QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(K.line_ctas, count), kLineThreads,
+                                               (size_t)(q.n / K.line_ctas) * sizeof(double2), st>>>(dG, dS)));
   } else {
     const dim3 gr(q.nrowblk, count);
     QSF_TIMED(QSF_K_ROW_OPEN, (K.row_open<<<gr, kRowThreads, q.row_smem, st>>>(dG, dS, q.row_L)));
@@ -449,7 +452,7 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   S.m_mant = g->m_mant;
   S.texp = g->ibuf;
   S.gmin = g->ibuf + kTexp;
-  S.sc = g->ibuf + kTexp + 4;
+  S.sc = g->ibuf + kTexp + kGmin;
   S.scmax = g->scmax;
   S.nmax = g->nmax;
   S.partials = g->partials;
@@ -458,6 +461,8 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   for (int ax = 0; ax < 3; ++ax) S.naxblk[ax] = g->ax_blocks[ax];
   S.obs = d->obs | QSF_OBS_NORM;
   if (nb == 0) S.obs &= ~QSF_OBS_FLUX;
+  // steps of a call stay in fixed point between steps unless E_kin needs psi_n in memory
+  S.fused = (G.dim >= 2 && !(S.obs & QSF_OBS_EKIN)) ? 1 : 0;
   S.normalize = d->normalize;
   S.energy_after_normalize = d->energy_after_normalize;
   S.state_accuracy = d->mode == QSF_MODE_IM ? d->state_accuracy : 0.0;
@@ -758,7 +763,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
       g->ax_smem[ax] = (size_t)a.n * C * sizeof(double2);
     }
   } else {
-    g->nrowblk = 1;
+    g->nrowblk = ks->line_ctas;  // partial sums per CTA of the line
   }
   g->nmax = 0;
   for (int k = 0; k < D; ++k) g->nmax = std::max(g->nmax, G.ax[k].n);
@@ -768,8 +773,8 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   g->l2m = 0;
   while ((1LL << (g->l2m + 1)) <= G.m) ++g->l2m;
   g->m_mant = std::ldexp(1.0, g->l2m) / (double)G.m;
-  if ((rc = dev_alloc(g->ibuf, (size_t)kTexp + 4 + 4 * (size_t)g->scmax)) ||
-      (rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)2 * D * g->nmax)) ||
+  if ((rc = dev_alloc(g->ibuf, (size_t)kTexp + kGmin + 4 * (size_t)g->scmax)) ||
+      (rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)3 * D * g->nmax)) ||
       (rc = dev_alloc(g->partials, (size_t)5 * g->pmax)) || (rc = dev_alloc(g->ctl, 8)) ||
       (rc = dev_alloc(g->energy, 2)) || (rc = dev_alloc(g->scale, 2)) ||
       (rc = dev_alloc(g->fpartials, (size_t)64 * kMaxFluxBorders)) || (rc = dev_alloc(g->dG, 1)) ||
@@ -870,8 +875,12 @@ int qsf_fourier(qsf_grid* g, int to_rep) {
       const int n = G.ax[ax].n;
       const long long nrows = G.m / n;
       const int L = (int)std::max<long long>(1, std::min<long long>(nrows, (16LL * kLineThreads) / n));
-      const int blocks = (int)((nrows + L - 1) / L);
-      const size_t smem = (size_t)L * n * sizeof(double2);
+      int blocks = (int)((nrows + L - 1) / L);
+      size_t smem = (size_t)L * n * sizeof(double2);
+      if (K.line_ctas > 1) {  // one 1D line held by a cluster pair
+        blocks = K.line_ctas;
+        smem = (size_t)(n / K.line_ctas) * sizeof(double2);
+      }
       if (fwd) K.row_fft_f<<<blocks, kLineThreads, smem, st>>>(G, L, sc);
       else K.row_fft_b<<<blocks, kLineThreads, smem, st>>>(G, L, sc);
     } else {

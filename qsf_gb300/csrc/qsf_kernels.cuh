@@ -94,9 +94,13 @@ struct StepDev {
   int l2m;                 // 1/m = m_mant * 2^-l2m, m_mant in (0.5, 1] (folded into axis 0's P table)
   double m_mant;
   int* texp;               // [3][3] exponents taken out of the per-step tables (set by k_tables)
-  int* gmin;               // [4] minimum block exponent of each fixed-point pass of the step
+  int* gmin;               // [kGmin] minimum block exponent of each fixed-point pass (gmin_slot)
   int* sc;                 // [4][scmax] block exponents of each fixed-point pass
   int scmax;
+  // fused: a sub-step's closing row pass also applies the next sub-step's opening X half
+  // and forward transform (ψ stays in fixed point between the steps of a call); the
+  // pending Normalize factor then folds into the next sub-step's axis-0 P table
+  int fused;
   int nmax;
   // reductions
   double* partials;  // [5][pmax]: norm, epot, ekin axis 0..2
@@ -243,8 +247,14 @@ __device__ __forceinline__ int producer_block(int pass, int dim, long long p) {
 // magnitude <= 1 in 2^62 fixed point; a table whose exact values exceed 1 (imaginary
 // time) is stored times 2^-e and e is added back to the block exponent.
 //   texp[0][d]: P table of axis d, texp[1][d] / texp[2][d]: length-gauge X tables of
-//   axis d (open / close half).  The static X table's exponent is StepDev::xs_exp.
-constexpr int kTexp = 9;
+//   axis d (open / close half), texp[3][d]: opening half of the next sub-step (fused).
+//   The static X table's exponent is StepDev::xs_exp.
+constexpr int kTexp = 12;
+// Pass minima: [1..3] passes 1-3 of the sub-step; pass 0 alternates between [0] and
+// [4] with the parity of the sub-step, because in fused mode the closing pass of
+// sub-step k produces pass 0 of sub-step k + 1 while pass 0 of k may still be read.
+constexpr int kGmin = 5;
+__device__ __forceinline__ int gmin_slot(int pass, long long sub) { return pass ? pass : ((sub & 1) ? 4 : 0); }
 
 // sum |x|^2 and sum V |x|^2 of fixed-point values, exact in 128-bit integers
 struct Acc128 {
@@ -359,9 +369,10 @@ __global__ void k_build_static(GridDev g, int mode, double delta, int xs_exp, lo
 
 // value of one per-step table entry: kind 0 P phase (hamiltonian.h:52-58: kinetic and,
 // in the velocity gauge, A.k), kind 1 / 2 length-gauge x.E factor of the open / close
-// X half (hamiltonian.h:60-66 via DipoleCoupling)
-__device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& S, const double* cp, int kind, int d,
-                                               int i) {
+// X half (hamiltonian.h:60-66 via DipoleCoupling), kind 3 the open half of the next
+// sub-step (coupling row `cn`)
+__device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& S, const double* cp, const double* cn,
+                                               int kind, int d, int i) {
   const AxisDev& a = g.ax[d];
   if (kind == 0) {
     double A = 0.0;
@@ -373,16 +384,18 @@ __device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& 
     const double k = kpos(a, i);
     return expop(S.mode, S.dt * (0.5 * k * k + k * A));
   }
-  const double E = (cp && g.n_fields) ? cp[(kind - 1) * 3 + d] : 0.0;
+  const double* row = kind == 3 ? cn : cp;
+  const double E = (row && g.n_fields) ? row[(kind == 2 ? 3 : 0) + d] : 0.0;
   return expop(S.mode, (S.dt * 0.5) * (xpos(a, i) * E));
 }
 
 // Per-step tables: `tb` blocks per (kind, axis) table, each storing a contiguous slice.
-// A table whose exact values exceed 1 (imaginary time) is stored times 2^-e, e from
-// its maximum (every block of the table evaluates that maximum, so the slices agree),
-// and e is recorded in texp.  Axis 0's P table also carries the mantissa of 1/m (its
-// power of two goes into the exponent).  Block 0 resets the per-pass minimum
-// exponents of the step.
+// A table whose values exceed 1 in magnitude (imaginary time, or a Normalize factor
+// folded in) is stored times 2^-e, e from its maximum (every block of the table
+// evaluates that maximum, so the slices agree), and e is recorded in texp.  Axis 0's P
+// table carries the mantissa of 1/m (its power of two goes into the exponent) and, in
+// fused mode, the pending Normalize factor.  Block 0 resets the pass minima this
+// sub-step's passes will produce.
 __global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
                                                 int tb) {
   const GridDev& g = Gs[blockIdx.y];
@@ -393,38 +406,45 @@ __global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, 
   const int D = g.dim;
   const int table = blockIdx.x / tb, part = blockIdx.x % tb;
   const int kind = table / D, d = table % D;
+  const long long sub = S.ctl[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S.gmin[1] = S.gmin[2] = S.gmin[3] = 0x7fffffff;
+    S.gmin[gmin_slot(0, sub + 1)] = 0x7fffffff;               // produced by this sub-step's closing pass
+    if (!S.fused || sub == 0) S.gmin[gmin_slot(0, sub)] = 0x7fffffff;  // produced by this sub-step's opening pass
+  }
   if (kind > 0 && g.gauge != 1) return;
-  if (blockIdx.x == 0 && threadIdx.x < 4) S.gmin[threadIdx.x] = 0x7fffffff;
-  const long long step = S.ctl[0];
-  const double* cp = S.coupling ? S.coupling + step * S.coup_stride : nullptr;
+  if (kind == 3 && (!S.fused || sub + 1 >= S.nsteps)) return;
+  const double* cp = S.coupling ? S.coupling + sub * S.coup_stride : nullptr;
+  const double* cn = (S.coupling && sub + 1 < S.nsteps) ? S.coupling + (sub + 1) * S.coup_stride : nullptr;
   const int n = g.ax[d].n;
-  const double mant = (kind == 0 && d == 0) ? S.m_mant : 1.0;
-  if (S.mode == 1) {  // imaginary time: real factors that may exceed 1
-    double mx = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, table_entry(g, S, cp, kind, d, i).x * mant);
+  double mant = 1.0;
+  if (kind == 0 && d == 0) {
+    mant = S.m_mant;
+    if (S.fused && S.normalize) mant *= *S.scale;
+  }
+  double mx = mant;  // real time: phases of modulus 1 times the mantissa
+  if (S.mode == 1) {  // imaginary time: real factors, maximum over the table
+    mx = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, table_entry(g, S, cp, cn, kind, d, i).x * mant);
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double m2 = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m2 = fmax(m2, red[w]);
-      int e = 0;
-      if (m2 > 1.0) frexp(m2, &e);  // m2 < 2^e
-      e_sh = e;
-      if (part == 0) S.texp[kind * 3 + d] = e;
-    }
-    __syncthreads();
-  } else {
-    if (part == 0 && threadIdx.x == 0) S.texp[kind * 3 + d] = 0;
-    if (threadIdx.x == 0) e_sh = 0;
-    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
   }
+  if (threadIdx.x == 0) {
+    int e = 0;
+    if (mx > 1.0) frexp(mx, &e);  // mx < 2^e
+    e_sh = e;
+    if (part == 0) S.texp[kind * 3 + d] = e;
+  }
+  __syncthreads();
   const double sc = ldexp(mant, -e_sh);
   longlong2* out = kind == 0 ? S.ptab + (size_t)d * S.nmax : S.xdyn + ((size_t)(kind - 1) * D + d) * S.nmax;
   const int chunk = (n + tb - 1) / tb;
   const int i1 = min(n, (part + 1) * chunk);
   for (int i = part * chunk + threadIdx.x; i < i1; i += blockDim.x) {
-    const double2 f = table_entry(g, S, cp, kind, d, i);
+    const double2 f = table_entry(g, S, cp, cn, kind, d, i);
     out[i] = to_fx62(make_double2(fmin(fmax(f.x * sc, -1.0), 1.0), fmin(fmax(f.y * sc, -1.0), 1.0)));
   }
 }
@@ -494,7 +514,7 @@ __device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, lo
   int scale = s_in;
   long long F = 0;
   int k = 0;
-  const bool use_s = S.normalize && *S.scale != 1.0;
+  const bool use_s = !S.fused && S.normalize && *S.scale != 1.0;
   if (use_s) {
     split_scale(*S.scale, F, k);
     scale -= k;
@@ -515,13 +535,13 @@ __device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, lo
 }
 
 // psi_n from the block after the last inverse transform (held conjugated in smx when
-// conj_in): closing X factor, 1/m's power of two, store as double, norm / E_pot
+// conj_in): closing X factor, 1/m's power of two, [store as double], norm / E_pot
 // partial sums (exact integers).  On return smx holds psi_n in fixed point with
 // exponent `scale` and bit length `bits`.
 template <int N>
 __device__ __forceinline__ void close_block(const GridDev& g, const StepDev& S, longlong2* smx, long long base, int cnt,
                                             long long row0, int* red, int& scale, int& bits, double* dacc,
-                                            bool conj_in) {
+                                            bool conj_in, bool store) {
   const bool real_f = S.mode == 1 && g.gauge != 1;
   const int pre = product_headroom(bits);
   u64 mag = 0;
@@ -544,7 +564,7 @@ __device__ __forceinline__ void close_block(const GridDev& g, const StepDev& S, 
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const long long p = base + e;
     const longlong2 x = smx[e];
-    g.psi[p] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
+    if (store) g.psi[p] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
     acc_point(an, av, x, q, S.Vx, p, epot);
   }
   dacc[0] = acc_value(an);
@@ -580,6 +600,8 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_open(co
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
+  const long long sub = S.ctl[0];
+  if (S.fused && sub > 0) return;  // the previous sub-step's closing pass produced pass 0
   extern __shared__ longlong2 smx[];
   __shared__ int red[32];
   const long long row0 = (long long)blockIdx.x * L;
@@ -597,7 +619,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_open(co
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
   if (threadIdx.x == 0) {
     S.sc[blockIdx.x] = scale;
-    atomicMin(&S.gmin[0], scale);
+    atomicMin(&S.gmin[gmin_slot(0, sub)], scale);
   }
 }
 
@@ -609,7 +631,7 @@ template <int N>
 __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, int in_pass, longlong2* smx,
                                             long long obase, long long inner, int rows, int Ch, int ldc, int* red,
                                             int& bits, bool conj) {
-  const int gm = S.gmin[in_pass];
+  const int gm = S.gmin[gmin_slot(in_pass, S.ctl[0])];
   const int* sc = S.sc + (size_t)in_pass * S.scmax;
   const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
   const int cnt = rows * Ch;
@@ -630,8 +652,11 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
 }
 
 // Close: (fixed point, produced by the last strided-axis pass) inverse FFT . X half
-// -> psi_n (double), norm / E_pot partials, flux snapshot, E_kin part of the last axis.
-// The inverse transform is the forward one on conjugated data.
+// -> psi_n: norm / E_pot partials, flux snapshot, E_kin part of the last axis.  The
+// inverse transform is the forward one on conjugated data.  psi_n is stored as double
+// at the last sub-step of the call (or always when not fused); otherwise the pass goes
+// on into the next sub-step: its opening X half and the forward transform of the last
+// axis, leaving pass 0 of that sub-step in fixed point.
 template <int N>
 __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(const GridDev* __restrict__ Gs,
                                                            const StepDev* __restrict__ Ss, int L) {
@@ -642,6 +667,8 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   __shared__ int red[32];
   __shared__ double dred[32 * 3];
   const AxisDev& a = g.ax[g.dim - 1];
+  const long long sub = S.ctl[0];
+  const bool last = !S.fused || sub >= S.ctl[1] || sub + 1 >= S.nsteps;
   const long long row0 = (long long)blockIdx.x * L;
   const int Lh = (int)min((long long)L, g.m / N - row0);
   const long long base = row0 * N;
@@ -649,24 +676,53 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   int bits = 0;
   // rows are contiguous: treat the block as one "column" of cnt elements
   int scale = load_aligned<N>(g, S, g.dim == 3 ? 3 : 2, smx, base, 1, cnt, 1, 1, red, bits, true);
-  const int sh = first_pass_shift<N>(bits);
+  int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
   fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
-  close_block<N>(g, S, smx, base, cnt, row0, red, scale, bits, dacc, true);
-  __syncthreads();
-  if (S.row_ptr) {
+  close_block<N>(g, S, smx, base, cnt, row0, red, scale, bits, dacc, true, last);
+  if (S.row_ptr) {  // flux snapshot of psi_n (this thread's own elements of smx are not needed)
     const int e0 = S.row_ptr[row0], e1 = S.row_ptr[row0 + Lh];
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = g.psi[S.snap_idx[e]];
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const longlong2 x = smx[S.snap_idx[e] - base];
+      S.snap[e] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
+    }
   }
   dacc[2] = (S.obs & 4u) ? ekin_rows<N>(a, smx, ls, cnt, scale, bits, red) : 0.0;
   const double e_n = dacc[3], e_v = dacc[4];
-  block_sum<3>(dacc, dred);
+  block_sum<3>(dacc, dred);  // its barriers also end the snapshot reads of smx
   if (threadIdx.x == 0) {
     S.partials[0 * S.pmax + blockIdx.x] = ldexp(dacc[0], (int)e_n);
     S.partials[1 * S.pmax + blockIdx.x] = ldexp(dacc[1], (int)e_v);
     S.partials[(2 + g.dim - 1) * S.pmax + blockIdx.x] = dacc[2];
+  }
+  if (last) return;
+  // next sub-step: opening X half (static factor and the length-gauge factors of the
+  // next coupling row) and the forward transform of the last axis
+  const bool real_f = S.mode == 1 && g.gauge != 1;
+  const int pre = product_headroom(bits);
+  u64 mag = 0;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const long long p = base + e;
+    longlong2 x = smx[e];
+    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+    x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 2), real_f);
+    smx[e] = x;
+    mag |= fmag(x);
+  }
+  scale += pre - xfactor_exp(g, S, 2);
+  bits = block_max_int(bitlen(mag), red);
+  sh = first_pass_shift<N>(bits);
+  scale += sh;
+  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  longlong2* out = reinterpret_cast<longlong2*>(g.psi);
+#pragma unroll 4
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
+  if (threadIdx.x == 0) {
+    S.sc[blockIdx.x] = scale;
+    atomicMin(&S.gmin[gmin_slot(0, sub + 1)], scale);
   }
 }
 
@@ -814,7 +870,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   scale += sh;
   fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
-  close_block<N>(g, S, smx, 0, N, 0, red, scale, bits, dacc, true);
+  close_block<N>(g, S, smx, 0, N, 0, red, scale, bits, dacc, true, true);
   __syncthreads();
   if (S.row_ptr) {
     const int e1 = S.row_ptr[1];
@@ -1210,17 +1266,32 @@ struct KernelSet {
   void (*row_fft_b)(GridDev, int, double);
   void (*axis_fft_f)(GridDev, int, int, double);
   void (*axis_fft_b)(GridDev, int, int, double);
+  int line_ctas;  // CTAs holding one 1D line (2: a cluster pair, lines above 8192 points)
 };
 
 // kernel table of the supported sizes (qsf_sizes_*.cu); nullptr when n is not built
 const KernelSet* kernels_for(int n);
 
-// sizes up to 4096 get the multi-dimensional passes; up to 8192 the 1D line kernel
+}  // namespace qsf
+#include "qsf_cluster.cuh"
+namespace qsf {
+
+// sizes up to 4096 get the multi-dimensional passes; up to 8192 the 1D line kernel of
+// one CTA, up to 16384 the one of a cluster pair
 template <int N>
 KernelSet make_kernel_set() {
   static_assert(is_smooth(N), "grid sizes must be 2^a 3^b 5^c");
+  static_assert(N <= 16384, "1D lines longer than 16384 points are not built");
   KernelSet k{};
   k.n = N;
+  k.line_ctas = 1;
+  if constexpr (N > 8192) {
+    k.line_ctas = 2;
+    k.line_step = k_line_step_cl<N>;
+    k.row_fft_f = k_row_fft_cl<N, true>;
+    k.row_fft_b = k_row_fft_cl<N, false>;
+    return k;
+  } else {
   if constexpr (N <= 4096) {
     k.row_open = k_row_open<N>;
     k.row_close = k_row_close<N>;
@@ -1235,6 +1306,7 @@ KernelSet make_kernel_set() {
   k.row_fft_f = k_row_fft<N, true>;
   k.row_fft_b = k_row_fft<N, false>;
   return k;
+  }
 }
 
 }  // namespace qsf

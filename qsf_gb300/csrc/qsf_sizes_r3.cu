@@ -1,7 +1,8 @@
-// Kernel instantiations for grid sizes 3 * 2^k (12 .. 6144).
+// Kernel instantiations for grid sizes 3 * 2^k, 12 .. 384 (the rest in qsf_sizes_r3b.cu).
 #include <vector>
 #include "qsf_kernels.cuh"
 namespace qsf {
+void add_sizes_r3b(std::vector<KernelSet>& out);
 void add_sizes_r3(std::vector<KernelSet>& out) {
   out.push_back(make_kernel_set<12>());
   out.push_back(make_kernel_set<24>());
@@ -9,9 +10,6 @@ void add_sizes_r3(std::vector<KernelSet>& out) {
   out.push_back(make_kernel_set<96>());
   out.push_back(make_kernel_set<192>());
   out.push_back(make_kernel_set<384>());
-  out.push_back(make_kernel_set<768>());
-  out.push_back(make_kernel_set<1536>());
-  out.push_back(make_kernel_set<3072>());
-  out.push_back(make_kernel_set<6144>());
+  add_sizes_r3b(out);
 }
 }  // namespace qsf

@@ -132,6 +132,16 @@ class Grid:
     def add_gaussian(self, at: float = 0.0, delta: float = 1.0) -> None:
         check(lib().qsf_add_gaussian(self._h, at, delta), "qsf_add_gaussian")
 
+    def average_der(self, direction: int) -> float:
+        """average_der<X, direction, PotentialEnergy> (grid.h:443-465)."""
+        out = ctypes.c_double(0.0)
+        check(lib().qsf_average_der(self._h, int(direction), ctypes.byref(out)), "qsf_average_der")
+        return float(out.value)
+
+    def antisymmetrize(self, particles: int) -> None:
+        """operation<M, R, AntiSymmetrize<particles>> (grid.h:611-723)."""
+        check(lib().qsf_antisymmetrize(self._h, int(particles)), "qsf_antisymmetrize")
+
     # ------------------------------------------------------------ .psi files
     # Paths are relative to the working directory, as in the reference.
     _snapshot_counts = {}

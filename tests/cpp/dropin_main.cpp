@@ -33,6 +33,10 @@ int main(int argc, char** argv) {
   im.wf.backup(0);
   im.wf.restore();
   im.wf.remove_backups();
+  // other members: the potential's derivative observable and the exchange antisymmetrisation
+  const double dVdx = im.wf.template average_der<REP::X, 0, PotentialEnergy>();
+  im.wf.template operation<MODE::IM, REP::X, AntiSymmetrize<2>>();
+  printf("<dV/dx0> of the ground state: %.3e\n", dVdx);
   _FieldConfig fc{.field = 0.1, .omega = 1.0, .ncycles = 1.0, .FWHM_percent = 0, .phase_in_pi_units = 0,
                   .delay_in_cycles = 0};
   using C = DipoleCoupling<VelocityGauge, F>;

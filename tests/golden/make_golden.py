@@ -43,6 +43,9 @@ CASES = {
     # MultiProductSplit<Split3Base, K> real-time runs, K = 2, 3, both gauges
     "mp": ("mp", dict(n=256, dx=0.2, nCAP=25, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, re_dt=0.05, F0=0.05,
                       omega=0.5, ncycles=1, phase=0.0), 0, 4, 1),
+    # average_der of the potential, AntiSymmetrize<2> (2D, 3D) and <3> (3D)
+    "as2": ("as2", dict(n=12, dx=0.5, nCAP=1, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, seed=5), 0, 0, 2),
+    "as3": ("as3", dict(n=8, dx=0.5, nCAP=1, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, seed=6), 0, 0, 3),
     "io1": ("io1", dict(n=16, dx=0.3, nCAP=2, seed=3), 0, 0, 1),
     "io2": ("io2", dict(n=8, dx=0.5, nCAP=1, seed=5), 0, 0, 2),
     "io3": ("io3", dict(n=8, dx=0.4, nCAP=1, seed=9), 0, 0, 3),
@@ -63,7 +66,13 @@ def make(name):
         args = [REF, case, tmp] + [f"{k}={v}" for k, v in params.items()]
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL)
         out = {"params": json.dumps(params), "case": case, "dim": dim}
-        if case == "mp":
+        if case in ("as2", "as3"):
+            out["psi_in"] = _read_psi(os.path.join(tmp, "psi_in.bin"), shape)
+            out["psi_as2"] = _read_psi(os.path.join(tmp, "psi_as2.bin"), shape)
+            if case == "as3":
+                out["psi_as3"] = _read_psi(os.path.join(tmp, "psi_as3.bin"), shape)
+            out["der"] = np.fromfile(os.path.join(tmp, "der.bin"), dtype=np.float64)
+        elif case == "mp":
             for tag in ("MP2VG", "MP3VG", "MP2LG", "MP3LG"):
                 out[tag + "_psi0"] = _read_psi(os.path.join(tmp, tag + "_psi0.bin"), shape)
                 out[tag + "_psi"] = _read_psi(os.path.join(tmp, tag + "_psi.bin"), shape)

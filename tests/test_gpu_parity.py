@@ -92,6 +92,40 @@ def test_fft_1d_matches_numpy(Q, n):
     assert C.rel_l2(g.download(), psi) < 1e-14 * max(1.0, np.log2(n))
 
 
+def _exact_dft(x):
+    """DFT in extended precision: angles reduced exactly (k j mod n), long-double
+    cos / sin and sums (numpy longdouble)."""
+    n = len(x)
+    k = np.arange(n)
+    pi = np.longdouble("3.141592653589793238462643383279502884")
+    ang = -2 * pi * k.astype(np.longdouble) / n
+    tw = np.cos(ang) + 1j * np.sin(ang)  # the n distinct twiddles
+    return tw[np.outer(k, k) % n] @ x.astype(np.clongdouble)
+
+
+@pytest.mark.parametrize("n", [48, 256, 1024, 2048])
+def test_fixed_point_fft_beats_fp64(Q, n):
+    """The block fixed-point transform is more accurate than an FP64 FFT: normwise error
+    against an extended-precision DFT, next to numpy's FP64 FFT on the same inputs."""
+    if np.finfo(np.longdouble).eps >= np.finfo(np.float64).eps:
+        pytest.skip("long double is not wider than double on this host")
+    rng = np.random.default_rng(n + 1)
+    worst_gpu = worst_fp64 = 0.0
+    for _ in range(2):
+        x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.exp(-0.5 * ((np.arange(n) - n / 2) / (n / 8)) ** 2)
+        ex = _exact_dft(x)
+        nrm = float(np.sqrt(np.sum(np.abs(ex) ** 2)))
+        g = Q.Grid(1, n, 0.1)
+        g.upload(x)
+        g.fourier(Q.REP_P)
+        y = g.download()
+        g.close()
+        worst_gpu = max(worst_gpu, float(np.sqrt(np.sum(np.abs(y.astype(np.clongdouble) - ex) ** 2))) / nrm)
+        worst_fp64 = max(worst_fp64, float(np.sqrt(np.sum(np.abs(np.fft.fft(x).astype(np.clongdouble) - ex) ** 2))) / nrm)
+    assert worst_gpu < 1.5e-16
+    assert worst_gpu < 0.7 * worst_fp64
+
+
 @pytest.mark.parametrize("dim,n", [(2, 64), (2, 384), (2, 2048), (3, 16), (3, 48), (3, 256)])
 def test_fft_nd_matches_numpy(Q, dim, n):
     rng = np.random.default_rng(7 * n + dim)
