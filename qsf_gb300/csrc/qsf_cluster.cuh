@@ -111,7 +111,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
   cg::cluster_group cl = cg::this_cluster();
   if (!step_active(S)) return;  // uniform over the pair
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   __shared__ double dred[32 * 3];
   constexpr int H = N / 2;
   const int rank = (int)cl.block_rank();
@@ -229,7 +229,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
     k_row_fft_cl(GridDev g, int L, double post_scale) {
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   constexpr int H = N / 2;
   const int rank = (int)cl.block_rank();
   const long long base = (long long)rank * H;

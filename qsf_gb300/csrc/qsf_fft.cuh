@@ -186,14 +186,18 @@ __host__ __device__ constexpr bool is_smooth(int n) {
   while (v % 5 == 0) v /= 5;
   return v == 1 && n > 1;
 }
+// log2 of the largest power-of-two radix of the plans (16)
+#ifndef QSF_RADIX_LOG2
+#define QSF_RADIX_LOG2 4
+#endif
 __host__ __device__ constexpr int nstages(int n) {
   const int a = count_factor(n, 2);
-  return a / 4 + (a % 4 ? 1 : 0) + count_factor(n, 3) + count_factor(n, 5);
+  return a / QSF_RADIX_LOG2 + (a % QSF_RADIX_LOG2 ? 1 : 0) + count_factor(n, 3) + count_factor(n, 5);
 }
 __host__ __device__ constexpr int radix_at(int n, int i) {
   const int a = count_factor(n, 2);
-  const int q = a / 4, r = a % 4;
-  if (i < q) return 16;
+  const int q = a / QSF_RADIX_LOG2, r = a % QSF_RADIX_LOG2;
+  if (i < q) return 1 << QSF_RADIX_LOG2;
   int k = i - q;
   if (r) {
     if (k == 0) return 1 << r;

@@ -196,7 +196,23 @@ __device__ __forceinline__ i64 fshift(i64 x, int sh) {
 // guard bits a radix-R pass needs above the block maximum (growth <= R * sqrt(2))
 __host__ __device__ constexpr int fguard(int r) { return r == 16 ? 5 : r == 8 ? 4 : r == 5 ? 4 : r == 4 ? 3 : r == 3 ? 3 : 2; }
 
-// Block-wide max of per-thread values (smem needs 32 ints); result returned to all.
+// Block-wide max of per-thread values over one barrier: every warp's maximum goes to
+// slot[warp], then all threads read the slots.  The slots are reused only after at
+// least one further barrier (the FFT passes alternate between two slot arrays).
+__device__ __forceinline__ int block_max_once(int v, int* slot) {
+  v = __reduce_max_sync(0xffffffffu, (unsigned)v);
+  if ((threadIdx.x & 31) == 0) slot[threadIdx.x >> 5] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  int m = 0;
+  for (int w = 0; w < nw; ++w) m = max(m, slot[w]);
+  return m;
+}
+
+// Block-wide max of per-thread values (red[0..31]); result returned to all.  The
+// shared arrays named red in the kernels hold kRedInts ints: [0, 32) for this function,
+// [32, 96) for the alternating slots of the FFT passes.
+constexpr int kRedInts = 96;
 __device__ __forceinline__ int block_max_int(int v, int* red) {
   v = __reduce_max_sync(0xffffffffu, (unsigned)v);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
@@ -263,7 +279,7 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
       }
     }
   }
-  return block_max_int(bitlen(mag), red);  // includes the barrier that ends the pass
+  return block_max_once(bitlen(mag), red);  // its barrier ends the pass
 }
 
 // Full forward fixed-point transform of every line of the set, in place.  On entry
@@ -276,7 +292,7 @@ __device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const l
                                        int nth, int& scale, int& bits, int* red, int shift_in = 0) {
   if constexpr (S < nstages(N)) {
     constexpr int R = radix_at(N, S);
-    bits = fx_stockham<R, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red);
+    bits = fx_stockham<R, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red + 32 + 32 * (S & 1));
     if constexpr (S + 1 < nstages(N)) {
       // renormalise for the next pass: largest component below 2^(62 - guard(next))
       const int target = 62 - fguard(radix_at(N, S + 1));

@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_open(co
   const long long sub = S.ctl[0];
   if (S.fused && sub > 0) return;  // the previous sub-step's closing pass produced pass 0
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   const long long row0 = (long long)blockIdx.x * L;
   const int Lh = (int)min((long long)L, g.m / N - row0);
   const long long base = row0 * N;
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   __shared__ double dred[32 * 3];
   const AxisDev& a = g.ax[g.dim - 1];
   const long long sub = S.ctl[0];
@@ -766,7 +766,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis(const 
   if (!step_active(S)) return;
   if (MODE == 3 && !(S.obs & 4u)) return;
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   __shared__ double dred[32];
   __shared__ longlong2 pcol[64];
   const AxisDev& a = g.ax[ax];
@@ -856,7 +856,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   const StepDev& S = Ss[blockIdx.y];
   if (!step_active(S)) return;
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   __shared__ double dred[32 * 3];
   const AxisDev& a = g.ax[0];
   int bits = 0;
@@ -894,7 +894,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
 template <int N, bool FWD>
 __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_row_fft(GridDev g, int L, double post_scale) {
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   const AxisDev& a = g.ax[g.dim - 1];
   const long long row0 = (long long)blockIdx.x * L;
   const long long nrows = g.m / N;
@@ -930,7 +930,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
 template <int N, bool FWD>
 __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
   extern __shared__ longlong2 smx[];
-  __shared__ int red[32];
+  __shared__ int red[kRedInts];
   const AxisDev& a = g.ax[ax];
   const long long inner = a.stride;
   const long long tiles_per_outer = (inner + C - 1) / C;
