@@ -5,11 +5,11 @@
 // of lines) is held as 64-bit integers sharing one power-of-two block exponent,
 // value = int * 2^-scale.  Additions are exact; products by twiddles and butterfly
 // constants (62 fractional bits) keep the top 64 bits of the 124-bit product to within
-// 2.5 units, from three 32 x 32 -> 64-bit partial products.  After every radix pass the
+// 1.5 units, from three 32 x 32 -> 64-bit partial products.  After every radix pass the
 // block is renormalised so that its largest component again uses all bits the next
 // pass can afford (62 minus the pass's growth), i.e. block floating point with a 55-60
-// bit mantissa at every pass.  Against an exact DFT this is ~2.5x more accurate than an
-// FP64 FFT (normwise relative error ~9e-17 vs ~2.3e-16 at N = 48 .. 2048); FP64
+// bit mantissa at every pass.  Against an exact DFT this is ~3.5x more accurate than an
+// FP64 FFT (normwise relative error ~6e-17 vs ~2.3e-16 at N = 48 .. 2048); FP64
 // storage of psi is unchanged.
 //
 // Radix plans, pass structure and index maps are those of qsf_fft.cuh.
@@ -24,17 +24,16 @@ namespace qsf {
 typedef long long i64;
 typedef unsigned long long u64;
 
-// a * w / 2^62 for w in 2^62 fixed point, from three 32 x 32 -> 64-bit partial
-// products (IMAD.WIDE): the low x low product is dropped and the result centred, so it
-// lies within 2.5 units of the exact quotient.  Needs |a|, |w| < 2^62.5.
+// a * w / 2^62 for w in 2^62 fixed point, from three signed 32 x 32 -> 64-bit partial
+// products (IMAD.WIDE): both operands are split into a high word and a signed low
+// word, x = xh 2^32 + xl with xl in [-2^31, 2^31); the low x low product (at most one
+// unit of the result) is dropped and the middle terms are rounded, so the result lies
+// within 1.5 units of the exact quotient.  Needs |a|, |w| < 2^62.5.
 __device__ __forceinline__ i64 mulq62(i64 a, i64 w) {
-  const int ah = (int)(a >> 32), wh = (int)(w >> 32);
-  const unsigned al = (unsigned)a, wl = (unsigned)w;
-  const i64 hh = (i64)ah * (i64)wh;
-  // signed x unsigned: unsigned wide product, corrected for a negative signed factor
-  const i64 m1 = (i64)((u64)(unsigned)ah * (u64)wl) - (ah < 0 ? (i64)((u64)wl << 32) : 0);
-  const i64 m2 = (i64)((u64)(unsigned)wh * (u64)al) - (wh < 0 ? (i64)((u64)al << 32) : 0);
-  return (hh << 2) + (((m1 >> 1) + (m2 >> 1) + (3LL << 28)) >> 29);
+  const int al = (int)a, wl = (int)w;
+  const int ah = (int)((a - (i64)al) >> 32), wh = (int)((w - (i64)wl) >> 32);
+  const i64 mid = (i64)ah * wl + (i64)al * wh + (1LL << 29);
+  return (i64)(((u64)((i64)ah * wh) << 2) + (u64)(mid >> 30));
 }
 
 __device__ __forceinline__ longlong2 fadd(longlong2 a, longlong2 b) { return make_longlong2(a.x + b.x, a.y + b.y); }
@@ -52,6 +51,13 @@ __device__ __forceinline__ longlong2 fmul62(longlong2 a, longlong2 w) {
 // the block maximum's bit length, or one less when that maximum is a negative power of two
 __device__ __forceinline__ u64 fmag(longlong2 x) { return (u64)(x.x ^ (x.x >> 63)) | (u64)(x.y ^ (x.y >> 63)); }
 __device__ __forceinline__ int bitlen(u64 v) { return 64 - __clzll((long long)v); }
+// the same from the high words alone (32-bit operations): 32 + the high words' bit
+// length, or 0 when every component is below 2^32 in magnitude
+__device__ __forceinline__ unsigned fmag_hi(longlong2 x) {
+  const int hx = (int)(x.x >> 32), hy = (int)(x.y >> 32);
+  return (unsigned)(hx ^ (hx >> 31)) | (unsigned)(hy ^ (hy >> 31));
+}
+__device__ __forceinline__ int bitlen_hi(unsigned v) { return v ? 64 - __clz((int)v) : 0; }
 template <bool FWD> __device__ __forceinline__ longlong2 fmul_si(longlong2 a) {
   return FWD ? make_longlong2(a.y, -a.x) : make_longlong2(-a.y, a.x);
 }
@@ -230,10 +236,14 @@ __device__ __forceinline__ int block_max_int(int v, int* red) {
 // largest output component (see fmag).
 template <int R, int MAXB, int N, int NS>
 __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const LineSet& L,
-                                           const longlong2* __restrict__ tw, int tid, int nth, int shift_in, int* red) {
+                                           const longlong2* __restrict__ tw, int tid, int nth, int shift_in, int* red,
+                                           int parity) {
   constexpr int nr = N / R;
   constexpr int twstep = N / (NS * R);
   const int total = nr * L.nlines;
+  // the load-time scaling 2^shift_in without branches: (x << sl + half) >> sr
+  const int sl = shift_in > 0 ? shift_in : 0, sr = shift_in < 0 ? min(-shift_in, 63) : 0;
+  const i64 half = sr ? (i64)1 << (sr - 1) : 0;
   longlong2 v[MAXB][R];
   int dsto[MAXB];
 #pragma unroll
@@ -252,9 +262,8 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
       const longlong2* src = buf + line * L.ls;
 #pragma unroll
       for (int q = 0; q < R; ++q) {
-        longlong2 x = src[(j + q * nr) * L.es];
-        if (shift_in) x = make_longlong2(fshift(x.x, shift_in), fshift(x.y, shift_in));
-        v[b][q] = x;
+        const longlong2 x = src[(j + q * nr) * L.es];
+        v[b][q] = make_longlong2(((i64)((u64)x.x << sl) + half) >> sr, ((i64)((u64)x.y << sl) + half) >> sr);
       }
       const int jm = j % NS;
       if constexpr (NS > 1) {
@@ -265,7 +274,7 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
     }
   }
   __syncthreads();
-  u64 mag = 0;
+  unsigned mag = 0;
 #pragma unroll
   for (int b = 0; b < MAXB; ++b) {
     if (dsto[b] >= 0) {
@@ -275,11 +284,21 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         dst[q * st] = v[b][q];
-        mag |= fmag(v[b][q]);
+        mag |= fmag_hi(v[b][q]);
       }
     }
   }
-  return block_max_once(bitlen(mag), red);  // its barrier ends the pass
+  int bits = block_max_once(bitlen_hi(mag), red + 32 + 32 * parity);  // its barrier ends the pass
+  if (bits == 0) {  // every component below 2^32 (rare): bit length from the full words
+    u64 m64 = 0;
+#pragma unroll
+    for (int b = 0; b < MAXB; ++b)
+      if (dsto[b] >= 0)
+#pragma unroll
+        for (int q = 0; q < R; ++q) m64 |= fmag(v[b][q]);
+    bits = block_max_int(bitlen(m64), red);
+  }
+  return bits;
 }
 
 // Full forward fixed-point transform of every line of the set, in place.  On entry
@@ -292,7 +311,7 @@ __device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const l
                                        int nth, int& scale, int& bits, int* red, int shift_in = 0) {
   if constexpr (S < nstages(N)) {
     constexpr int R = radix_at(N, S);
-    bits = fx_stockham<R, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red + 32 + 32 * (S & 1));
+    bits = fx_stockham<R, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red, S & 1);
     if constexpr (S + 1 < nstages(N)) {
       // renormalise for the next pass: largest component below 2^(62 - guard(next))
       const int target = 62 - fguard(radix_at(N, S + 1));
