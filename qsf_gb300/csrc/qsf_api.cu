@@ -552,15 +552,16 @@ struct qsf_batch {
   cudaGraphExec_t exec = nullptr;
   long long* ctl_host = nullptr;  // pinned, 8 words per member
   size_t ctl_cap = 0;
+  // descriptor arrays of all groups (grow-only, so membership changes do not free device
+  // memory, which would synchronise the device)
+  GridDev* dG_all = nullptr;
+  StepDev* dS_all = nullptr;
+  size_t desc_cap = 0, dS_cap = 0;
 };
 
 namespace {
 
 void free_groups(qsf_batch* b) {
-  for (BatchGroup& gr : b->groups) {
-    if (gr.dG) cudaFree(gr.dG);
-    if (gr.dS) cudaFree(gr.dS);
-  }
   b->groups.clear();
   if (b->exec) cudaGraphExecDestroy(b->exec);
   b->exec = nullptr;
@@ -583,21 +584,27 @@ int rebuild_batch(qsf_batch* b) {
     gr.ekin = gr.ekin || (kv.second.S.obs & QSF_OBS_EKIN);
     if (kv.second.S.nfterms > 0) gr.nfblk = std::max(gr.nfblk, g->nfblk);
   }
+  const size_t total = b->members.size();
+  int rc;
+  if ((rc = dev_reserve(b->dG_all, b->desc_cap, total)) || (rc = dev_reserve(b->dS_all, b->dS_cap, total))) return rc;
+  std::vector<GridDev> hg;
+  std::vector<StepDev> hs;
+  hg.reserve(total);
+  hs.reserve(total);
   for (auto& kv : by) {
     BatchGroup gr = kv.second;
-    const size_t c = gr.slots.size();
-    std::vector<GridDev> hg(c);
-    std::vector<StepDev> hs(c);
-    for (size_t i = 0; i < c; ++i) {
-      const BatchMember& mb = b->members[gr.slots[i]];
-      hg[i] = mb.g->G;
-      hs[i] = mb.S;
+    gr.dG = b->dG_all + hg.size();
+    gr.dS = b->dS_all + hs.size();
+    for (int64_t slot : gr.slots) {
+      const BatchMember& mb = b->members[slot];
+      hg.push_back(mb.g->G);
+      hs.push_back(mb.S);
     }
-    int rc;
-    if ((rc = dev_alloc(gr.dG, c)) || (rc = dev_alloc(gr.dS, c))) return rc;
-    QSF_CU(cudaMemcpyAsync(gr.dG, hg.data(), c * sizeof(GridDev), cudaMemcpyHostToDevice, b->stream));
-    QSF_CU(cudaMemcpyAsync(gr.dS, hs.data(), c * sizeof(StepDev), cudaMemcpyHostToDevice, b->stream));
     b->groups.push_back(gr);
+  }
+  if (total) {
+    QSF_CU(cudaMemcpyAsync(b->dG_all, hg.data(), total * sizeof(GridDev), cudaMemcpyHostToDevice, b->stream));
+    QSF_CU(cudaMemcpyAsync(b->dS_all, hs.data(), total * sizeof(StepDev), cudaMemcpyHostToDevice, b->stream));
   }
   QSF_CU(cudaStreamSynchronize(b->stream));
   if (!b->groups.empty()) {
@@ -969,14 +976,14 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
   int ncol = 0, rc;
   if ((rc = prepare_step(g, d, &S, &ncol))) return rc;
   if (d->kernel_ms) {
+    // one event pair per launch of the whole call (at most 8 per step), read at the end,
+    // so the profiled call has no host synchronisation between its steps
     Prof P;
     P.ms = d->kernel_ms;
     P.count = d->kernel_launches;
-    rc = P.init(g->stream, 16);
-    for (int64_t k = 0; k < S.nsteps && rc == QSF_OK; ++k) {
-      rc = launch_step(g, S, &P);
-      if (rc == QSF_OK) rc = P.flush();
-    }
+    rc = P.init(g->stream, (int)std::min<int64_t>(S.nsteps * 8 + 8, 1 << 20));
+    for (int64_t k = 0; k < S.nsteps && rc == QSF_OK; ++k) rc = launch_step(g, S, &P);
+    if (rc == QSF_OK) rc = P.flush();
     P.release();
     if (rc) return rc;
   } else if (S.nsteps < 4) {
@@ -1018,6 +1025,8 @@ int qsf_batch_destroy(qsf_batch* b) {
   if (!b) return QSF_OK;
   cudaStreamSynchronize(b->stream);
   free_groups(b);
+  if (b->dG_all) cudaFree(b->dG_all);
+  if (b->dS_all) cudaFree(b->dS_all);
   if (b->ctl_host) cudaFreeHost(b->ctl_host);
   if (b->own_stream) cudaStreamDestroy(b->stream);
   delete b;

@@ -42,6 +42,7 @@ struct Running {
   int64_t m = 0;
   int nb = 0;
   double dt = 0.0;
+  qsf_grid_desc desc{};          // for returning the grid to the pool
   std::vector<double> coupling;  // kept alive while in the batch
   clk::time_point submitted, admitted;
 };
@@ -74,9 +75,72 @@ struct qsf_server {
   std::thread worker;
   qsf_batch* batch = nullptr;
   qsf_server_stats stats{};
+  // finished solves' grids kept for the next request with the same descriptor: their
+  // allocations, static X / potential tables and flux point lists are reused (worker
+  // thread only)
+  std::vector<std::pair<qsf_grid_desc, qsf_grid*>> pool;
 };
 
 namespace {
+
+bool same_grid(const qsf_grid_desc& a, const qsf_grid_desc& b) {
+  if (a.dim != b.dim || a.nCAP != b.nCAP || a.potential != b.potential || a.gauge != b.gauge ||
+      a.n_fields != b.n_fields || a.p_axis_swap != b.p_axis_swap || a.Ncharge != b.Ncharge ||
+      a.Echarge != b.Echarge || a.Nsoft != b.Nsoft || a.Esoft != b.Esoft)
+    return false;
+  for (int k = 0; k < a.dim; ++k)
+    if (a.n[k] != b.n[k] || a.dx[k] != b.dx[k]) return false;
+  for (int k = 0; k < 4; ++k)
+    if (a.border_nodes[k] != b.border_nodes[k]) return false;
+  return true;
+}
+
+size_t pooled_bytes(const qsf_server* s) {
+  size_t b = 0;
+  for (const auto& e : s->pool) {
+    int64_t m = 1;
+    for (int k = 0; k < e.first.dim; ++k) m *= e.first.n[k];
+    b += (size_t)m * (16 + 16 + 8);
+  }
+  return b;
+}
+
+void drain_pool(qsf_server* s) {
+  for (auto& e : s->pool) qsf_grid_destroy(e.second);
+  s->pool.clear();
+}
+
+// a grid for this descriptor: a pooled one (psi cleared) or a new one
+int take_grid(qsf_server* s, const qsf_grid_desc& d, qsf_grid** out) {
+  for (size_t i = 0; i < s->pool.size(); ++i) {
+    if (!same_grid(s->pool[i].first, d)) continue;
+    qsf_grid* g = s->pool[i].second;
+    s->pool.erase(s->pool.begin() + (long)i);
+    void* psi = nullptr;
+    int64_t m = 0;
+    int rc = qsf_psi_device_ptr(g, &psi);
+    if (!rc) rc = qsf_grid_size(g, &m);
+    if (!rc) rc = qsf_synchronize(g);
+    if (!rc && cudaMemset(psi, 0, (size_t)m * 16) != cudaSuccess) rc = QSF_ECUDA;
+    if (rc) {
+      qsf_grid_destroy(g);
+      return rc;
+    }
+    *out = g;
+    return QSF_OK;
+  }
+  int rc = qsf_grid_create(&d, nullptr, out);
+  if (rc == QSF_ENOMEM && !s->pool.empty()) {  // pooled grids hold the memory: free them and retry
+    drain_pool(s);
+    rc = qsf_grid_create(&d, nullptr, out);
+  }
+  return rc;
+}
+
+void release_grid(qsf_server* s, const qsf_grid_desc& d, qsf_grid* g) {
+  if ((int)s->pool.size() < s->cfg.max_slots) s->pool.emplace_back(d, g);
+  else qsf_grid_destroy(g);
+}
 
 void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t steps) {
   qsf_result res{};
@@ -108,7 +172,7 @@ void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t s
 // admit one request: grid, start state, batch membership
 int admit(qsf_server* s, Pending& p, Running& r) {
   qsf_grid* g = nullptr;
-  int rc = qsf_grid_create(&p.req.grid, nullptr, &g);
+  int rc = take_grid(s, p.req.grid, &g);
   if (rc) return rc;
   const int64_t m = grid_points(p.req.grid);
   if (!p.psi0.empty()) {
@@ -123,6 +187,7 @@ int admit(qsf_server* s, Pending& p, Running& r) {
   }
   r.ticket = p.ticket;
   r.grid = g;
+  r.desc = p.req.grid;
   r.nsteps = p.req.nsteps;
   r.remaining = p.req.nsteps;
   r.m = m;
@@ -163,7 +228,7 @@ void worker_loop(qsf_server* s) {
       size_t free_b = 0, total_b = 0;
       cudaMemGetInfo(&free_b, &total_b);
       const double reserve = s->cfg.hbm_reserve_gb * 1e9;
-      double budget = (double)free_b - reserve;
+      double budget = (double)free_b - reserve + (double)pooled_bytes(s);  // pooled grids can be freed
       while (!s->queue.empty() && (int)(s->running.size() + take.size()) < s->cfg.max_slots) {
         const double need = (double)solve_bytes(s->queue.front().req);
         if (need > budget) break;
@@ -203,7 +268,8 @@ void worker_loop(qsf_server* s) {
       int64_t steps = 0;
       int rc = rc_run ? rc_run : qsf_batch_result(s->batch, r.slot, rows.data(), &steps);
       qsf_batch_remove(s->batch, r.slot);
-      qsf_grid_destroy(r.grid);
+      if (rc) qsf_grid_destroy(r.grid);
+      else release_grid(s, r.desc, r.grid);
       finish(s, r, rc, rows.data(), steps);
       s->running.erase(t);
     }
@@ -295,6 +361,7 @@ int qsf_server_stop(qsf_server* s) {
     s->cv_done.notify_all();
   }
   if (s->worker.joinable()) s->worker.join();
+  drain_pool(s);
   qsf_batch_destroy(s->batch);
   delete s;
   return QSF_OK;
