@@ -77,6 +77,64 @@ def coupling_schedule(coupling: Coupling, dt: float, nsteps: int, timer: float =
     return rows, timer
 
 
+# BufferedOutputs column classes (computations.h:58-111): VALUE and CHANGE fill the
+# plain buffer, AVG, FLUX and SUM of AVGs the reduced one; OPERATION stores nothing.
+_PLAIN_OUTPUTS = ("time", "step", "ediff")
+_REDUCED_OUTPUTS = ("norm", "epot", "ekin", "etot")
+DAT_FORMAT = "|%13.5g "  # FMT_DOUBLE (constants.h:15); a row ends with FMT_END "\n"
+
+
+def dat_columns(outputs: list) -> List[tuple]:
+    """Column order of a .dat row (buffer.h:296-338): the plain-buffer entries in
+    declaration order, then the reduced-buffer entries in declaration order.  Each item
+    is (output name, index within a flux entry or None)."""
+    plain = [(o, None) for o in outputs if isinstance(o, str) and o in _PLAIN_OUTPUTS]
+    reduced = []
+    for o in outputs:
+        if _is_flux(o):
+            reduced += [("flux", i) for i in range(len(o[1]))]
+        elif isinstance(o, str) and o in _REDUCED_OUTPUTS:
+            reduced.append((o, None))
+    return plain + reduced
+
+
+def dat_values(rows: List[dict], outputs: list) -> np.ndarray:
+    """The rows as the (n_rows, n_columns) matrix a .dat file holds."""
+    cols = dat_columns(outputs)
+    out = np.empty((len(rows), len(cols)), dtype=np.float64)
+    for r, row in enumerate(rows):
+        for c, (name, i) in enumerate(cols):
+            v = row.get(name, 0.0)
+            out[r, c] = v[i] if i is not None else v
+    return out
+
+
+def write_dat(path: str, rows: List[dict], outputs: list, binary: bool = False) -> None:
+    """Write rows in the reference's .dat layout (BufferedOutputs::logOrPass,
+    buffer.h:296-338): text rows of FMT_DOUBLE fields, or raw doubles row after row."""
+    vals = dat_values(rows, outputs)
+    if binary:
+        with open(path, "wb") as f:
+            f.write(np.ascontiguousarray(vals, dtype="<f8").tobytes())
+        return
+    with open(path, "w") as f:
+        for row in vals:
+            f.write("".join(DAT_FORMAT % v for v in row) + "\n")
+
+
+def read_dat(path: str, outputs: list, binary: bool = False) -> np.ndarray:
+    """Inverse of write_dat (the reader side of flx.wl / wf.wl): (n_rows, n_columns)."""
+    ncol = len(dat_columns(outputs))
+    if binary:
+        return np.fromfile(path, dtype="<f8").reshape(-1, ncol)
+    rows = []
+    with open(path) as f:
+        for line in f:
+            fields = [t.strip() for t in line.rstrip("\n").split("|")[1:]]
+            rows.append([float(t) for t in fields])
+    return np.array(rows, dtype=np.float64).reshape(-1, ncol)
+
+
 class SplitPropagator:
     def __init__(self, mode: int, dt: float, max_steps: int, grid: Grid, coupling: Coupling, outputs: list,
                  state_accuracy: float = 0.0, order: int = 1):
@@ -205,6 +263,13 @@ class SplitPropagator:
             self.step += 1
             self.rows.append(self._finish_row(raw, self.step, times[s]))
         return done
+
+    def write_dat(self, name: str, binary: bool = False) -> str:
+        """<name>.dat with one row per computed step (comp_interval 1), as
+        BufferedOutputs writes it (buffer.h:89-91, 296-338); returns the path."""
+        path = name + ".dat"
+        write_dat(path, self.rows, self.outputs, binary)
+        return path
 
     def _times(self, t0: float, n: int) -> List[float]:
         """Timer after each of n steps: the last chain's increments (incrementBy,
