@@ -452,7 +452,9 @@ __global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, 
 #endif  // QSF_DEFINE_KERNELS
 
 // X factor (2^62 fixed point, |.| <= 1) at point p (row r of the last axis, position
-// j on it); half 0 opens the step, 1 closes it
+// j on it); half 0 opens the step, 1 closes it, 2 opens the next sub-step.  NA is the
+// length of the axes before the last one when known at compile time (0: read it).
+template <int NA = 0>
 __device__ __forceinline__ longlong2 xfactor(const GridDev& g, const StepDev& S, long long p, long long r, int j,
                                              int half) {
   longlong2 f = S.xs[p];
@@ -462,8 +464,9 @@ __device__ __forceinline__ longlong2 xfactor(const GridDev& g, const StepDev& S,
     longlong2 d = t[(D - 1) * S.nmax + j];
     long long rr = r;
     for (int dd = D - 2; dd >= 0; --dd) {
-      const int ii = (int)(rr % g.ax[dd].n);
-      rr /= g.ax[dd].n;
+      const long long n = NA ? NA : g.ax[dd].n;
+      const int ii = (int)(rr % n);
+      rr /= n;
       d = fmul62(d, t[dd * S.nmax + ii]);
     }
     f = fmul62(f, d);
@@ -526,7 +529,7 @@ __device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, lo
     const double2 v = sd[e];  // written by this thread
     longlong2 x = make_longlong2(d2fx(v.x, s_in), d2fx(v.y, s_in));
     if (use_s) x = make_longlong2(mulq62(x.x, F), mulq62(x.y, F));
-    x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 0), real_f);
+    x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 0), real_f);
     smx[e] = x;
     mag |= fmag(x);
   }
@@ -551,7 +554,7 @@ __device__ __forceinline__ void close_block(const GridDev& g, const StepDev& S, 
     longlong2 x = smx[e];
     if (conj_in) x = fconj(x);
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 1), real_f);
+    x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 1), real_f);
     smx[e] = x;
     mag |= fmag(x);
   }
@@ -626,11 +629,13 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_open(co
 // Loads the elements [obase + i * inner + c] (i < rows, c < Ch) of a fixed-point pass
 // output into smx[i * ldc + c] aligned to the pass minimum exponent (conjugated when
 // conj); returns the block's common exponent and the bit length of its largest
-// component.
+// component.  With dtab, the alignment shift of element (i, c) is dtab[key], key = i
+// (tab_by_row) or (obase + i * inner + c) % N; otherwise it is looked up per element.
 template <int N>
 __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, int in_pass, longlong2* smx,
                                             long long obase, long long inner, int rows, int Ch, int ldc, int* red,
-                                            int& bits, bool conj) {
+                                            int& bits, bool conj, const int* dtab = nullptr,
+                                            bool tab_by_row = false) {
   const int gm = S.gmin[gmin_slot(in_pass, S.ctl[0])];
   const int* sc = S.sc + (size_t)in_pass * S.scmax;
   const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
@@ -641,7 +646,7 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
     const int i = e / Ch, c = e % Ch;
     const long long p = obase + (long long)i * inner + c;
     longlong2 x = in[p];
-    const int d = gm - sc[producer_block<N>(in_pass, g.dim, p)];
+    const int d = dtab ? dtab[tab_by_row ? i : (int)(p % N)] : gm - sc[producer_block<N>(in_pass, g.dim, p)];
     if (d) x = make_longlong2(fshift(x.x, d), fshift(x.y, d));
     if (conj) x = fconj(x);
     smx[i * ldc + c] = x;
@@ -649,6 +654,17 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
   }
   bits = block_max_int(bitlen(mag), red);
   return gm;
+}
+
+// Alignment shifts of a consumer block whose producer depends on one index of N values:
+// dtab[k] = gmin - sc[producer(k)], producer(k) = base_block + (kbase + k) / div.
+template <int N>
+__device__ __forceinline__ void build_dtab(const StepDev& S, int in_pass, int* dtab, long long base_block,
+                                           long long kbase, int div) {
+  const int gm = S.gmin[gmin_slot(in_pass, S.ctl[0])];
+  const int* sc = S.sc + (size_t)in_pass * S.scmax;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) dtab[k] = gm - sc[base_block + (kbase + k) / div];
+  __syncthreads();
 }
 
 // Close: (fixed point, produced by the last strided-axis pass) inverse FFT . X half
@@ -674,8 +690,18 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   const long long base = row0 * N;
   const int cnt = Lh * N;
   int bits = 0;
+  // producer of element (row, j): axis-0 tile j / C (2D) or axis-1 tile (i0, j / C) (3D,
+  // when the block's rows share i0)
+  __shared__ int dtab[N];
+  const bool use_tab = g.dim == 2 || N % row_lines(N) == 0;
+  if (use_tab) {
+    constexpr int C = tile_cols(N) < N ? tile_cols(N) : N;
+    const long long i0 = g.dim == 3 ? row0 / N : 0;
+    build_dtab<N>(S, g.dim == 3 ? 3 : 2, dtab, g.dim == 3 ? i0 * ((N + C - 1) / C) : 0, 0, C);
+  }
   // rows are contiguous: treat the block as one "column" of cnt elements
-  int scale = load_aligned<N>(g, S, g.dim == 3 ? 3 : 2, smx, base, 1, cnt, 1, 1, red, bits, true);
+  int scale = load_aligned<N>(g, S, g.dim == 3 ? 3 : 2, smx, base, 1, cnt, 1, 1, red, bits, true,
+                              use_tab ? dtab : nullptr, false);
   int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
@@ -708,7 +734,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
     const long long p = base + e;
     longlong2 x = smx[e];
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    x = apply_f(x, xfactor(g, S, p, row0 + e / N, e % N, 2), real_f);
+    x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 2), real_f);
     smx[e] = x;
     mag |= fmag(x);
   }
@@ -811,7 +837,12 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis(const 
   }
   const int in_pass = MODE == 0 ? 0 : MODE == 1 ? 2 : (g.dim == 3 ? 1 : 0);
   const int out_pass = MODE == 0 ? 1 : MODE == 1 ? 3 : 2;
-  scale = load_aligned<N>(g, S, in_pass, smx, obase, inner, N, Ch, C, red, bits, MODE == 1);
+  // producer row block of element (i, c) when the input is the row pass: (o N + i) / L
+  __shared__ int dtab[N];
+  const bool by_row = in_pass == 0;
+  if (by_row) build_dtab<N>(S, 0, dtab, 0, o * N, row_lines(N));
+  scale = load_aligned<N>(g, S, in_pass, smx, obase, inner, N, Ch, C, red, bits, MODE == 1, by_row ? dtab : nullptr,
+                          true);
   const bool multi_col = MODE == 2 && ax + 1 < g.dim;
   if (multi_col && threadIdx.x < Ch) {
     // per-column factor: product of the P tables of the axes after `ax`
