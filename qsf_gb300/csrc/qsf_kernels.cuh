@@ -221,6 +221,39 @@ __device__ __forceinline__ double2 expop(int mode, double val) {
 // Rows per block of the last-axis passes and columns per tile of the strided-axis
 // passes are compile-time functions of the line length (<= kMaxTile points per block),
 // so a consumer pass finds the block that produced an element with a few integer ops.
+// 16-byte global -> shared copy that bypasses registers (cp.async, cache-global); the
+// copies of a thread are visible to that thread after cp_async_wait_all.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Hint: bring [p, p + bytes) into L2 (bulk prefetch of the 16-byte aligned interior).
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned long long bytes) {
+  const unsigned long long a = (unsigned long long)p, lo = (a + 15) & ~15ull, hi = (a + bytes) & ~15ull;
+  for (unsigned long long q = lo; q < hi; q += 1u << 20) {
+    const unsigned n = (unsigned)((hi - q) < (1ull << 20) ? (hi - q) : (1ull << 20));
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(q), "r"(n) : "memory");
+  }
+}
+
+// (i, c) = (e / Ch, e % Ch) for e = e0, e0 + step, e0 + 2 step, ... without a division
+// per element (Ch is a runtime tile width in the strided-axis passes)
+struct TileWalk {
+  int i, c, di, dc, Ch;
+  __device__ __forceinline__ TileWalk(int e0, int step, int ch)
+      : i(e0 / ch), c(e0 % ch), di(step / ch), dc(step % ch), Ch(ch) {}
+  __device__ __forceinline__ void next() {
+    i += di;
+    c += dc;
+    if (c >= Ch) {
+      c -= Ch;
+      ++i;
+    }
+  }
+};
+
 __host__ __device__ constexpr int row_lines(int n) { return n >= 4096 ? 1 : 4096 / n; }
 __host__ __device__ constexpr int tile_cols(int n) { return (4096 / n) < 64 ? (4096 / n) : 64; }
 
@@ -577,6 +610,59 @@ __device__ __forceinline__ void close_block(const GridDev& g, const StepDev& S, 
   dacc[4] = (double)(2 * q - 2 * scale + 50 - S.vshift);
 }
 
+// Fused close of one sub-step and open of the next (no E_kin, psi_n not stored): in one
+// sweep over the block (held conjugated in smx after the inverse transform), psi_n =
+// f1 x feeds the norm / E_pot sums and becomes f2 psi_n, the next sub-step's opening X
+// half, left in smx.  The bit length of psi_n is bounded by that of x plus one (|f1| <=
+// 1), which fixes its accumulation shift and product headroom before the sweep.  The
+// flux snapshot of psi_n is taken first, at its listed points only.
+template <int N>
+__device__ __forceinline__ void close_open_block(const GridDev& g, const StepDev& S, longlong2* smx, long long base,
+                                                 int cnt, long long row0, int Lh, int* red, int& scale, int& bits,
+                                                 double* dacc) {
+  const bool real_f = S.mode == 1 && g.gauge != 1;
+  const int pre = product_headroom(bits);
+  const int by = min(bits + pre + 1, 62);
+  const int sy = scale + pre - xfactor_exp(g, S, 1) + S.l2m;
+  const int q = by > 56 ? by - 56 : 0;
+  const int pre2 = product_headroom(by);
+  if (S.row_ptr) {
+    const int e0 = S.row_ptr[row0], e1 = S.row_ptr[row0 + Lh];
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const long long p = S.snap_idx[e];
+      const int k = (int)(p - base);
+      longlong2 x = fconj(smx[k]);
+      if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+      x = apply_f(x, xfactor<N>(g, S, p, row0 + k / N, k % N, 1), real_f);
+      S.snap[e] = make_double2(fx2d(x.x, sy), fx2d(x.y, sy));
+    }
+    __syncthreads();
+  }
+  Acc128 an{0ull, 0ll}, av{0ull, 0ll};
+  const bool epot = (S.obs & 2u) != 0;
+  u64 mag = 0;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const long long p = base + e;
+    longlong2 x = fconj(smx[e]);
+    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+    const longlong2 f1 = xfactor<N>(g, S, p, row0 + e / N, e % N, 1);
+    const longlong2 f2 = g.gauge == 1 ? xfactor<N>(g, S, p, row0 + e / N, e % N, 2) : f1;
+    x = apply_f(x, f1, real_f);
+    acc_point(an, av, x, q, S.Vx, p, epot);
+    if (pre2) x = make_longlong2(fshift(x.x, pre2), fshift(x.y, pre2));
+    x = apply_f(x, f2, real_f);
+    smx[e] = x;
+    mag |= fmag(x);
+  }
+  dacc[0] = acc_value(an);
+  dacc[1] = acc_value(av);
+  dacc[3] = (double)(2 * q - 2 * sy);
+  dacc[4] = (double)(2 * q - 2 * sy + 50 - S.vshift);
+  scale = sy + pre2 - xfactor_exp(g, S, 2);
+  bits = block_max_int(bitlen(mag), red);
+}
+
 // E_kin part of the last axis: forward transform of psi_n (in smx) and sum k^2 |.|^2
 template <int N>
 __device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, const LineSet& ls, int cnt, int scale,
@@ -641,11 +727,18 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
   const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
   const int cnt = rows * Ch;
   u64 mag = 0;
+  {  // all of this thread's copies in flight at once, then fixed up in place
+    TileWalk w(threadIdx.x, blockDim.x, Ch);
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x, w.next())
+      cp_async16(&smx[w.i * ldc + w.c], in + obase + (long long)w.i * inner + w.c);
+    cp_async_wait_all();
+  }
+  TileWalk w(threadIdx.x, blockDim.x, Ch);
 #pragma unroll 4
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int i = e / Ch, c = e % Ch;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x, w.next()) {
+    const int i = w.i, c = w.c;
     const long long p = obase + (long long)i * inner + c;
-    longlong2 x = in[p];
+    longlong2 x = smx[i * ldc + c];
     const int d = dtab ? dtab[tab_by_row ? i : (int)(p % N)] : gm - sc[producer_block<N>(in_pass, g.dim, p)];
     if (d) x = make_longlong2(fshift(x.x, d), fshift(x.y, d));
     if (conj) x = fconj(x);
@@ -690,6 +783,10 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   const long long base = row0 * N;
   const int cnt = Lh * N;
   int bits = 0;
+  if (threadIdx.x == 0) {  // the X table (and potential) rows of this block, needed after the transform
+    prefetch_l2(S.xs + base, (unsigned long long)cnt * sizeof(longlong2));
+    if (S.obs & 2u) prefetch_l2(S.Vx + base, (unsigned long long)cnt * sizeof(long long));
+  }
   // producer of element (row, j): axis-0 tile j / C (2D) or axis-1 tile (i0, j / C) (3D,
   // when the block's rows share i0)
   __shared__ int dtab[N];
@@ -707,15 +804,21 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   const LineSet ls{Lh, N, 1, false};
   fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
-  close_block<N>(g, S, smx, base, cnt, row0, red, scale, bits, dacc, true, last);
-  if (S.row_ptr) {  // flux snapshot of psi_n (this thread's own elements of smx are not needed)
-    const int e0 = S.row_ptr[row0], e1 = S.row_ptr[row0 + Lh];
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      const longlong2 x = smx[S.snap_idx[e] - base];
-      S.snap[e] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
+  const bool fuse_x = !last && !(S.obs & 4u);
+  if (fuse_x) {
+    close_open_block<N>(g, S, smx, base, cnt, row0, Lh, red, scale, bits, dacc);
+    dacc[2] = 0.0;
+  } else {
+    close_block<N>(g, S, smx, base, cnt, row0, red, scale, bits, dacc, true, last);
+    if (S.row_ptr) {  // flux snapshot of psi_n (this thread's own elements of smx are not needed)
+      const int e0 = S.row_ptr[row0], e1 = S.row_ptr[row0 + Lh];
+      for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const longlong2 x = smx[S.snap_idx[e] - base];
+        S.snap[e] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
+      }
     }
+    dacc[2] = (S.obs & 4u) ? ekin_rows<N>(a, smx, ls, cnt, scale, bits, red) : 0.0;
   }
-  dacc[2] = (S.obs & 4u) ? ekin_rows<N>(a, smx, ls, cnt, scale, bits, red) : 0.0;
   const double e_n = dacc[3], e_v = dacc[4];
   block_sum<3>(dacc, dred);  // its barriers also end the snapshot reads of smx
   if (threadIdx.x == 0) {
@@ -725,21 +828,23 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   }
   if (last) return;
   // next sub-step: opening X half (static factor and the length-gauge factors of the
-  // next coupling row) and the forward transform of the last axis
-  const bool real_f = S.mode == 1 && g.gauge != 1;
-  const int pre = product_headroom(bits);
-  u64 mag = 0;
+  // next coupling row; already applied when fused) and the forward transform of the last axis
+  if (!fuse_x) {
+    const bool real_f = S.mode == 1 && g.gauge != 1;
+    const int pre = product_headroom(bits);
+    u64 mag = 0;
 #pragma unroll 4
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const long long p = base + e;
-    longlong2 x = smx[e];
-    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 2), real_f);
-    smx[e] = x;
-    mag |= fmag(x);
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const long long p = base + e;
+      longlong2 x = smx[e];
+      if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+      x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 2), real_f);
+      smx[e] = x;
+      mag |= fmag(x);
+    }
+    scale += pre - xfactor_exp(g, S, 2);
+    bits = block_max_int(bitlen(mag), red);
   }
-  scale += pre - xfactor_exp(g, S, 2);
-  bits = block_max_int(bitlen(mag), red);
   sh = first_pass_shift<N>(bits);
   scale += sh;
   fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
@@ -761,9 +866,10 @@ __device__ __forceinline__ int p_phase(const GridDev& g, const StepDev& S, longl
   const int pre = product_headroom(bits);
   const int cnt = rows * Ch;
   u64 mag = 0;
+  TileWalk w(threadIdx.x, blockDim.x, Ch);
 #pragma unroll 4
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int i = e / Ch, c = e % Ch;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x, w.next()) {
+    const int i = w.i, c = w.c;
     longlong2 x = smx[i * ldc + c];
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
     const longlong2 f = pcol ? fmul62(S.ptab[(size_t)ax * S.nmax + i], pcol[c]) : S.ptab[(size_t)ax * S.nmax + i];
@@ -866,9 +972,10 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis(const 
   }
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
   const bool conj_out = MODE != 0;
+  TileWalk w(threadIdx.x, blockDim.x, Ch);
 #pragma unroll 4
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const int i = e / Ch, c = e % Ch;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x, w.next()) {
+    const int i = w.i, c = w.c;
     const longlong2 x = smx[i * C + c];
     out[obase + (long long)i * inner + c] = conj_out ? fconj(x) : x;
   }
