@@ -229,15 +229,6 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// Hint: bring [p, p + bytes) into L2 (bulk prefetch of the 16-byte aligned interior).
-__device__ __forceinline__ void prefetch_l2(const void* p, unsigned long long bytes) {
-  const unsigned long long a = (unsigned long long)p, lo = (a + 15) & ~15ull, hi = (a + bytes) & ~15ull;
-  for (unsigned long long q = lo; q < hi; q += 1u << 20) {
-    const unsigned n = (unsigned)((hi - q) < (1ull << 20) ? (hi - q) : (1ull << 20));
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(q), "r"(n) : "memory");
-  }
-}
-
 // (i, c) = (e / Ch, e % Ch) for e = e0, e0 + step, e0 + 2 step, ... without a division
 // per element (Ch is a runtime tile width in the strided-axis passes)
 struct TileWalk {
@@ -783,10 +774,6 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   const long long base = row0 * N;
   const int cnt = Lh * N;
   int bits = 0;
-  if (threadIdx.x == 0) {  // the X table (and potential) rows of this block, needed after the transform
-    prefetch_l2(S.xs + base, (unsigned long long)cnt * sizeof(longlong2));
-    if (S.obs & 2u) prefetch_l2(S.Vx + base, (unsigned long long)cnt * sizeof(long long));
-  }
   // producer of element (row, j): axis-0 tile j / C (2D) or axis-1 tile (i0, j / C) (3D,
   // when the block's rows share i0)
   __shared__ int dtab[N];
