@@ -4,13 +4,14 @@
 // restatement in oracle/qsf_oracle.c and the GPU path can be pinned against it.
 //
 // Test infrastructure only.  Built by oracle/Makefile (target `ref`) into oracle/_ref/
-// against the single-rank MPI and FFTW stand-ins in oracle/ref/shim/.
+// against the MPI and FFTW stand-ins in oracle/ref/shim/.
 //
 // Usage: qsf_ref <case> <outdir> key=value ...
 //   cases: prim2d, prim3d, c1 (1D IM + RE), c2 (2D IM + RE VG), c3 (3D RE LG),
 //          io1 / io2 / io3 (.psi save / load / backup / orthogonalizeWith / snapshot),
 //          mp (1D real time with MultiProductSplit of order 2 and 3, VG and LG),
-//          as2 / as3 (average_der of the potential, AntiSymmetrize<2> and <3>)
+//          as2 / as3 (average_der of the potential, AntiSymmetrize<2> and <3>),
+//          mg1 / mg2 / mg3 (multi-region grid, one process per region: QSF_SHIM_NP=2^D)
 #include "QSF.h"
 
 #include <map>
@@ -232,6 +233,38 @@ static void c3(const std::string& out) {
 }
 
 
+// ---------------------------------------------------------------- multigrid
+// Real-time run on the reference's multi-region grid (MultiCartesianGrid<D>: regions
+// NO, X, (Y, XY, ...), multigrid.h) with one process per region (QSF_SHIM_NP = 2^D).
+// The main region starts from seeded complex noise, the others from zero; each step
+// ends with the region transfer and the region masks (postCompute, multigrid.h:617-657).
+// Rank r (region r) writes psi_r<r>.bin; rank 0 also the main region's .dat rows.
+template <DIMS D> using MGrid = CAP<MultiCartesianGrid<D>>;
+
+template <DIMS D> static void mg(const std::string& out) {
+  using F = Field<D == 1 ? AXIS::X : (D == 2 ? AXIS::XY : AXIS::XYZ), Sin2>;
+  using C = DipoleCoupling<VelocityGauge, F>;
+  using Ham = Schrodinger::Spin0<MGrid<D>, Eberly, C>;
+  using Outs = BufferedBinaryOutputs<VALUE<Step, Time>, AVG<Identity>, AVG<PotentialEnergy>, AVG<KineticEnergy>>;
+  MGrid<D> grid(MultiCartesianGrid<D>(par("dx", 0.3), (ind)par("n", 32)), (ind)par("nCAP", 4));
+  Ham wf(grid, make_pot(), C(F(Sin2(field_cfg()))));
+  SplitPropagator<MODE::RE, Split, Ham> re(PropagatorBase{.dt = par("re_dt", 0.05), .max_steps = 0, .state_accuracy = 0},
+                                           std::move(wf), "RE");
+  const ind m = re.wf.m_l;
+  g_state = (uint64_t)par("seed", 1);
+  std::vector<cxd> psi0((size_t)m);
+  for (ind i = 0; i < m; i++) {
+    const double a = urand(), b = urand();
+    psi0[(size_t)i] = cxd(a, b);
+  }
+  for (ind i = 0; i < m; i++) re.wf[i] = MPI::region == 0 ? psi0[(size_t)i] : cxd(0.0, 0.0);
+  if (MPI::region == 0) dump(out + "/psi_in.bin", psi0.data(), m);
+  const std::string tag = "/psi_r" + std::to_string(MPI::region) + ".bin";
+  re.run(Outs(BufferedOutputsBase{1, 1}), [&](WHEN when, ind, uind, auto& w) {
+    if (when == WHEN::AT_END) dump(out + tag, &w[0], m);
+  });
+}
+
 // ---------------------------------------------------------------- .psi I/O
 // Writes the reference's .psi files (grid.h:948-1153) from a seeded state: X and P
 // representation, complex and probability (doubles) payloads, downscale 2, the
@@ -360,6 +393,11 @@ int main(int argc, char** argv) {
   }
   MPI::init(argc, argv);
   std::filesystem::current_path(out);
+  if (MPI::pID) {  // every rank but 0 in a directory of its own (each opens the .dat file)
+    const std::string sub = "rank" + std::to_string(MPI::pID);
+    std::filesystem::create_directories(sub);
+    std::filesystem::current_path(sub);
+  }
   out = ".";
   set_borders();
   if (cs == "prim2d") prim<2>(out);
@@ -374,6 +412,9 @@ int main(int argc, char** argv) {
   else if (cs == "mp") mp(out);
   else if (cs == "as2") as_case<2>(out);
   else if (cs == "as3") as_case<3>(out);
+  else if (cs == "mg1") mg<1>(out);
+  else if (cs == "mg2") mg<2>(out);
+  else if (cs == "mg3") mg<3>(out);
   else if (cs == "io1") io<1>(out);
   else if (cs == "io2") io<2>(out);
   else if (cs == "io3") io<3>(out);

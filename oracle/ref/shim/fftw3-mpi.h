@@ -9,8 +9,8 @@ static inline void fftw_mpi_init() {}
 static inline fftw_plan fftw_mpi_plan_many_dft(int rnk, const std::ptrdiff_t* n, std::ptrdiff_t howmany,
                                                std::ptrdiff_t, std::ptrdiff_t, fftw_complex* in,
                                                fftw_complex* out, MPI_Comm, int sign, unsigned flags) {
-  if (howmany != 1 || in != out) {
-    fprintf(stderr, "FFTW-MPI stand-in: only in-place, howmany=1 plans are available\n");
+  if (in != out || (howmany != 1 && (flags & (FFTW_MPI_TRANSPOSED_IN | FFTW_MPI_TRANSPOSED_OUT)))) {
+    fprintf(stderr, "FFTW-MPI stand-in: only in-place plans, transposed ones with howmany=1, are available\n");
     abort();
   }
   fftw_plan p = new qsf_shim_plan();
@@ -20,6 +20,7 @@ static inline fftw_plan fftw_mpi_plan_many_dft(int rnk, const std::ptrdiff_t* n,
   p->sign = sign;
   p->flags = flags;
   p->guru = false;
+  p->howmany = (long)howmany;
   return p;
 }
 

@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <vector>
+#include "qsf_shim_arena.h"
 
 extern "C" void orc_fft_nd(double* data, int dim, const long* n, int sign);
 
@@ -34,15 +35,22 @@ struct qsf_shim_plan {
   int sign;
   unsigned flags;
   bool guru;
+  long howmany;                      // FFTW-MPI "many" plans: trailing contiguous batch
+  std::vector<fftw_iodim64> dims;     // guru plans: transformed axes (n, stride in elements)
+  std::vector<fftw_iodim64> hdims;    // guru plans: batch axes
 };
 typedef qsf_shim_plan* fftw_plan;
 
 static inline void* fftw_malloc(size_t n) {
+  if (void* a = qsf_shim_arena_alloc(n ? n : 64)) return a;  // shared between ranks
   void* p = nullptr;
   if (posix_memalign(&p, 64, n ? n : 64)) return nullptr;
   return p;
 }
-static inline void fftw_free(void* p) { free(p); }
+static inline void fftw_free(void* p) {
+  if (qsf_shim_in_arena(p)) return;  // arena space is never reused
+  free(p);
+}
 static inline void fftw_print_plan(const fftw_plan) {}
 static inline void fftw_destroy_plan(fftw_plan p) { delete p; }
 
@@ -56,10 +64,64 @@ static inline void qsf_shim_swap01(double* d, long n0, long n1, long rest) {
   memcpy(d, tmp.data(), tmp.size() * sizeof(double));
 }
 
+/* gather the sub-array at `base` with the given axes (C order) into buf, or scatter back */
+static inline void qsf_shim_strided(double* base, const std::vector<fftw_iodim64>& d, double* buf, bool gather) {
+  const size_t r = d.size();
+  std::vector<long> idx(r, 0);
+  long total = 1;
+  for (auto& x : d) total *= (long)x.n;
+  for (long k = 0; k < total; ++k) {
+    long off = 0;
+    for (size_t a = 0; a < r; ++a) off += idx[a] * (long)d[a].is;
+    if (gather) memcpy(buf + 2 * k, base + 2 * off, 2 * sizeof(double));
+    else memcpy(base + 2 * off, buf + 2 * k, 2 * sizeof(double));
+    for (size_t a = r; a-- > 0;) {
+      if (++idx[a] < (long)d[a].n) break;
+      idx[a] = 0;
+    }
+  }
+}
+
 static inline void fftw_execute(const fftw_plan p) {
   if (p->guru) {
-    fprintf(stderr, "FFTW stand-in: guru (partial) plans are not available\n");
-    abort();
+    /* every combination of the batch axes: gather, transform, scatter (in place) */
+    std::vector<long> n;
+    long len = 1;
+    for (auto& x : p->dims) { n.push_back((long)x.n); len *= (long)x.n; }
+    std::vector<double> buf((size_t)(2 * len));
+    const size_t hr = p->hdims.size();
+    std::vector<long> h(hr, 0);
+    long batches = 1;
+    for (auto& x : p->hdims) batches *= (long)x.n;
+    for (long b = 0; b < batches; ++b) {
+      long off = 0;
+      for (size_t a = 0; a < hr; ++a) off += h[a] * (long)p->hdims[a].is;
+      qsf_shim_strided(p->data + 2 * off, p->dims, buf.data(), true);
+      orc_fft_nd(buf.data(), (int)n.size(), n.data(), p->sign);
+      qsf_shim_strided(p->data + 2 * off, p->dims, buf.data(), false);
+      for (size_t a = hr; a-- > 0;) {
+        if (++h[a] < (long)p->hdims[a].n) break;
+        h[a] = 0;
+      }
+    }
+    return;
+  }
+  if (p->howmany > 1) {
+    /* n[0] x ... x n[rank-1] x howmany, the batch index contiguous: one transform per batch index */
+    std::vector<fftw_iodim64> d;
+    long stride = p->howmany;
+    for (int a = p->rank; a-- > 0;) {
+      d.insert(d.begin(), fftw_iodim64{(std::ptrdiff_t)p->n[(size_t)a], (std::ptrdiff_t)stride, (std::ptrdiff_t)stride});
+      stride *= p->n[(size_t)a];
+    }
+    long len = stride / p->howmany;
+    std::vector<double> buf((size_t)(2 * len));
+    for (long b = 0; b < p->howmany; ++b) {
+      qsf_shim_strided(p->data + 2 * b, d, buf.data(), true);
+      orc_fft_nd(buf.data(), p->rank, p->n.data(), p->sign);
+      qsf_shim_strided(p->data + 2 * b, d, buf.data(), false);
+    }
+    return;
   }
   long rest = 1;
   for (int i = 2; i < p->rank; ++i) rest *= p->n[(size_t)i];
@@ -73,9 +135,23 @@ static inline void fftw_execute(const fftw_plan p) {
   }
 }
 
-static inline fftw_plan fftw_plan_guru64_dft(int, const fftw_iodim64*, int, const fftw_iodim64*, fftw_complex*,
-                                             fftw_complex*, int, unsigned) {
+/* in-place guru plan: `rank` transformed axes and `howmany_rank` batch axes, strides in
+ * complex elements (fftw_plan_guru64_dft) */
+static inline fftw_plan fftw_plan_guru64_dft(int rank, const fftw_iodim64* dims, int howmany_rank,
+                                             const fftw_iodim64* howmany_dims, fftw_complex* in, fftw_complex* out,
+                                             int sign, unsigned flags) {
+  if (in != out) {
+    fprintf(stderr, "FFTW stand-in: only in-place guru plans are available\n");
+    abort();
+  }
   fftw_plan p = new qsf_shim_plan();
   p->guru = true;
+  p->rank = rank;
+  p->data = reinterpret_cast<double*>(in);
+  p->sign = sign;
+  p->flags = flags;
+  p->howmany = 1;
+  p->dims.assign(dims, dims + rank);
+  p->hdims.assign(howmany_dims, howmany_dims + howmany_rank);
   return p;
 }
