@@ -89,6 +89,8 @@ def lib():
         L.orc_field_eval.restype = ctypes.c_double
         L.orc_field_max_duration.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_field_max_duration.restype = ctypes.c_double
+        L.orc_grid_set_region.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.orc_mg_transfer.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_int, ctypes.c_int]
     return _LIB
 
 
@@ -247,6 +249,18 @@ class Grid:
     def mask_region(self, bounded):
         b = (ctypes.c_int * 3)(*(list(bounded) + [1] * (3 - len(bounded))))
         lib().orc_mask_region(self._buf, self._p(), b)
+
+    def set_region(self, free_mask: int, multi: bool = True):
+        """Make this grid region `free_mask` (bit d: axis d kept in P space) of a
+        multi-region grid (multigrid.h, mpi_logic.h:104-150): partial potentials, no
+        absorber in evolve, fourier along the bounded axes only, untransposed P layout
+        unless it is the main region."""
+        self.free_mask = int(free_mask)
+        lib().orc_grid_set_region(self._buf, int(free_mask), 1 if multi else 0)
+
+    def mg_transfer_from(self, src: "Grid", fc: int, group: int):
+        """psi += FFT_fc(margins of src.psi along axis fc, masked) (multigrid.h:454-615)."""
+        lib().orc_mg_transfer(self._buf, self._p(), src._p(), int(fc), int(group))
 
     def average_der(self, direction: int) -> float:
         """average_der<X, direction, PotentialEnergy> (grid.h:443-465)."""
@@ -432,4 +446,79 @@ class Propagator:
             self.compute_each()
         self.make_step()
         self.compute_each()
+        return self.rows
+
+
+def region_axes(dim: int) -> List[int]:
+    """Free-axis masks of the regions of MultiRegionsReduced<dim> in region order
+    (mpi_logic.h:262-278): NO, X, (Y, XY) / NO, X, Y, Z, XY, XZ, YZ, XYZ."""
+    return {1: [0, 1], 2: [0, 1, 2, 3], 3: [0, 1, 2, 4, 3, 5, 6, 7]}[dim]
+
+
+def region_sources(dim: int) -> List[List[tuple]]:
+    """Per region, its sources (region index, transferred axis) in the order of
+    LocalGrid::init (multigrid.h:127-146): the regions with one free axis fewer whose
+    free set differs by exactly one axis."""
+    regs = region_axes(dim)
+    out = []
+    for fr in regs:
+        src = []
+        for i, fi in enumerate(regs):
+            if bin(fr).count("1") - bin(fi).count("1") == 1:
+                diff = fr ^ fi
+                if diff in (1, 2, 4):
+                    src.append((i, diff.bit_length() - 1))
+        out.append(src)
+    return out
+
+
+class MultiRegionPropagator:
+    """SplitPropagator over a multi-region grid (CAP<MultiCartesianGrid<dim>>), as the
+    reference runs it with one process per region: every region makes the same Strang
+    step on its own wavefunction (its own coupling state, partial potentials, fourier
+    along its bounded axes); the main region alone computes the outputs
+    (calcsEnabled, mpi_logic.h:247); then postCompute (multigrid.h:617-625): the
+    transfer from group to group (multigrid.h:627-657) and the region masks of every
+    group but the last (grid.h:582-597)."""
+
+    def __init__(self, dt: float, grids: List[Grid], couplings: List[Coupling], outputs: list):
+        self.dim = grids[0].dim
+        self.regions = region_axes(self.dim)
+        assert len(grids) == len(self.regions) == len(couplings)
+        self.groups = [bin(f).count("1") for f in self.regions]
+        self.sources = region_sources(self.dim)
+        self.props = []
+        for r, (g, c) in enumerate(zip(grids, couplings)):
+            g.coupling = c
+            g.set_region(self.regions[r], True)
+            self.props.append(Propagator(MODE_RE, dt, 0, g, outputs if r == 0 else []))
+        self.rows = self.props[0].rows
+
+    def post_compute(self):
+        G = max(self.groups) + 1
+        grids = [p.grid for p in self.props]
+        for gi in range(1, G):
+            for si in range(gi):
+                for r, fr in enumerate(self.regions):
+                    if self.groups[r] == gi:
+                        src, fc = self.sources[r][si]
+                        grids[r].mg_transfer_from(grids[src], fc, gi)
+        for r, fr in enumerate(self.regions):
+            if self.groups[r] != G - 1:
+                grids[r].mask_region([0 if (fr >> d) & 1 else 1 for d in range(self.dim)])
+
+    def _step_all(self):
+        for p in self.props:
+            p.make_step()
+
+    def run(self):
+        main = self.props[0]
+        main.compute_each()
+        while main.should_continue():
+            self._step_all()
+            main.compute_each()
+            self.post_compute()
+        self._step_all()
+        main.compute_each()
+        self.post_compute()
         return self.rows

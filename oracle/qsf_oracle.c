@@ -130,8 +130,9 @@ static void fft_line(orc_cx* x, orc_cx* y, long n, int sign) {
   if (in != x) memcpy(x, in, sizeof(orc_cx) * (size_t)n);
 }
 
-/* In-place N-D transform over all axes of a C-ordered array (last axis contiguous). */
-void orc_fft_nd(double* data, int dim, const long* n, int sign) {
+/* In-place transform along the axes d with use[d] != 0 (all axes: use == NULL) of a
+ * C-ordered array (last axis contiguous), last axis first. */
+void orc_fft_axes(double* data, int dim, const long* n, const int* use, int sign) {
   orc_cx* a = (orc_cx*)data;
   long m = 1;
   for (int d = 0; d < dim; ++d) m *= n[d];
@@ -143,6 +144,10 @@ void orc_fft_nd(double* data, int dim, const long* n, int sign) {
   for (int d = dim - 1; d >= 0; --d) {
     long nd = n[d];
     long outer = m / (nd * stride);
+    if (use && !use[d]) {
+      stride *= nd;
+      continue;
+    }
     for (long o = 0; o < outer; ++o)
       for (long in = 0; in < stride; ++in) {
         orc_cx* base = a + o * nd * stride + in;
@@ -159,6 +164,9 @@ void orc_fft_nd(double* data, int dim, const long* n, int sign) {
   free(line);
   free(scr);
 }
+
+/* In-place N-D transform over all axes of a C-ordered array (last axis contiguous). */
+void orc_fft_nd(double* data, int dim, const long* n, int sign) { orc_fft_axes(data, dim, n, NULL, sign); }
 
 /* ------------------------------------------------------------------ grid */
 
@@ -181,6 +189,8 @@ typedef struct {
   int gauge;
   int n_fields; /* coupling has this many fields; 0 -> coupling term is exactly 0 */
   int p_swap;   /* emulate the transposed P layout (coupling of axes 0 and 1 swapped) */
+  int free_mask; /* region of a multi-region grid: axes kept in P space (bit d = axis d) */
+  int multi;     /* multi-region grid: partial potentials, no absorber in evolve */
 } orc_grid;
 
 /* coords.h:55-93 (CartesianGrid_::init), absorbers.h:27-33 (eta), potential.h:122-124 */
@@ -224,6 +234,15 @@ void orc_grid_init(orc_grid* g, int dim, const long* n, const double* dx, long n
   g->p_swap = dim >= 2 ? 1 : 0;
 }
 
+/* Region `free_mask` of a multi-region grid (mpi_logic.h:104-150, multigrid.h:11-47):
+ * only the main region (free_mask 0) keeps the transposed P layout
+ * (canLeaveTransposed, grid.h:118) */
+void orc_grid_set_region(orc_grid* g, int free_mask, int multi) {
+  g->free_mask = free_mask;
+  g->multi = multi;
+  g->p_swap = (g->dim >= 2 && free_mask == 0) ? 1 : 0;
+}
+
 /* coords.h:132-138 */
 static inline double pos(const orc_grid* g, int rep, int d, long i) {
   if (rep == ORC_REP_X) return g->xmin[d] + (double)i * g->dx[d];
@@ -237,8 +256,32 @@ static inline double ee_i(const orc_grid* g, double x, double y) {
 }
 static inline double Ne_i(const orc_grid* g, double x) { return g->NEcharge / sqrt(x * x + g->Nsoft); }
 
+/* ReducedDimInteraction::partial (potential.h:144-178): interactions of the bounded
+ * coordinates only; fc = free-axis mask (1 X, 2 Y, 4 Z) */
+static inline double partial_potential(const orc_grid* g, int fc, const double* c) {
+  if (g->dim == 1) return fc == 0 ? Ne_i(g, c[0]) : 0.0;
+  if (g->dim == 2) {
+    if (fc == 0) return ee_i(g, c[0], c[1]) + Ne_i(g, c[0]) + Ne_i(g, c[1]);
+    if (fc == 2) return Ne_i(g, c[0]);
+    if (fc == 1) return Ne_i(g, c[1]);
+    return 0.0;
+  }
+  switch (fc) {
+    case 0: return ee_i(g, c[0], c[1]) + ee_i(g, c[1], c[2]) + ee_i(g, c[2], c[0]) + Ne_i(g, c[0]) + Ne_i(g, c[1]) +
+                   Ne_i(g, c[2]);
+    case 4: return ee_i(g, c[0], c[1]) + Ne_i(g, c[0]) + Ne_i(g, c[1]);
+    case 2: return ee_i(g, c[0], c[2]) + Ne_i(g, c[0]) + Ne_i(g, c[2]);
+    case 1: return ee_i(g, c[1], c[2]) + Ne_i(g, c[1]) + Ne_i(g, c[2]);
+    case 6: return Ne_i(g, c[0]);
+    case 5: return Ne_i(g, c[1]);
+    case 3: return Ne_i(g, c[2]);
+    default: return 0.0;
+  }
+}
+
 static inline double potential(const orc_grid* g, const double* c) {
   if (g->pot == ORC_POT_NONE) return 0.0;
+  if (g->multi) return partial_potential(g, g->free_mask, c);
   if (g->pot == ORC_POT_COULOMB) {
     double s;
     if (g->dim == 1) s = c[0] * c[0];
@@ -318,6 +361,71 @@ void orc_mask_region(const orc_grid* g, double* psi_d, const int* bounded) {
   }
 }
 
+/* CAP::mask of one node (absorbers.h:48-54): 1 outside the margin */
+static inline double mask1(const orc_grid* g, long nd) {
+  long nodes = g->nCAP + nd;
+  if (nodes < 0) return 1.0;
+  double v = nodes > 0 ? (double)(nodes * (nodes * (nodes * nodes))) : 0.0;
+  return exp(-(v + 0) * g->eta);
+}
+
+/* Region transfer (multigrid.h:454-615, one source): the absorber margins of `src`
+ * along axis fc (both edges; in 3D only the boxes of nCAP planes along the sliding
+ * axis, n / nCAP of them) times inv_mask(fc) and, for a destination in group 1, the
+ * corner correction; then the forward DFT along fc (unnormalised) and dst += slice.
+ * In 1D getBox copies whole rows, and the one row is the whole line: the interior
+ * between the margins enters the slice unmasked (getBox / maskSlice, multigrid.h:
+ * 454-481, 532-569, with an empty index pack). */
+void orc_mg_transfer(const orc_grid* g, double* dst_d, const double* src_d, int fc, int group) {
+  const orc_cx* src = (const orc_cx*)src_d;
+  orc_cx* dst = (orc_cx*)dst_d;
+  orc_cx* slice = (orc_cx*)calloc((size_t)g->m, sizeof(orc_cx));
+  const int D = g->dim;
+  const int slide = D == 3 ? (fc == 1 ? 2 : 1) : -1;
+  const long slide_lim = D == 3 ? (g->n[0] / g->nCAP) * g->nCAP : 0;
+  long idx[3] = {0, 0, 0};
+  for (long p = 0; p < g->m; ++p) {
+    long r = p;
+    for (int d = D - 1; d >= 0; --d) { idx[d] = r % g->n[d]; r /= g->n[d]; }
+    const long i = idx[fc];
+    if (!(i < g->nCAP || i >= g->n[fc] - g->nCAP)) {
+      if (D == 1) slice[p] = src[p];
+      continue;
+    }
+    if (slide >= 0 && idx[slide] >= slide_lim) continue;
+    const double mv = 1.0 - mask1(g, neg_dist_from_edge(g, fc, i));
+    double f = mv;
+    if (group == 1) {
+      double corr = 1.0;
+      if (D == 2) {
+        const int o = 1 - fc;
+        const double b0 = fc == 0 ? 1.0 : 1.0 - mask1(g, neg_dist_from_edge(g, o, idx[o]));
+        const double b1 = fc == 1 ? 1.0 : 1.0 - mask1(g, neg_dist_from_edge(g, o, idx[o]));
+        corr = 1 - 0.5 * (b0 * b1);
+      } else if (D == 3) {
+        double a[3], b[3];
+        for (int d = 0; d < 3; ++d) {
+          const double mk = mask1(g, neg_dist_from_edge(g, d, idx[d]));
+          a[d] = d == fc ? 0 : mk;
+          b[d] = d == fc ? 1.0 : mk;
+        }
+        corr = 0.5 * (a[0] + (a[1] + (a[2] + 0))) + (1.0 / 6.0) * (1 - (b[0] * (b[1] * b[2])));
+      }
+      f = mv * corr;
+    }
+    slice[p].re = src[p].re * f;
+    slice[p].im = src[p].im * f;
+  }
+  int use[3] = {0, 0, 0};
+  use[fc] = 1;
+  orc_fft_axes((double*)slice, D, g->n, use, -1);
+  for (long p = 0; p < g->m; ++p) {
+    dst[p].re += slice[p].re;
+    dst[p].im += slice[p].im;
+  }
+  free(slice);
+}
+
 /* coupling vector as seen by the P-space loop; the reference's P layout for dim>1 is
  * axis-0/1 transposed (grid.h:242-247), so its loop applies the axis-0 coupling to
  * the physical axis-1 wavenumber; on square grids this equals a swap of cv[0], cv[1]. */
@@ -351,7 +459,7 @@ void orc_evolve(const orc_grid* g, double* psi_d, int mode, int rep, double delt
       orc_cx f = {cos(-val), sin(-val)};
       psi[i] = cmul(psi[i], f);
     }
-    if (rep == ORC_REP_X && g->nCAP > 0) {
+    if (rep == ORC_REP_X && g->nCAP > 0 && !g->multi) {
       for (int d = 0; d < g->dim; ++d) nodes[d] = neg_dist_from_edge(g, d, idx[d]);
       double a = absorb(g, delta, nodes);
       psi[i].re *= a;
@@ -362,6 +470,24 @@ void orc_evolve(const orc_grid* g, double* psi_d, int mode, int rep, double delt
 
 /* grid.h:369-378 (fourier) + 363-367 (normalizeAfterTwoFFT) */
 void orc_fourier(const orc_grid* g, double* psi_d, int to_rep) {
+  if (g->free_mask) {
+    /* fourier_partial (multigrid.h:660-674): the bounded axes only, then the product of
+     * their 1/n on the way back (when there is any bounded axis) */
+    int use[3] = {0, 0, 0}, any = 0;
+    double s = 1.0;
+    for (int d = 0; d < g->dim; ++d) {
+      use[d] = !((g->free_mask >> d) & 1);
+      any |= use[d];
+      s *= use[d] ? 1.0 / (double)g->n[d] : 1.0;
+    }
+    if (!any) return;
+    orc_fft_axes(psi_d, g->dim, g->n, use, to_rep == ORC_REP_P ? -1 : +1);
+    if (to_rep == ORC_REP_X) {
+      orc_cx* psi = (orc_cx*)psi_d;
+      for (long i = 0; i < g->m; ++i) { psi[i].re *= s; psi[i].im *= s; }
+    }
+    return;
+  }
   orc_fft_nd(psi_d, g->dim, g->n, to_rep == ORC_REP_P ? -1 : +1);
   if (to_rep == ORC_REP_X) {
     orc_cx* psi = (orc_cx*)psi_d;

@@ -126,3 +126,22 @@ def gpu_re(p, dim, psi0):
     prop = Q.SplitPropagator(Q.MODE_RE, p["re_dt"], 0, g, c, re_outputs(dim, int(p.get("box", 0))))
     rows = prop.run()
     return g, rows
+
+
+MG_OUTPUTS = ["step", "time", "norm", "epot", "ekin"]
+
+
+def mg_dat_row(row):
+    return [row[k] for k in MG_OUTPUTS]
+
+
+def oracle_mg(p, dim, psi0):
+    """The fixture's multi-region run on the oracle: one grid and one coupling per
+    region (each region's process keeps its own coupling state in the reference)."""
+    regs = O.region_axes(dim)
+    cs = [O.Coupling(O.GAUGE_VELOCITY, [O.Field(field_axis(dim), [pulse(p)])]) for _ in regs]
+    gs = [oracle_grid(p, dim, c) for c in cs]
+    gs[0].psi[...] = psi0
+    mp = O.MultiRegionPropagator(p["re_dt"], gs, cs, MG_OUTPUTS)
+    rows = mp.run()
+    return gs, rows

@@ -46,6 +46,14 @@ CASES = {
     # average_der of the potential, AntiSymmetrize<2> (2D, 3D) and <3> (3D)
     "as2": ("as2", dict(n=12, dx=0.5, nCAP=1, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, seed=5), 0, 0, 2),
     "as3": ("as3", dict(n=8, dx=0.5, nCAP=1, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, seed=6), 0, 0, 3),
+    # multi-region grids (multigrid.h), one process per region: the main region's .dat
+    # rows and every region's final wavefunction
+    "mg1": ("mg1", dict(n=128, dx=0.3, nCAP=16, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, seed=3, F0=0.1, omega=1.0,
+                        ncycles=1, re_dt=0.05), 0, 5, 1),
+    "mg2": ("mg2", dict(n=32, dx=0.4, nCAP=4, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, seed=5, F0=0.1, omega=1.0,
+                        ncycles=1, re_dt=0.05), 0, 5, 2),
+    "mg3": ("mg3", dict(n=8, dx=0.5, nCAP=3, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, seed=9, F0=0.12, omega=1.5,
+                        ncycles=1, re_dt=0.05), 0, 5, 3),
     "io1": ("io1", dict(n=16, dx=0.3, nCAP=2, seed=3), 0, 0, 1),
     "io2": ("io2", dict(n=8, dx=0.5, nCAP=1, seed=5), 0, 0, 2),
     "io3": ("io3", dict(n=8, dx=0.4, nCAP=1, seed=9), 0, 0, 3),
@@ -64,7 +72,10 @@ def make(name):
     shape = (int(params["n"]),) * dim
     with tempfile.TemporaryDirectory() as tmp:
         args = [REF, case, tmp] + [f"{k}={v}" for k, v in params.items()]
-        subprocess.run(args, check=True, stdout=subprocess.DEVNULL)
+        env = dict(os.environ)
+        if case.startswith("mg"):  # one rank per region of MultiRegionsReduced<dim>
+            env["QSF_SHIM_NP"] = str(2 ** dim)
+        subprocess.run(args, check=True, stdout=subprocess.DEVNULL, env=env)
         out = {"params": json.dumps(params), "case": case, "dim": dim}
         if case in ("as2", "as3"):
             out["psi_in"] = _read_psi(os.path.join(tmp, "psi_in.bin"), shape)
@@ -77,6 +88,12 @@ def make(name):
                 out[tag + "_psi0"] = _read_psi(os.path.join(tmp, tag + "_psi0.bin"), shape)
                 out[tag + "_psi"] = _read_psi(os.path.join(tmp, tag + "_psi.bin"), shape)
                 out[tag + "_rows"] = np.fromfile(os.path.join(tmp, tag + ".dat"), dtype=np.float64).reshape(-1, re_cols)
+        elif case.startswith("mg"):
+            out["psi_in"] = _read_psi(os.path.join(tmp, "psi_in.bin"), shape)
+            for r in range(2 ** dim):
+                sub = "" if r == 0 else "rank%d" % r
+                out["psi_r%d" % r] = _read_psi(os.path.join(tmp, sub, "psi_r%d.bin" % r), shape)
+            out["re_rows"] = np.fromfile(os.path.join(tmp, "RE.dat"), dtype=np.float64).reshape(-1, re_cols)
         elif case.startswith("io"):
             for f in ("psi_in", "psi_b", "psi_after_sp", "psi_load_sx", "psi_load_sn", "psi_orth"):
                 out[f] = _read_psi(os.path.join(tmp, f + ".bin"), shape)
