@@ -95,6 +95,18 @@ typedef struct qsf_grid_desc {
                          space, as the reference's transposed P layout does
                          (grid.h:242-247); ignored for dim == 1                    */
   int64_t border_nodes[4]; /* p_NS, p_SD, p_DT, p_CAP (borders.h:30-36); 0 = default */
+  /* Region of a multi-region grid (CAP<MultiCartesianGrid<D>>, multigrid.h; regions of
+   * MultiRegionsReduced<D>, mpi_logic.h:262-278).  multi_region = 0: an ordinary grid
+   * (both fields 0).  multi_region = 1: evolve applies no absorber (the region masks of
+   * qsf_mask_region take its place after each step) and the potential is the partial
+   * one of the region (ReducedDimInteraction::partial, potential.h:144-178);
+   * free_axes (bit d = axis d) are the axes the region keeps in momentum space:
+   * qsf_fourier transforms the other (bounded) axes only and scales by the product of
+   * their 1/n (fourier_partial, multigrid.h:660-674), and the P layout is untransposed
+   * (set p_axis_swap = 0) unless free_axes = 0 (the main region).  Regions with free
+   * axes step through the member operations; qsf_step rejects them.              */
+  int free_axes;
+  int multi_region;
 } qsf_grid_desc;
 
 typedef struct qsf_grid qsf_grid;
@@ -122,6 +134,18 @@ int qsf_fourier(qsf_grid* g, int to_rep);
  * the absorber (absorbers.h:40-46).  coupling[3] holds the coupling values per axis
  * (A in the velocity gauge, E in the length gauge, as _coupling[Axis<d>] returns). */
 int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* coupling3);
+/* Region transfer of a multi-region grid, one source (LocalGrid<..., Slices, true>::
+ * transfer / coherentAddition, multigrid.h:454-657): dst += DFT_axis(slice), slice =
+ * src in the absorber margins along `axis` (both edges), times 1 - mask of that axis
+ * and, when dst is in group 1 (one free axis), the corner correction mask_correction
+ * (multigrid.h:519-530); in 3D only the n / nCAP boxes of nCAP planes along the
+ * sliding axis take part, in 1D the whole line enters and only its margins are masked
+ * (as the reference's getBox / maskSlice do).  The DFT is forward and unnormalised.
+ * `group` is dst's number of free axes; src must be the region with `axis` bounded and
+ * dst's other free axes free.  Both grids need the same geometry and 2 nCAP <= n.
+ * The call orders dst's stream after src's and src's after the transfer. */
+int qsf_region_transfer(qsf_grid* dst, const qsf_grid* src, int axis, int group);
+
 /* average<R, Op>() (grid.h:425-441). */
 int qsf_average(qsf_grid* g, int rep, int op, double* out);
 /* operation<M, R, Normalize>() (grid.h:601-606); returns the norm divided out. */

@@ -37,6 +37,8 @@ class GridDesc(ctypes.Structure):
         ("n_fields", ctypes.c_int),
         ("p_axis_swap", ctypes.c_int),
         ("border_nodes", ctypes.c_int64 * 4),
+        ("free_axes", ctypes.c_int),
+        ("multi_region", ctypes.c_int),
     ]
 
 
@@ -150,6 +152,7 @@ def lib():
         "qsf_normalize": [vp, dp],
         "qsf_flux": [vp, dp, ctypes.c_int, ip, i64, dp],
         "qsf_mask_region": [vp, ip],
+        "qsf_region_transfer": [vp, vp, ctypes.c_int, ctypes.c_int],
         "qsf_add_gaussian": [vp, ctypes.c_double, ctypes.c_double],
         "qsf_step": [vp, ctypes.POINTER(StepDesc), dp, ctypes.POINTER(i64)],
         "qsf_fft_plan_radices": [i64, ip, ip],

@@ -410,6 +410,8 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   if (d->nsteps < 1) return fail(QSF_EINVAL, "nsteps < 1");
   if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
   if (d->substeps < 0 || d->substeps > 64) return fail(QSF_EINVAL, "substeps must be in [0, 64]");
+  if (g->G.free_mask)
+    return fail(QSF_EINVAL, "a region with free axes keeps them in momentum space: step it with the member operations");
   const GridDev& G = g->G;
   const int K = std::max(1, d->substeps);
   const int64_t total = d->nsteps * K;  // sub-steps
@@ -656,6 +658,17 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   if (d->dim >= 2 && d->n[0] > kMaxTile) return fail(QSF_EINVAL, "axes longer than 4096 points are not supported");
   if (d->potential < 0 || d->potential > 3) return fail(QSF_EINVAL, "unknown potential");
   if (d->gauge != QSF_GAUGE_VELOCITY && d->gauge != QSF_GAUGE_LENGTH) return fail(QSF_EINVAL, "unknown gauge");
+  if (d->multi_region != 0 && d->multi_region != 1) return fail(QSF_EINVAL, "multi_region must be 0 or 1");
+  if (d->free_axes < 0 || d->free_axes >= (1 << d->dim) || (d->free_axes && !d->multi_region))
+    return fail(QSF_EINVAL, "free_axes must be a mask of the grid's axes, on a multi-region grid");
+  if (d->multi_region) {
+    // multigrid.h:19 (an absorber is required); partial potentials exist for the
+    // reduced-dimensionality interactions (potential.h:144-178)
+    if (d->nCAP < 1 || 2 * d->nCAP > d->n[0])
+      return fail(QSF_EINVAL, "a multi-region grid needs 1 <= nCAP <= n / 2");
+    if (d->potential == QSF_POT_COULOMB)
+      return fail(QSF_EINVAL, "multi-region grids need a reduced-dimensionality interaction (no partial Coulomb)");
+  }
   if (int rc = init_kernel_table()) return rc;
   const KernelSet* ks = kernels_for((int)d->n[0]);
   if (!ks) return fail(QSF_EINVAL, "grid size " + std::to_string(d->n[0]) + " has no kernels in this build");
@@ -745,6 +758,8 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   G.gauge = d->gauge;
   G.n_fields = d->n_fields;
   G.p_swap = d->p_axis_swap ? 1 : 0;
+  G.free_mask = d->free_axes;
+  G.multi = d->multi_region;
   if (d->border_nodes[0] > 0) g->bn.NS = d->border_nodes[0];
   if (d->border_nodes[1] > 0) g->bn.SD = d->border_nodes[1];
   if (d->border_nodes[2] > 0) g->bn.DT = d->border_nodes[2];
@@ -828,6 +843,8 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->fterms);
   fr(g->dG);
   fr(g->dS);
+  fr(g->mg_slice);
+  if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->own_stream) cudaStreamDestroy(g->stream);
   delete g;
   return QSF_OK;
@@ -867,16 +884,12 @@ int qsf_synchronize(qsf_grid* g) {
   return QSF_OK;
 }
 
-int qsf_fourier(qsf_grid* g, int to_rep) {
-  if (!g || (to_rep != QSF_REP_X && to_rep != QSF_REP_P)) return fail(QSF_EINVAL, "bad argument");
-  const GridDev& G = g->G;
+// one-axis transform of the array G.psi (grid geometry of g), scaled by sc on the way out
+static void axis_fft(qsf_grid* g, const GridDev& G, int ax, bool fwd, double sc) {
   const KernelSet& K = *g->ks;
   const int D = G.dim;
-  const bool fwd = to_rep == QSF_REP_P;
-  const double last_scale = fwd ? 1.0 : G.inv_m;
   cudaStream_t st = g->stream;
-  for (int ax = D - 1; ax >= 0; --ax) {
-    const double sc = ax == 0 ? last_scale : 1.0;
+  {
     if (ax == D - 1) {
       // rows of the last axis with up to 16 * kLineThreads points per block
       const int n = G.ax[ax].n;
@@ -895,7 +908,64 @@ int qsf_fourier(qsf_grid* g, int to_rep) {
       else K.axis_fft_b<<<g->ax_blocks[ax], kRowThreads, g->ax_smem[ax], st>>>(G, ax, g->ax_C[ax], sc);
     }
   }
+}
+
+int qsf_fourier(qsf_grid* g, int to_rep) {
+  if (!g || (to_rep != QSF_REP_X && to_rep != QSF_REP_P)) return fail(QSF_EINVAL, "bad argument");
+  const GridDev& G = g->G;
+  const int D = G.dim;
+  const bool fwd = to_rep == QSF_REP_P;
+  // the axes a region keeps in momentum space are not transformed; the way back scales by
+  // the product of the transformed axes' 1/n (fourier_partial, multigrid.h:660-674)
+  int last = -1;
+  double partial = 1.0;
+  for (int ax = 0; ax < D; ++ax) {
+    const bool use = !((G.free_mask >> ax) & 1);
+    partial *= use ? 1.0 / (double)G.ax[ax].n : 1.0;
+    if (use && last < 0) last = ax;
+  }
+  if (last < 0) return QSF_OK;
+  const double back = G.free_mask ? partial : G.inv_m;
+  for (int ax = D - 1; ax >= 0; --ax) {
+    if ((G.free_mask >> ax) & 1) continue;
+    axis_fft(g, G, ax, fwd, ax == last && !fwd ? back : 1.0);
+  }
   QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+int qsf_region_transfer(qsf_grid* dst, const qsf_grid* src, int axis, int group) {
+  if (!dst || !src || dst == src) return fail(QSF_EINVAL, "two distinct grids are needed");
+  const GridDev& G = dst->G;
+  const GridDev& H = src->G;
+  if (!G.multi || !H.multi) return fail(QSF_EINVAL, "region transfers need grids created with multi_region = 1");
+  if (axis < 0 || axis >= G.dim) return fail(QSF_EINVAL, "axis out of range");
+  if (G.dim != H.dim || G.m != H.m || G.nCAP != H.nCAP) return fail(QSF_EINVAL, "the grids differ in geometry");
+  for (int k = 0; k < G.dim; ++k)
+    if (G.ax[k].n != H.ax[k].n || G.ax[k].dx != H.ax[k].dx) return fail(QSF_EINVAL, "the grids differ in geometry");
+  const int bit = 1 << axis;
+  int nfree = 0;
+  for (int k = 0; k < G.dim; ++k) nfree += (G.free_mask >> k) & 1;
+  if (!(G.free_mask & bit) || H.free_mask != (G.free_mask & ~bit) || group != nfree)
+    return fail(QSF_EINVAL, "src must be dst's region with `axis` bounded, and group dst's number of free axes");
+  if (!dst->mg_slice)
+    if (int rc = dev_alloc(dst->mg_slice, (size_t)G.m)) return rc;
+  if (!dst->mg_event) QSF_CU(cudaEventCreateWithFlags(&dst->mg_event, cudaEventDisableTiming));
+  qsf_grid* s = const_cast<qsf_grid*>(src);
+  if (!s->mg_event) QSF_CU(cudaEventCreateWithFlags(&s->mg_event, cudaEventDisableTiming));
+  // dst's stream after src's work; src's after the transfer has read it
+  QSF_CU(cudaEventRecord(s->mg_event, s->stream));
+  QSF_CU(cudaStreamWaitEvent(dst->stream, s->mg_event, 0));
+  // boxes of nCAP planes along the sliding axis (multigrid.h:184, 296-317): n / nCAP of them
+  const long long slide_lim = G.dim == 3 ? (G.ax[0].n / G.nCAP) * G.nCAP : 0;
+  k_mg_slice<<<grid_blocks(G.m), 256, 0, dst->stream>>>(G, H.psi, dst->mg_slice, axis, group, slide_lim);
+  GridDev Gs = G;
+  Gs.psi = dst->mg_slice;
+  axis_fft(dst, Gs, axis, true, 1.0);
+  k_add_slice<<<grid_blocks(G.m), 256, 0, dst->stream>>>(G.psi, dst->mg_slice, G.m);
+  QSF_CU(cudaGetLastError());
+  QSF_CU(cudaEventRecord(dst->mg_event, dst->stream));
+  QSF_CU(cudaStreamWaitEvent(s->stream, dst->mg_event, 0));
   return QSF_OK;
 }
 

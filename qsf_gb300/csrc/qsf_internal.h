@@ -112,4 +112,7 @@ struct qsf_grid {
   int ax_C[3] = {1, 1, 1};
   int ax_blocks[3] = {0, 0, 0};
   size_t ax_smem[3] = {0, 0, 0};
+  // multi-region transfer: slice buffer (m points) and the event that orders streams
+  double2* mg_slice = nullptr;
+  cudaEvent_t mg_event = nullptr;
 };

@@ -63,6 +63,8 @@ struct GridDev {
   int pot;
   double NEcharge, EEcharge, Nsoft, Esoft;
   int gauge, n_fields, p_swap;
+  int free_mask;  // region of a multi-region grid: axes kept in momentum space (bit d)
+  int multi;      // multi-region grid: partial potentials, no absorber in evolve
   double2* psi;
 };
 
@@ -163,9 +165,37 @@ __device__ __forceinline__ void block_sum(double* v, double* red) {
 __device__ __forceinline__ double xpos(const AxisDev& a, int i) { return a.xmin + (double)i * a.dx; }
 __device__ __forceinline__ double kpos(const AxisDev& a, int i) { return a.dp * (double)(i < a.n2 ? i : i - a.n); }
 
+// ReducedDimInteraction::partial (potential.h:144-178): the interactions of the bounded
+// coordinates of region fc (free-axis mask), same operation order
+__device__ __forceinline__ double partial_potential(const GridDev& g, int fc, const double* c) {
+  auto ne = [&](double x) { return g.NEcharge / sqrt(x * x + g.Nsoft); };
+  auto ee = [&](double x, double y) {
+    return g.pot == 1 ? g.EEcharge / sqrt((x - y) * (x - y) + x * y + g.Esoft)
+                      : g.EEcharge / sqrt((x - y) * (x - y) + g.Esoft);
+  };
+  if (g.dim == 1) return fc == 0 ? ne(c[0]) : 0.0;
+  if (g.dim == 2) {
+    if (fc == 0) return ee(c[0], c[1]) + ne(c[0]) + ne(c[1]);
+    if (fc == 2) return ne(c[0]);
+    if (fc == 1) return ne(c[1]);
+    return 0.0;
+  }
+  switch (fc) {
+    case 0: return ee(c[0], c[1]) + ee(c[1], c[2]) + ee(c[2], c[0]) + ne(c[0]) + ne(c[1]) + ne(c[2]);
+    case 4: return ee(c[0], c[1]) + ne(c[0]) + ne(c[1]);
+    case 2: return ee(c[0], c[2]) + ne(c[0]) + ne(c[2]);
+    case 1: return ee(c[1], c[2]) + ne(c[1]) + ne(c[2]);
+    case 6: return ne(c[0]);
+    case 5: return ne(c[1]);
+    case 3: return ne(c[2]);
+    default: return 0.0;
+  }
+}
+
 // potential at a point (potential.h:130-143 and 40-44), same operation order
 __device__ __forceinline__ double potential_at(const GridDev& g, const double* c) {
   if (g.pot == 3) return 0.0;
+  if (g.multi) return partial_potential(g, g.free_mask, c);
   if (g.pot == 2) {
     double s;
     if (g.dim == 1) s = c[0] * c[0];
@@ -385,7 +415,7 @@ __global__ void k_build_static(GridDev g, int mode, double delta, int xs_exp, lo
     const double v = potential_at(g, c);
     Vx[p] = __double2ll_rn(v * vs);
     const double2 f = expop(mode, delta * v);
-    const double a = absorb_at(g, delta, idx) * xsc;
+    const double a = (g.multi ? 1.0 : absorb_at(g, delta, idx)) * xsc;
     const double2 fa = make_double2(f.x * a, f.y * a);
     xsx[p] = to_fx62(make_double2(fmin(fmax(fa.x, -1.0), 1.0), fmin(fmax(fa.y, -1.0), 1.0)));
   }
@@ -1281,7 +1311,7 @@ __global__ void k_evolve(GridDev g, int mode, int rep, double delta, double c0, 
       sincos(-val, &sn, &cs);
       v = make_double2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
     }
-    if (rep == 1 && g.nCAP > 0) v = cscale(v, absorb_at(g, delta, idx));
+    if (rep == 1 && g.nCAP > 0 && !g.multi) v = cscale(v, absorb_at(g, delta, idx));
     g.psi[p] = v;
   }
 }
@@ -1328,6 +1358,70 @@ __global__ void k_gather(const double2* psi, const long long* idx, int n, double
 }
 
 // maskRegion (grid.h:582-597) with CAP::mask (absorbers.h:48-54)
+// CAP::mask of one node (absorbers.h:48-54): 1 outside the margin
+__device__ __forceinline__ double mask1(const GridDev& g, long long nd) {
+  const long long nodes = g.nCAP + nd;
+  if (nodes < 0) return 1.0;
+  const double v = nodes > 0 ? (double)(nodes * (nodes * (nodes * nodes))) : 0.0;
+  return exp(-(v + 0) * g.eta);
+}
+__device__ __forceinline__ long long neg_dist(const GridDev& g, int d, int i) {
+  return i < g.ax[d].n2 ? -(long long)i : (long long)i - g.ax[d].n + 1;
+}
+
+// Slice of a region transfer (getBox + maskSlice, multigrid.h:454-569): src in the
+// margins along fc times 1 - mask(fc) and, for a destination in group 1, the corner
+// correction (mask_correction, multigrid.h:519-530); zero elsewhere, except in 1D,
+// where the whole line is copied and only its margins are masked.  In 3D the sliding
+// axis is limited to the n / nCAP boxes (slide_lim planes).
+__global__ void k_mg_slice(GridDev g, const double2* __restrict__ src, double2* __restrict__ slice, int fc, int group,
+                           long long slide_lim) {
+  const int D = g.dim;
+  const int slide = D == 3 ? (fc == 1 ? 2 : 1) : -1;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
+    int idx[kMaxDim];
+    unflatten(g, p, idx);
+    const int i = idx[fc];
+    const bool band = i < g.nCAP || i >= g.ax[fc].n - g.nCAP;
+    if (!band || (slide >= 0 && idx[slide] >= slide_lim)) {
+      slice[p] = (D == 1 && !band) ? src[p] : make_double2(0.0, 0.0);
+      continue;
+    }
+    const double mv = 1.0 - mask1(g, neg_dist(g, fc, i));
+    double f = mv;
+    if (group == 1) {
+      double corr = 1.0;
+      if (D == 2) {
+        const int o = 1 - fc;
+        const double b0 = fc == 0 ? 1.0 : 1.0 - mask1(g, neg_dist(g, o, idx[o]));
+        const double b1 = fc == 1 ? 1.0 : 1.0 - mask1(g, neg_dist(g, o, idx[o]));
+        corr = 1 - 0.5 * (b0 * b1);
+      } else if (D == 3) {
+        double a[3], b[3];
+        for (int d = 0; d < 3; ++d) {
+          const double mk = mask1(g, neg_dist(g, d, idx[d]));
+          a[d] = d == fc ? 0 : mk;
+          b[d] = d == fc ? 1.0 : mk;
+        }
+        corr = 0.5 * (a[0] + (a[1] + (a[2] + 0))) + (1.0 / 6.0) * (1 - (b[0] * (b[1] * b[2])));
+      }
+      f = mv * corr;
+    }
+    const double2 v = src[p];
+    slice[p] = make_double2(v.x * f, v.y * f);
+  }
+}
+
+// coherent addition (add, multigrid.h:571-586): dst += slice
+__global__ void k_add_slice(double2* __restrict__ dst, const double2* __restrict__ slice, long long m) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += stride) {
+    const double2 a = dst[p], b = slice[p];
+    dst[p] = make_double2(a.x + b.x, a.y + b.y);
+  }
+}
+
 __global__ void k_mask(GridDev g, int b0, int b1, int b2) {
   const int bounded[3] = {b0, b1, b2};
   const long long stride = (long long)gridDim.x * blockDim.x;

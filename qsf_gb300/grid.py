@@ -38,7 +38,7 @@ class Grid:
     def __init__(self, dim: int, n, dx, nCAP: int = 0, potential: int = POT_EBERLY, Ncharge: float = 1.0,
                  Echarge: float = -1.0, Nsoft: float = 1.0, Esoft: float = 1.0, gauge: int = 0,
                  n_fields: int = 0, p_axis_swap: Optional[bool] = None, border_nodes=(25, 14, 10, 40),
-                 stream: Optional[int] = None):
+                 stream: Optional[int] = None, free_axes: int = 0, multi_region: bool = False):
         n = [int(n)] * dim if np.isscalar(n) else [int(v) for v in n]
         dx = [float(dx)] * dim if np.isscalar(dx) else [float(v) for v in dx]
         d = GridDesc()
@@ -51,7 +51,12 @@ class Grid:
         d.Ncharge, d.Echarge, d.Nsoft, d.Esoft = Ncharge, Echarge, Nsoft, Esoft
         d.gauge = gauge
         d.n_fields = n_fields
-        d.p_axis_swap = int(dim >= 2 if p_axis_swap is None else p_axis_swap)
+        if p_axis_swap is None:  # the transposed P layout: main (or single) region only
+            p_axis_swap = dim >= 2 and free_axes == 0
+        d.p_axis_swap = int(p_axis_swap)
+        d.free_axes = int(free_axes)
+        d.multi_region = int(bool(multi_region))
+        self.free_axes = int(free_axes)
         for k in range(4):
             d.border_nodes[k] = int(border_nodes[k])
         self.desc = d
@@ -128,6 +133,10 @@ class Grid:
     def mask_region(self, bounded: Sequence[int]) -> None:
         b = (ctypes.c_int * 3)(*(list(bounded) + [1] * (3 - len(bounded))))
         check(lib().qsf_mask_region(self._h, b), "qsf_mask_region")
+
+    def region_transfer(self, src: "Grid", axis: int, group: int) -> None:
+        """psi += DFT_axis(masked margins of src along axis) (multigrid.h:454-657)."""
+        check(lib().qsf_region_transfer(self._h, src._h, int(axis), int(group)), "qsf_region_transfer")
 
     def add_gaussian(self, at: float = 0.0, delta: float = 1.0) -> None:
         check(lib().qsf_add_gaussian(self._h, at, delta), "qsf_add_gaussian")
