@@ -330,6 +330,67 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128):
 
 
 # ------------------------------------------------------------------ GPU arm
+MG_EDGE, MG_NCAP = 1024, 102
+
+
+def _mg_oracle_rate(n: int, nsteps: int) -> float:
+    """Grid-pt-steps/s of the oracle's multi-region propagator (one core), n^2 regions."""
+    from oracle import oracle as O
+    pa = _pulse_args()
+    regs = O.region_axes(2)
+    cs = [O.Coupling(O.GAUGE_VELOCITY, [O.Field(3, [O.Pulse(**pa)])]) for _ in regs]
+    gs = [O.Grid(2, n, DX, nCAP=max(1, n // 10), Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT, Esoft=ESOFT,
+                 coupling=c) for c in cs]
+    gs[0].psi[...] = _gauss_state(2, n, DX)
+    mp = O.MultiRegionPropagator(DT, gs, cs, ["norm", "epot"])
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        mp._step_all()
+        mp.props[0].compute_each()
+        mp.post_compute()
+    return len(regs) * n * n * nsteps / (time.perf_counter() - t0)
+
+
+def run_multigrid(steps, warmup, cpu=True):
+    """Multi-region 2D grid (regions NO, X, Y, XY of 1024^2 each): one step = the Strang
+    step of every region, norm and E_pot of the main region, the region transfer and the
+    region masks.  Timed on the host around `steps` steps with every region's stream
+    synchronised at both ends (the regions run on four streams)."""
+    import qsf_gb300 as Q
+    from qsf_gb300.multigrid import MultiGrid, MultiRegionPropagator
+    pa = _pulse_args()
+    mg = MultiGrid(2, MG_EDGE, DX, MG_NCAP, potential=Q.POT_EBERLY, Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT,
+                   Esoft=ESOFT, gauge=Q.GAUGE_VELOCITY, n_fields=1)
+    mg.main.upload(_gauss_state(2, MG_EDGE, DX))
+    prop = MultiRegionPropagator(DT, mg, Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(3, [Q.Pulse(**pa)])]),
+                                 ["norm", "epot"])
+
+    def one():
+        prop._make_step()
+        prop._compute_each()
+        mg.post_compute()
+
+    for _ in range(warmup):
+        one()
+    mg.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    mg.synchronize()
+    wall = time.perf_counter() - t0
+    pts = 4.0 * MG_EDGE * MG_EDGE * steps
+    out = {"value": pts / wall, "unit": UNIT, "ms_per_step": wall * 1e3 / steps, "steps": steps,
+           "config": f"2D multi-region grid, 4 regions x {MG_EDGE}^2, nCAP {MG_NCAP}, VG sin^2 pulse, "
+                     f"norm + E_pot of the main region every step, transfer + masks every step"}
+    if cpu:
+        n_cpu = 256
+        out["cpu_baseline"] = {"value": _mg_oracle_rate(n_cpu, 4), "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"4 steps of the same multi-region propagator on 4 x {n_cpu}^2 regions "
+                                         f"(oracle, one core)"}
+    mg.close()
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = _dist()
     import torch
@@ -405,6 +466,7 @@ def run_gpu(args):
 
     batched = run_batched(steps=20, warmup=3)
     served = run_served(rate=100.0, duration_s=3.0)
+    multigrid = run_multigrid(steps=20, warmup=3, cpu=rank == 0)
 
     if rank == 0:
         cpu = cpu_baseline(all_cores=False)
@@ -431,6 +493,7 @@ def run_gpu(args):
             "clocks": clk,
             "batched": batched,
             "served": served,
+            "multigrid": multigrid,
             "batched_vs_plain": batched["value"] / value * ws,
         }
         print(json.dumps(line))
@@ -471,7 +534,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served", "multigrid"])
     ap.add_argument("--rates", default="10,30,100,300,1000")
     ap.add_argument("--duration", type=float, default=5.0)
     args = ap.parse_args()
@@ -486,6 +549,10 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         for r in [float(v) for v in args.rates.split(",")]:
             print(json.dumps({"metric": METRIC, **run_served(r, args.duration)}), flush=True)
+    elif args.workload == "multigrid":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"metric": METRIC, **run_multigrid(args.steps, args.warmup)}), flush=True)
     else:
         run_gpu(args)
 
