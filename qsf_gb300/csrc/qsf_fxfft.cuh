@@ -231,15 +231,16 @@ __device__ __forceinline__ int block_max_int(int v, int* red) {
 }
 
 // One in-place forward Stockham pass in fixed point (an inverse transform is the
-// forward one between two conjugations).  Inputs are scaled by 2^shift_in on load;
-// returns, valid in every thread after the call, the bit length of the block's
-// largest output component (see fmag).
-template <int R, int MAXB, int N, int NS>
+// forward one between two conjugations) with stride NS (the product of the earlier
+// radices; a runtime value, so that passes of equal radix share one code body).
+// Inputs are scaled by 2^shift_in on load; returns, valid in every thread after the
+// call, the bit length of the block's largest output component (see fmag).
+template <int R, int MAXB, int N>
 __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const LineSet& L,
                                            const longlong2* __restrict__ tw, int tid, int nth, int shift_in, int* red,
-                                           int parity) {
+                                           int parity, int NS) {
   constexpr int nr = N / R;
-  constexpr int twstep = N / (NS * R);
+  const int twstep = N / (NS * R);
   const int total = nr * L.nlines;
   // the load-time scaling 2^shift_in without branches: (x << sl + half) >> sr
   const int sl = shift_in > 0 ? shift_in : 0, sr = shift_in < 0 ? min(-shift_in, 63) : 0;
@@ -266,7 +267,7 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
         v[b][q] = make_longlong2(((i64)((u64)x.x << sl) + half) >> sr, ((i64)((u64)x.y << sl) + half) >> sr);
       }
       const int jm = j % NS;
-      if constexpr (NS > 1) {
+      if (NS > 1) {
 #pragma unroll
         for (int q = 1; q < R; ++q) v[b][q] = fmul62(v[b][q], tw[jm * q * twstep]);
       }
@@ -305,20 +306,57 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
 // the data have block exponent `scale` (value = int * 2^-scale) and, after the shift
 // 2^shift_in applied on load, fit the first pass's guard; on return `scale` is the
 // exponent of the output and its largest component has bit length `bits`.
-// Requires nlines * N <= 16 * nth.
-template <int N, int S = 0>
-__device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw, int tid,
-                                       int nth, int& scale, int& bits, int* red, int shift_in = 0) {
+// Requires nlines * N <= 16 * nth.  The passes run as a loop over the stages with one
+// inlined pass body per distinct radix of N (instruction-cache footprint).
+// radix_at(N, s) for a runtime stage index, from compile-time stage counts
+template <int N>
+__device__ __forceinline__ int radix_rt(int s) {
+  constexpr int a = count_factor(N, 2), q = a / QSF_RADIX_LOG2, rem = a % QSF_RADIX_LOG2;
+  constexpr int c3 = count_factor(N, 3);
+  if (s < q) return 1 << QSF_RADIX_LOG2;
+  int k = s - q;
+  if (rem) {
+    if (k == 0) return 1 << rem;
+    k -= 1;
+  }
+  return k < c3 ? 3 : 5;
+}
+// the compile-time stages S.. of fft_fx
+template <int N, int S>
+__device__ __forceinline__ void fft_fx_tail(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw,
+                                            int tid, int nth, int& scale, int& bits, int* red, int shift_in) {
   if constexpr (S < nstages(N)) {
     constexpr int R = radix_at(N, S);
-    bits = fx_stockham<R, maxb_for(R), N, ns_at(N, S)>(buf, L, tw, tid, nth, shift_in, red, S & 1);
+    bits = fx_stockham<R, maxb_for(R), N>(buf, L, tw, tid, nth, shift_in, red, S & 1, ns_at(N, S));
     if constexpr (S + 1 < nstages(N)) {
       // renormalise for the next pass: largest component below 2^(62 - guard(next))
       const int target = 62 - fguard(radix_at(N, S + 1));
       const int sh = bits == 0 ? 0 : target - bits;
       scale += sh;
-      fft_fx<N, S + 1>(buf, L, tw, tid, nth, scale, bits, red, sh);
+      fft_fx_tail<N, S + 1>(buf, L, tw, tid, nth, scale, bits, red, sh);
     }
+  }
+}
+template <int N>
+__device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw, int tid,
+                                       int nth, int& scale, int& bits, int* red, int shift_in = 0) {
+  // the leading radix-16 passes share one code body (a loop); the rest are unrolled
+  constexpr int q = count_factor(N, 2) / QSF_RADIX_LOG2;
+  if constexpr (q >= 2 && QSF_RADIX_LOG2 == 4) {
+    int sh = shift_in, ns = 1;
+#pragma unroll 1
+    for (int s = 0; s < q; ++s) {
+      bits = fx_stockham<16, maxb_for(16), N>(buf, L, tw, tid, nth, sh, red, s & 1, ns);
+      ns *= 16;
+      if (s + 1 < nstages(N)) {
+        const int target = 62 - fguard(radix_rt<N>(s + 1));
+        sh = bits == 0 ? 0 : target - bits;
+        scale += sh;
+      }
+    }
+    fft_fx_tail<N, q>(buf, L, tw, tid, nth, scale, bits, red, sh);
+  } else {
+    fft_fx_tail<N, 0>(buf, L, tw, tid, nth, scale, bits, red, shift_in);
   }
 }
 
