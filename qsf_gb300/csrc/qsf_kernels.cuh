@@ -662,7 +662,7 @@ __device__ __forceinline__ void close_open_block(const GridDev& g, const StepDev
   Acc128 an{0ull, 0ll}, av{0ull, 0ll};
   const bool epot = (S.obs & 2u) != 0;
   u64 mag = 0;
-#pragma unroll 4
+#pragma unroll 1  // a large body: unrolling costs more in instruction fetch than it gains
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const long long p = base + e;
     longlong2 x = fconj(smx[e]);
