@@ -884,7 +884,7 @@ __device__ __forceinline__ int p_phase(const GridDev& g, const StepDev& S, longl
   const int cnt = rows * Ch;
   u64 mag = 0;
   TileWalk w(threadIdx.x, blockDim.x, Ch);
-#pragma unroll 4
+#pragma unroll 1
   for (int e = threadIdx.x; e < cnt; e += blockDim.x, w.next()) {
     const int i = w.i, c = w.c;
     longlong2 x = smx[i * ldc + c];
