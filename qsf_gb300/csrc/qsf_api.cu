@@ -844,6 +844,8 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->dG);
   fr(g->dS);
   fr(g->mg_slice);
+  fr(g->etab);
+  fr(g->eptab);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->own_stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -972,7 +974,27 @@ int qsf_region_transfer(qsf_grid* dst, const qsf_grid* src, int axis, int group)
 int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* c3) {
   if (!g || (mode != 1 && mode != 2) || (rep != 1 && rep != 2)) return fail(QSF_EINVAL, "bad argument");
   const double c0 = c3 ? c3[0] : 0.0, c1 = c3 ? c3[1] : 0.0, c2 = c3 ? c3[2] : 0.0;
-  k_evolve<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, mode, rep, delta, c0, c1, c2);
+  const GridDev& G = g->G;
+  if (rep == QSF_REP_X && !(G.gauge == QSF_GAUGE_LENGTH && G.n_fields)) {
+    // no X-space coupling: the factor per point depends on (mode, delta) only; it is
+    // evaluated once and reused while they stay the same
+    if (!g->etab || g->etab_mode != mode || g->etab_delta != delta) {
+      if (!g->etab)
+        if (int rc = dev_alloc(g->etab, (size_t)G.m)) return rc;
+      k_evolve_xtab<<<grid_blocks(G.m), 256, 0, g->stream>>>(G, mode, delta, g->etab);
+      g->etab_mode = mode;
+      g->etab_delta = delta;
+    }
+    k_apply_xtab<<<grid_blocks(G.m), 256, 0, g->stream>>>(G.psi, g->etab, G.m);
+  } else if (rep == QSF_REP_P) {
+    if (!g->eptab)
+      if (int rc = dev_alloc(g->eptab, (size_t)3 * g->nmax)) return rc;
+    k_evolve_ptab<<<(G.dim * g->nmax + 255) / 256, 256, 0, g->stream>>>(G, mode, delta, c0, c1, c2, g->nmax,
+                                                                        g->eptab);
+    k_apply_ptab<<<grid_blocks(G.m), 256, 0, g->stream>>>(G, g->eptab, g->nmax);
+  } else {
+    k_evolve<<<grid_blocks(G.m), 256, 0, g->stream>>>(G, mode, rep, delta, c0, c1, c2);
+  }
   QSF_CU(cudaGetLastError());
   return QSF_OK;
 }

@@ -114,5 +114,10 @@ struct qsf_grid {
   size_t ax_smem[3] = {0, 0, 0};
   // multi-region transfer: slice buffer (m points) and the event that orders streams
   double2* mg_slice = nullptr;
+  // member evolve: cached X-phase factors for (mode, delta) and per-axis P factors
+  double2* etab = nullptr;
+  int etab_mode = 0;
+  double etab_delta = 0.0;
+  double2* eptab = nullptr;
   cudaEvent_t mg_event = nullptr;
 };

@@ -1275,6 +1275,60 @@ __global__ void k_scale(double2* psi, long long m, const double* scale) {
 
 // ------------------------------------------------------------ granular members
 // evolve<M,R>(delta) with the reference's per-point formula (grid.h:394-418)
+// X-phase factor per point of evolve<M, X>(delta) without an X-space coupling term:
+// expOp(delta V) times the absorber (grid.h:394-418), as one complex factor
+__global__ void k_evolve_xtab(GridDev g, int mode, double delta, double2* __restrict__ tab) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
+    int idx[kMaxDim];
+    double c[kMaxDim];
+    unflatten(g, p, idx);
+    for (int d = 0; d < g.dim; ++d) c[d] = xpos(g.ax[d], idx[d]);
+    double2 f = expop(mode, delta * potential_at(g, c));
+    if (g.nCAP > 0 && !g.multi) f = cscale(f, absorb_at(g, delta, idx));
+    tab[p] = f;
+  }
+}
+// per-axis factors of evolve<M, P>(delta): expOp(delta (k^2 / 2 + A_d k)) for axis d
+// (the P Hamiltonian is a sum over axes, so its exponential is their product)
+__global__ void k_evolve_ptab(GridDev g, int mode, double delta, double c0, double c1, double c2, int nmax,
+                              double2* __restrict__ tab) {
+  double cv[3] = {c0, c1, c2};
+  if (g.p_swap && g.dim >= 2) {
+    cv[0] = c1;
+    cv[1] = c0;
+  }
+  const bool coupled = g.gauge == 0 && g.n_fields;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.dim * nmax; e += gridDim.x * blockDim.x) {
+    const int d = e / nmax, i = e % nmax;
+    if (i >= g.ax[d].n) continue;
+    const double k = kpos(g.ax[d], i);
+    tab[e] = expop(mode, delta * (0.5 * k * k + (coupled ? k * cv[d] : 0.0)));
+  }
+}
+// psi *= tab[p] (X) or psi *= prod_d tab[d][idx_d] (P)
+__global__ void k_apply_xtab(double2* __restrict__ psi, const double2* __restrict__ tab, long long m) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < m; p += stride) {
+    const double2 a = psi[p], f = tab[p];
+    psi[p] = make_double2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+  }
+}
+__global__ void k_apply_ptab(GridDev g, const double2* __restrict__ tab, int nmax) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
+    int idx[kMaxDim];
+    unflatten(g, p, idx);
+    double2 f = tab[idx[0]];
+    for (int d = 1; d < g.dim; ++d) {
+      const double2 t = tab[d * nmax + idx[d]];
+      f = make_double2(f.x * t.x - f.y * t.y, f.x * t.y + f.y * t.x);
+    }
+    const double2 a = g.psi[p];
+    g.psi[p] = make_double2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+  }
+}
+
 __global__ void k_evolve(GridDev g, int mode, int rep, double delta, double c0, double c1, double c2) {
   double cv[3] = {c0, c1, c2};
   if (rep == 2 && g.p_swap && g.dim >= 2) {
