@@ -42,6 +42,7 @@ std::vector<KernelSet>& kernel_table();
 
 // kernel launch geometry
 constexpr int kMaxLine1D = 16384;       // 1D line in shared memory (one CTA up to 8192, a cluster pair above)
+constexpr int kMaxFluxBlocks = 512;  // blocks of the flux-term sums (256 terms each)
 constexpr int kMaxTile = 4096;          // points per block in row / axis passes
 
 }  // namespace
@@ -271,7 +272,8 @@ int ensure_flux(qsf_grid* g, int nb, const int* types, int64_t box) {
   g->nsnap = (int)need.size();
   g->nfpts = (int)fps.size();
   g->nfterms = (int)fts.size();
-  g->nfblk = (int)std::min<long long>(64, std::max<long long>(1, (g->nfterms + 2047) / 2048));
+  // one thread per flux term (each is a chain of dependent loads: latency, not bandwidth)
+  g->nfblk = (int)std::min<long long>(kMaxFluxBlocks, std::max<long long>(1, (g->nfterms + 255) / 256));
   g->fl_borders = want;
   g->fl_box = box;
   g->fl_ready = true;
@@ -799,12 +801,12 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
       (rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)3 * D * g->nmax)) ||
       (rc = dev_alloc(g->partials, (size_t)5 * g->pmax)) || (rc = dev_alloc(g->ctl, 8)) ||
       (rc = dev_alloc(g->energy, 2)) || (rc = dev_alloc(g->scale, 2)) ||
-      (rc = dev_alloc(g->fpartials, (size_t)64 * kMaxFluxBorders)) || (rc = dev_alloc(g->dG, 1)) ||
+      (rc = dev_alloc(g->fpartials, (size_t)kMaxFluxBlocks * kMaxFluxBorders)) || (rc = dev_alloc(g->dG, 1)) ||
       (rc = dev_alloc(g->dS, 1))) {
     qsf_grid_destroy(g);
     return rc;
   }
-  g->fpmax = (size_t)64 * kMaxFluxBorders;
+  g->fpmax = (size_t)kMaxFluxBlocks * kMaxFluxBorders;
   cudaMemcpyAsync(g->dG, &g->G, sizeof(GridDev), cudaMemcpyHostToDevice, g->stream);
   cudaMemsetAsync(g->partials, 0, sizeof(double) * 5 * g->pmax, g->stream);
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) {

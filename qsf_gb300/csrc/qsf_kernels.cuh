@@ -1230,7 +1230,13 @@ __global__ void __launch_bounds__(256) k_finalize(const GridDev* __restrict__ Gs
     for (int d = 0; d < g.dim - 1; ++d)
       for (int i = threadIdx.x; i < S.naxblk[d]; i += blockDim.x) acc[2 + d] += S.partials[(2 + d) * S.pmax + i];
   }
-  block_sum<5>(acc, red);
+  __shared__ double fsum[kMaxFluxBorders];
+  if (threadIdx.x < nb) {  // per border, the blocks' partials in block order
+    double v = 0.0;
+    for (int k = 0; k < (int)gridDim.x; ++k) v += S.fpartials[k * kMaxFluxBorders + threadIdx.x];
+    fsum[threadIdx.x] = v;
+  }
+  block_sum<5>(acc, red);  // its barriers also publish fsum
   if (threadIdx.x == 0) {
     const double norm = acc[0] * g.dV;
     const double epot = acc[1] * g.dV;
@@ -1244,11 +1250,7 @@ __global__ void __launch_bounds__(256) k_finalize(const GridDev* __restrict__ Gs
     row[0] = norm;
     row[1] = epot;
     row[2] = ekin;
-    for (int b = 0; b < nb; ++b) {
-      double v = 0.0;
-      for (int k = 0; k < (int)gridDim.x; ++k) v += S.fpartials[k * kMaxFluxBorders + b];
-      row[3 + b] = v * g.dV / g.ax[0].dx;
-    }
+    for (int b = 0; b < nb; ++b) row[3 + b] = fsum[b] * g.dV / g.ax[0].dx;
     if (!(norm > 0.0) || isnan(epot) || isnan(ekin)) S.ctl[4] = 1;
     if (S.normalize && norm > 0.0) *S.scale = sqrt(1.0 / norm);
     if (S.mode == 1 && S.state_accuracy > 0.0) {
