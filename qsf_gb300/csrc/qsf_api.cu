@@ -561,6 +561,11 @@ struct qsf_batch {
   GridDev* dG_all = nullptr;
   StepDev* dS_all = nullptr;
   size_t desc_cap = 0, dS_cap = 0;
+  // one stream per group while the step graph is captured, so that the groups become
+  // parallel branches of the graph (grow-only)
+  std::vector<cudaStream_t> gstreams;
+  std::vector<cudaEvent_t> gjoin;
+  cudaEvent_t gfork = nullptr;
 };
 
 namespace {
@@ -612,13 +617,28 @@ int rebuild_batch(qsf_batch* b) {
   }
   QSF_CU(cudaStreamSynchronize(b->stream));
   if (!b->groups.empty()) {
+    if (!b->gfork) QSF_CU(cudaEventCreateWithFlags(&b->gfork, cudaEventDisableTiming));
+    while (b->gstreams.size() < b->groups.size()) {
+      cudaStream_t s2 = nullptr;
+      cudaEvent_t e2 = nullptr;
+      QSF_CU(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+      QSF_CU(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+      b->gstreams.push_back(s2);
+      b->gjoin.push_back(e2);
+    }
     int rc = capture_graph(
         b->stream,
         [&]() {
-          for (const BatchGroup& gr : b->groups) {
+          // fork: every group on its own stream, joined back before the graph ends
+          QSF_CU(cudaEventRecord(b->gfork, b->stream));
+          for (size_t i = 0; i < b->groups.size(); ++i) {
+            const BatchGroup& gr = b->groups[i];
+            QSF_CU(cudaStreamWaitEvent(b->gstreams[i], b->gfork, 0));
             const int r = launch_group(*gr.ks, gr.q, gr.dG, gr.dS, (int)gr.slots.size(), gr.ekin, gr.nfblk,
-                                       b->stream, nullptr);
+                                       b->gstreams[i], nullptr);
             if (r) return r;
+            QSF_CU(cudaEventRecord(b->gjoin[i], b->gstreams[i]));
+            QSF_CU(cudaStreamWaitEvent(b->stream, b->gjoin[i], 0));
           }
           return QSF_OK;
         },
@@ -1122,6 +1142,9 @@ int qsf_batch_destroy(qsf_batch* b) {
   if (b->dG_all) cudaFree(b->dG_all);
   if (b->dS_all) cudaFree(b->dS_all);
   if (b->ctl_host) cudaFreeHost(b->ctl_host);
+  for (cudaStream_t s2 : b->gstreams) cudaStreamDestroy(s2);
+  for (cudaEvent_t e2 : b->gjoin) cudaEventDestroy(e2);
+  if (b->gfork) cudaEventDestroy(b->gfork);
   if (b->own_stream) cudaStreamDestroy(b->stream);
   delete b;
   return QSF_OK;
