@@ -659,6 +659,22 @@ __device__ __forceinline__ void close_open_block(const GridDev& g, const StepDev
     }
     __syncthreads();
   }
+  // length gauge in 3D: the x.E factors of the first two axes are constant along a row;
+  // their product per row and half is formed once
+  constexpr int kRowPre = 64;
+  __shared__ longlong2 rowpre[2][kRowPre];
+  const bool hoist = g.gauge == 1 && g.dim == 3 && Lh <= kRowPre;
+  const longlong2* t1 = S.xdyn + (size_t)1 * 3 * S.nmax;  // close half, axes 0..2
+  const longlong2* t2 = S.xdyn + (size_t)2 * 3 * S.nmax;  // next open half
+  if (hoist) {
+    for (int t = threadIdx.x; t < 2 * Lh; t += blockDim.x) {
+      const int h = t / Lh, rl = t % Lh;
+      const long long r = row0 + rl;
+      const longlong2* tab = h ? t2 : t1;
+      rowpre[h][rl] = fmul62(tab[S.nmax + (int)(r % N)], tab[(int)(r / N)]);
+    }
+    __syncthreads();
+  }
   Acc128 an{0ull, 0ll}, av{0ull, 0ll};
   const bool epot = (S.obs & 2u) != 0;
   u64 mag = 0;
@@ -667,8 +683,16 @@ __device__ __forceinline__ void close_open_block(const GridDev& g, const StepDev
     const long long p = base + e;
     longlong2 x = fconj(smx[e]);
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    const longlong2 f1 = xfactor<N>(g, S, p, row0 + e / N, e % N, 1);
-    const longlong2 f2 = g.gauge == 1 ? xfactor<N>(g, S, p, row0 + e / N, e % N, 2) : f1;
+    longlong2 f1, f2;
+    if (hoist) {
+      const int rl = e / N, j = e % N;
+      const longlong2 xsv = S.xs[p];
+      f1 = fmul62(xsv, fmul62(t1[2 * S.nmax + j], rowpre[0][rl]));
+      f2 = fmul62(xsv, fmul62(t2[2 * S.nmax + j], rowpre[1][rl]));
+    } else {
+      f1 = xfactor<N>(g, S, p, row0 + e / N, e % N, 1);
+      f2 = g.gauge == 1 ? xfactor<N>(g, S, p, row0 + e / N, e % N, 2) : f1;
+    }
     x = apply_f(x, f1, real_f);
     acc_point(an, av, x, q, S.Vx, p, epot);
     if (pre2) x = make_longlong2(fshift(x.x, pre2), fshift(x.y, pre2));
