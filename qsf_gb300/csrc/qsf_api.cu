@@ -379,20 +379,20 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
                                                (size_t)(q.n / K.line_ctas) * sizeof(double2), st>>>(dG, dS)));
   } else {
     const dim3 gr(q.nrowblk, count);
-    QSF_TIMED(QSF_K_ROW_OPEN, (K.row_open<<<gr, kRowThreads, q.row_smem, st>>>(dG, dS, q.row_L)));
+    QSF_TIMED(QSF_K_ROW_OPEN, (K.row_open<<<gr, K.row_threads, q.row_smem, st>>>(dG, dS, q.row_L)));
     if (D == 3)
       QSF_TIMED(QSF_K_AXIS_FWD,
-                (K.axis_fwd<<<dim3(q.ax_blocks[1], count), kRowThreads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
+                (K.axis_fwd<<<dim3(q.ax_blocks[1], count), K.row_threads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
     QSF_TIMED(QSF_K_AXIS_FPI,
-              (K.axis_fpi<<<dim3(q.ax_blocks[0], count), kRowThreads, q.ax_smem[0], st>>>(dG, dS, 0, q.ax_C[0])));
+              (K.axis_fpi<<<dim3(q.ax_blocks[0], count), K.row_threads, q.ax_smem[0], st>>>(dG, dS, 0, q.ax_C[0])));
     if (D == 3)
       QSF_TIMED(QSF_K_AXIS_INV,
-                (K.axis_inv<<<dim3(q.ax_blocks[1], count), kRowThreads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
-    QSF_TIMED(QSF_K_ROW_CLOSE, (K.row_close<<<gr, kRowThreads, q.row_smem, st>>>(dG, dS, q.row_L)));
+                (K.axis_inv<<<dim3(q.ax_blocks[1], count), K.row_threads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
+    QSF_TIMED(QSF_K_ROW_CLOSE, (K.row_close<<<gr, K.row_threads, q.row_smem, st>>>(dG, dS, q.row_L)));
     if (ekin)
       for (int ax = 0; ax < D - 1; ++ax)
         QSF_TIMED(QSF_K_AXIS_EKIN,
-                  (K.axis_ekin<<<dim3(q.ax_blocks[ax], count), kRowThreads, q.ax_smem[ax], st>>>(dG, dS, ax, q.ax_C[ax])));
+                  (K.axis_ekin<<<dim3(q.ax_blocks[ax], count), K.row_threads, q.ax_smem[ax], st>>>(dG, dS, ax, q.ax_C[ax])));
   }
   QSF_TIMED(QSF_K_FINALIZE, (k_finalize<<<dim3(nfblk, count), 256, 0, st>>>(dG, dS)));
 #undef QSF_TIMED
@@ -928,8 +928,8 @@ static void axis_fft(qsf_grid* g, const GridDev& G, int ax, bool fwd, double sc)
       if (fwd) K.row_fft_f<<<blocks, kLineThreads, smem, st>>>(G, L, sc);
       else K.row_fft_b<<<blocks, kLineThreads, smem, st>>>(G, L, sc);
     } else {
-      if (fwd) K.axis_fft_f<<<g->ax_blocks[ax], kRowThreads, g->ax_smem[ax], st>>>(G, ax, g->ax_C[ax], sc);
-      else K.axis_fft_b<<<g->ax_blocks[ax], kRowThreads, g->ax_smem[ax], st>>>(G, ax, g->ax_C[ax], sc);
+      if (fwd) K.axis_fft_f<<<g->ax_blocks[ax], K.row_threads, g->ax_smem[ax], st>>>(G, ax, g->ax_C[ax], sc);
+      else K.axis_fft_b<<<g->ax_blocks[ax], K.row_threads, g->ax_smem[ax], st>>>(G, ax, g->ax_C[ax], sc);
     }
   }
 }

@@ -190,14 +190,16 @@ __host__ __device__ constexpr bool is_smooth(int n) {
 #ifndef QSF_RADIX_LOG2
 #define QSF_RADIX_LOG2 4
 #endif
-__host__ __device__ constexpr int nstages(int n) {
+// Stage plan of an n-point transform: passes of radix 2^l2 (the main radix), one pass
+// of the remaining power of two, then radix-3 and radix-5 passes.
+__host__ __device__ constexpr int nstages(int n, int l2 = QSF_RADIX_LOG2) {
   const int a = count_factor(n, 2);
-  return a / QSF_RADIX_LOG2 + (a % QSF_RADIX_LOG2 ? 1 : 0) + count_factor(n, 3) + count_factor(n, 5);
+  return a / l2 + (a % l2 ? 1 : 0) + count_factor(n, 3) + count_factor(n, 5);
 }
-__host__ __device__ constexpr int radix_at(int n, int i) {
+__host__ __device__ constexpr int radix_at(int n, int i, int l2 = QSF_RADIX_LOG2) {
   const int a = count_factor(n, 2);
-  const int q = a / QSF_RADIX_LOG2, r = a % QSF_RADIX_LOG2;
-  if (i < q) return 1 << QSF_RADIX_LOG2;
+  const int q = a / l2, r = a % l2;
+  if (i < q) return 1 << l2;
   int k = i - q;
   if (r) {
     if (k == 0) return 1 << r;
@@ -205,9 +207,9 @@ __host__ __device__ constexpr int radix_at(int n, int i) {
   }
   return k < count_factor(n, 3) ? 3 : 5;
 }
-__host__ __device__ constexpr int ns_at(int n, int i) {
+__host__ __device__ constexpr int ns_at(int n, int i, int l2 = QSF_RADIX_LOG2) {
   int p = 1;
-  for (int j = 0; j < i; ++j) p *= radix_at(n, j);
+  for (int j = 0; j < i; ++j) p *= radix_at(n, j, l2);
   return p;
 }
 // butterflies per thread for radix R when lines * N <= 16 * nth

@@ -308,12 +308,12 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
 // exponent of the output and its largest component has bit length `bits`.
 // Requires nlines * N <= 16 * nth.  The passes run as a loop over the stages with one
 // inlined pass body per distinct radix of N (instruction-cache footprint).
-// radix_at(N, s) for a runtime stage index, from compile-time stage counts
-template <int N>
+// radix_at(N, s, L2) for a runtime stage index, from compile-time stage counts
+template <int N, int L2>
 __device__ __forceinline__ int radix_rt(int s) {
-  constexpr int a = count_factor(N, 2), q = a / QSF_RADIX_LOG2, rem = a % QSF_RADIX_LOG2;
+  constexpr int a = count_factor(N, 2), q = a / L2, rem = a % L2;
   constexpr int c3 = count_factor(N, 3);
-  if (s < q) return 1 << QSF_RADIX_LOG2;
+  if (s < q) return 1 << L2;
   int k = s - q;
   if (rem) {
     if (k == 0) return 1 << rem;
@@ -321,42 +321,54 @@ __device__ __forceinline__ int radix_rt(int s) {
   }
   return k < c3 ? 3 : 5;
 }
+// butterflies per thread of radix R when every thread holds PPT points of the tile
+__host__ __device__ constexpr int maxb_ppt(int r, int ppt) { return (ppt + r - 1) / r; }
+
+// main radix of the plan for PPT points per thread: radix 16 needs 16 per thread
+__host__ __device__ constexpr int plan_l2(int ppt) { return ppt >= 16 ? QSF_RADIX_LOG2 : 3; }
+
 // the compile-time stages S.. of fft_fx
-template <int N, int S>
+template <int N, int S, int PPT>
 __device__ __forceinline__ void fft_fx_tail(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw,
                                             int tid, int nth, int& scale, int& bits, int* red, int shift_in) {
-  if constexpr (S < nstages(N)) {
-    constexpr int R = radix_at(N, S);
-    bits = fx_stockham<R, maxb_for(R), N>(buf, L, tw, tid, nth, shift_in, red, S & 1, ns_at(N, S));
-    if constexpr (S + 1 < nstages(N)) {
+  constexpr int L2 = plan_l2(PPT);
+  if constexpr (S < nstages(N, L2)) {
+    constexpr int R = radix_at(N, S, L2);
+    bits = fx_stockham<R, maxb_ppt(R, PPT), N>(buf, L, tw, tid, nth, shift_in, red, S & 1, ns_at(N, S, L2));
+    if constexpr (S + 1 < nstages(N, L2)) {
       // renormalise for the next pass: largest component below 2^(62 - guard(next))
-      const int target = 62 - fguard(radix_at(N, S + 1));
+      const int target = 62 - fguard(radix_at(N, S + 1, L2));
       const int sh = bits == 0 ? 0 : target - bits;
       scale += sh;
-      fft_fx_tail<N, S + 1>(buf, L, tw, tid, nth, scale, bits, red, sh);
+      fft_fx_tail<N, S + 1, PPT>(buf, L, tw, tid, nth, scale, bits, red, sh);
     }
   }
 }
-template <int N>
+// PPT: points of the tile per thread (tile points / threads), which sets the butterflies
+// each thread carries per pass.
+template <int N, int PPT = 16>
 __device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw, int tid,
                                        int nth, int& scale, int& bits, int* red, int shift_in = 0) {
-  // the leading radix-16 passes share one code body (a loop); the rest are unrolled
-  constexpr int q = count_factor(N, 2) / QSF_RADIX_LOG2;
-  if constexpr (q >= 2 && QSF_RADIX_LOG2 == 4) {
+  // the leading passes of the plan's main radix share one code body (a loop); the rest
+  // are unrolled
+  constexpr int L2 = plan_l2(PPT);
+  constexpr int R0 = 1 << L2;
+  constexpr int q = count_factor(N, 2) / L2;
+  if constexpr (q >= 2) {
     int sh = shift_in, ns = 1;
 #pragma unroll 1
     for (int s = 0; s < q; ++s) {
-      bits = fx_stockham<16, maxb_for(16), N>(buf, L, tw, tid, nth, sh, red, s & 1, ns);
-      ns *= 16;
-      if (s + 1 < nstages(N)) {
-        const int target = 62 - fguard(radix_rt<N>(s + 1));
+      bits = fx_stockham<R0, maxb_ppt(R0, PPT), N>(buf, L, tw, tid, nth, sh, red, s & 1, ns);
+      ns *= R0;
+      if (s + 1 < nstages(N, L2)) {
+        const int target = 62 - fguard(radix_rt<N, L2>(s + 1));
         sh = bits == 0 ? 0 : target - bits;
         scale += sh;
       }
     }
-    fft_fx_tail<N, q>(buf, L, tw, tid, nth, scale, bits, red, sh);
+    fft_fx_tail<N, q, PPT>(buf, L, tw, tid, nth, scale, bits, red, sh);
   } else {
-    fft_fx_tail<N, 0>(buf, L, tw, tid, nth, scale, bits, red, shift_in);
+    fft_fx_tail<N, 0, PPT>(buf, L, tw, tid, nth, scale, bits, red, shift_in);
   }
 }
 

@@ -38,7 +38,12 @@
 namespace qsf {
 
 constexpr int kMaxDim = 3;
-constexpr int kRowThreads = 256;
+// Threads per block of the row / axis passes (tiles of 4096 points): 512 threads with
+// radix-8 plans (8 points per thread, twice the resident warps) for line lengths whose
+// radix-16 plan ends in a poor tail (512 = 16 16 2, 2048 = 16 16 8), 256 threads with
+// radix-16 plans otherwise (measured per size).
+__host__ __device__ constexpr int row_threads(int n) { return (n == 512 || n == 2048) ? 512 : 256; }
+__host__ __device__ constexpr int row_ppt(int n) { return 4096 / row_threads(n); }
 constexpr int kLineThreads = 512;
 constexpr int kMaxFluxBorders = 16;
 // resident blocks per SM the FFT kernels are compiled for (caps registers per thread)
@@ -709,12 +714,12 @@ __device__ __forceinline__ void close_open_block(const GridDev& g, const StepDev
 }
 
 // E_kin part of the last axis: forward transform of psi_n (in smx) and sum k^2 |.|^2
-template <int N>
+template <int N, int PPT>
 __device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, const LineSet& ls, int cnt, int scale,
                                             int bits, int* red) {
   const int sh = first_pass_shift<N>(bits);
   int sc = scale + sh, b = 0;
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, sc, b, red, sh);
+  fft_fx<N, PPT>(smx, ls, a.twx, threadIdx.x, blockDim.x, sc, b, red, sh);
   double ek = 0.0;
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const double kk = kpos(a, e % N);
@@ -729,7 +734,7 @@ __device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, co
 // Rows of the last axis: L rows of N points per block, contiguous in memory.
 // Open: psi (double) . [Normalize] . X half . forward FFT -> fixed point (pass 0).
 template <int N>
-__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_open(const GridDev* __restrict__ Gs,
+__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_open(const GridDev* __restrict__ Gs,
                                                           const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -747,7 +752,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_open(co
   const int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_fx<N>(smx, ls, g.ax[g.dim - 1].twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, g.ax[g.dim - 1].twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
 #pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
@@ -812,7 +817,7 @@ __device__ __forceinline__ void build_dtab(const StepDev& S, int in_pass, int* d
 // on into the next sub-step: its opening X half and the forward transform of the last
 // axis, leaving pass 0 of that sub-step in fixed point.
 template <int N>
-__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(const GridDev* __restrict__ Gs,
+__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_close(const GridDev* __restrict__ Gs,
                                                            const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -843,7 +848,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
   const bool fuse_x = !last && !(S.obs & 4u);
   if (fuse_x) {
@@ -858,7 +863,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
         S.snap[e] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
       }
     }
-    dacc[2] = (S.obs & 4u) ? ekin_rows<N>(a, smx, ls, cnt, scale, bits, red) : 0.0;
+    dacc[2] = (S.obs & 4u) ? ekin_rows<N, row_ppt(N)>(a, smx, ls, cnt, scale, bits, red) : 0.0;
   }
   const double e_n = dacc[3], e_v = dacc[4];
   block_sum<3>(dacc, dred);  // its barriers also end the snapshot reads of smx
@@ -888,7 +893,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_row_close(c
   }
   sh = first_pass_shift<N>(bits);
   scale += sh;
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
 #pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
@@ -932,7 +937,7 @@ __device__ __forceinline__ int p_phase(const GridDev& g, const StepDev& S, longl
 //   3 forward of psi_n (double) + E_kin partial
 // Inverse transforms run as forward ones on conjugated data.
 template <int MODE, int N>
-__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
+__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
                                                       int ax, int C) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -969,7 +974,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis(const 
       smx[i * C + c] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
     }
     __syncthreads();
-    fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+    fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
     double acc = 0.0;
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int i = e / Ch, c = e % Ch;
@@ -1004,12 +1009,12 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis(const 
   }
   int sh = first_pass_shift<N>(bits);
   scale += sh;
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   if (MODE == 2) {
     scale += p_phase(g, S, smx, ax, N, Ch, C, multi_col ? pcol : nullptr, red, bits);
     sh = first_pass_shift<N>(bits);
     scale += sh;
-    fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+    fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   }
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
   const bool conj_out = MODE != 0;
@@ -1055,7 +1060,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
     const int e1 = S.row_ptr[1];
     for (int e = threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = g.psi[S.snap_idx[e]];
   }
-  dacc[2] = (S.obs & 4u) ? ekin_rows<N>(a, smx, ls, N, scale, bits, red) : 0.0;
+  dacc[2] = (S.obs & 4u) ? ekin_rows<N, 16>(a, smx, ls, N, scale, bits, red) : 0.0;
   const double e_n = dacc[3], e_v = dacc[4];
   block_sum<3>(dacc, dred);
   if (threadIdx.x == 0) {
@@ -1107,7 +1112,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
 }
 
 template <int N, bool FWD>
-__global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
+__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
   const AxisDev& a = g.ax[ax];
@@ -1137,7 +1142,7 @@ __global__ void __launch_bounds__(kRowThreads, QSF_FFT_MIN_BLOCKS) k_axis_fft(Gr
   __syncthreads();
   const LineSet ls{Ch, 1, C, true};
   int bits = 0;
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
     const longlong2 x = FWD ? smx[i * C + c] : fconj(smx[i * C + c]);
@@ -1566,6 +1571,7 @@ struct KernelSet {
   void (*axis_fft_f)(GridDev, int, int, double);
   void (*axis_fft_b)(GridDev, int, int, double);
   int line_ctas;  // CTAs holding one 1D line (2: a cluster pair, lines above 8192 points)
+  int row_threads;  // threads per block of the row / axis passes
 };
 
 // kernel table of the supported sizes (qsf_sizes_*.cu); nullptr when n is not built
@@ -1584,6 +1590,7 @@ KernelSet make_kernel_set() {
   KernelSet k{};
   k.n = N;
   k.line_ctas = 1;
+  k.row_threads = row_threads(N);
   if constexpr (N > 8192) {
     k.line_ctas = 2;
     k.line_step = k_line_step_cl<N>;

@@ -158,3 +158,38 @@ def test_bad_sizes_are_rejected(Q):
         Q.Grid(2, [64, 32], 0.1)
     with pytest.raises(Q.QsfError):
         Q.Grid(1, 16384 * 2, 0.1)
+
+
+@pytest.mark.parametrize("n", [512, 1024, 2048])
+def test_fused_2d_steps_match_oracle(Q, n):
+    """Fused multi-step calls at the large 2D edges (512 and 2048 take the 512-thread,
+    radix-8 row / axis kernels, 1024 the 256-thread radix-16 ones) against the oracle:
+    velocity-gauge field, absorber, norm, E_pot and the ZOA_FLUX_2D fluxes every step."""
+    from oracle import oracle as O
+    from qsf_gb300.propagator import coupling_schedule
+    steps, dx, dt, ncap = 3, 0.3, 0.05, n // 10
+    rng = np.random.default_rng(n)
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    env = np.exp(-(x[:, None] ** 2 + x[None, :] ** 2) / (2 * (0.35 * n * dx) ** 2))
+    psi0 = env * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    pulse = dict(field=0.12, omega=0.3, ncycles=2)
+    O.set_border_nodes(25, 14, 10, 40)
+    oc = O.Coupling(O.GAUGE_VELOCITY, [O.Field(3, [O.Pulse(**pulse)])])
+    og = O.Grid(2, n, dx, nCAP=ncap, pot=O.POT_EBERLY, Ncharge=2.0, coupling=oc)
+    og.psi[...] = psi0
+    prop = O.Propagator(O.MODE_RE, dt, 0, og, ["norm", "epot", ("flux", O.ZOA_FLUX_2D, 0)])
+    orows = []
+    for _ in range(steps):
+        prop.make_step()
+        prop.compute_each()
+        r = prop.rows[-1]
+        orows.append([r["norm"], r["epot"]] + list(r["flux"]))
+    g = Q.Grid(2, n, dx, nCAP=ncap, potential=Q.POT_EBERLY, Ncharge=2.0, gauge=Q.GAUGE_VELOCITY, n_fields=1)
+    g.upload(psi0)
+    c = Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(3, [Q.Pulse(**pulse)])])
+    rows, _ = coupling_schedule(c, dt, steps)
+    out, done = g.step(Q.MODE_RE, dt, steps, rows, obs=Q.OBS_NORM | Q.OBS_EPOT, borders=Q.ZOA_FLUX_2D)
+    assert done == steps
+    got = np.concatenate([out[:, :2], out[:, 3:]], axis=1)
+    np.testing.assert_allclose(got, np.array(orows), rtol=OBS_TOL, atol=1e-12 * float(np.max(np.abs(orows))))
+    assert C.rel_l2(g.download(), og.psi) < PSI_TOL
