@@ -39,10 +39,11 @@ namespace qsf {
 
 constexpr int kMaxDim = 3;
 // Threads per block of the row / axis passes (tiles of 4096 points): 512 threads with
-// radix-8 plans (8 points per thread, twice the resident warps) for line lengths whose
-// radix-16 plan ends in a poor tail (512 = 16 16 2, 2048 = 16 16 8), 256 threads with
-// radix-16 plans otherwise (measured per size).
-__host__ __device__ constexpr int row_threads(int n) { return (n == 512 || n == 2048) ? 512 : 256; }
+// radix-8 plans (8 points per thread, twice the resident warps) for the line lengths
+// where that measured faster (384, 512, 2048: their radix-16 plans end in short
+// passes), 256 threads with radix-16 plans otherwise (256 included: its 3D cube loses
+// more than its 2D grid gains).
+__host__ __device__ constexpr int row_threads(int n) { return (n == 384 || n == 512 || n == 2048) ? 512 : 256; }
 __host__ __device__ constexpr int row_ppt(int n) { return 4096 / row_threads(n); }
 constexpr int kLineThreads = 512;
 constexpr int kMaxFluxBorders = 16;

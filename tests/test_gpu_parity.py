@@ -160,10 +160,10 @@ def test_bad_sizes_are_rejected(Q):
         Q.Grid(1, 16384 * 2, 0.1)
 
 
-@pytest.mark.parametrize("n", [512, 1024, 2048])
+@pytest.mark.parametrize("n", [384, 512, 1024, 2048])
 def test_fused_2d_steps_match_oracle(Q, n):
-    """Fused multi-step calls at the large 2D edges (512 and 2048 take the 512-thread,
-    radix-8 row / axis kernels, 1024 the 256-thread radix-16 ones) against the oracle:
+    """Fused multi-step calls at the large 2D edges (384, 512 and 2048 take the
+    512-thread radix-8 row / axis kernels, 1024 the 256-thread radix-16 ones) against the oracle:
     velocity-gauge field, absorber, norm, E_pot and the ZOA_FLUX_2D fluxes every step."""
     from oracle import oracle as O
     from qsf_gb300.propagator import coupling_schedule
