@@ -1104,9 +1104,21 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
     for (int64_t k = 0; k < S.nsteps; ++k)
       if ((rc = launch_step(g, S))) return rc;
   } else {
+    // one graph holds kGraphSteps steps (the kernels read the step index from the
+    // device, so every copy is the same), the remainder runs as single steps
+    constexpr int64_t kGraphSteps = 16;
+    const int64_t per = std::min<int64_t>(kGraphSteps, S.nsteps);
     cudaGraphExec_t exec = nullptr;
-    if ((rc = capture_graph(g->stream, [&]() { return launch_step(g, S); }, &exec))) return rc;
-    for (int64_t k = 0; k < S.nsteps; ++k) {
+    if ((rc = capture_graph(
+             g->stream,
+             [&]() {
+               for (int64_t k = 0; k < per; ++k)
+                 if (int r = launch_step(g, S)) return r;
+               return QSF_OK;
+             },
+             &exec)))
+      return rc;
+    for (int64_t k = 0; k + per <= S.nsteps; k += per) {
       const cudaError_t ce = cudaGraphLaunch(exec, g->stream);
       if (ce != cudaSuccess) {
         cudaGraphExecDestroy(exec);
@@ -1114,6 +1126,8 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
       }
     }
     cudaGraphExecDestroy(exec);
+    for (int64_t k = S.nsteps - S.nsteps % per; k < S.nsteps; ++k)
+      if ((rc = launch_step(g, S))) return rc;
   }
   return finish_step(g, d->normalize, d->nsteps, ncol, rows, steps_done);
 }

@@ -96,10 +96,14 @@ class Grid:
         assert a.size == self.m
         check(lib().qsf_upload(self._h, _dp(a.view(np.float64)), self.m), "qsf_upload")
 
-    def download(self) -> np.ndarray:
-        a = np.empty(self.m, dtype=np.complex128)
-        check(lib().qsf_download(self._h, _dp(a.view(np.float64)), self.m), "qsf_download")
-        return a.reshape(self.shape)
+    def download(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """psi as complex128 of the grid's shape; into `out` (C-contiguous complex128 of
+        m elements, e.g. a pinned buffer) when given."""
+        if out is None:
+            out = np.empty(self.m, dtype=np.complex128)
+        assert out.dtype == np.complex128 and out.size == self.m and out.flags.c_contiguous
+        check(lib().qsf_download(self._h, _dp(out.reshape(-1).view(np.float64)), self.m), "qsf_download")
+        return out.reshape(self.shape)
 
     def synchronize(self) -> None:
         check(lib().qsf_synchronize(self._h), "qsf_synchronize")
