@@ -153,6 +153,8 @@ def lib():
         "qsf_flux": [vp, dp, ctypes.c_int, ip, i64, dp],
         "qsf_mask_region": [vp, ip],
         "qsf_region_transfer": [vp, vp, ctypes.c_int, ctypes.c_int],
+        "qsf_average_log": [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64],
+        "qsf_read_log": [vp, dp, ctypes.c_int64],
         "qsf_add_gaussian": [vp, ctypes.c_double, ctypes.c_double],
         "qsf_step": [vp, ctypes.POINTER(StepDesc), dp, ctypes.POINTER(i64)],
         "qsf_fft_plan_radices": [i64, ip, ip],

@@ -868,6 +868,7 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->mg_slice);
   fr(g->etab);
   fr(g->eptab);
+  fr(g->obs_log);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->own_stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -1029,6 +1030,38 @@ int qsf_average(qsf_grid* g, int rep, int op, double* out) {
   k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nb, vol, g->energy + 1);
   QSF_CU(cudaGetLastError());
   QSF_CU(cudaMemcpyAsync(out, g->energy + 1, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  return QSF_OK;
+}
+
+int qsf_average_log(qsf_grid* g, int rep, int op, int64_t slot) {
+  if (!g || (rep != 1 && rep != 2) || op < 0 || op > 2 || slot < 0) return fail(QSF_EINVAL, "bad argument");
+  if ((size_t)slot >= g->obs_cap) {
+    // grow (keeping what is logged); the copy orders after the stream's earlier work
+    const size_t cap = std::max<size_t>((size_t)slot + 1, std::max<size_t>(g->obs_cap * 2, 1024));
+    double* nb = nullptr;
+    if (int rc = dev_alloc(nb, cap)) return rc;
+    QSF_CU(cudaMemsetAsync(nb, 0, cap * sizeof(double), g->stream));
+    if (g->obs_log) {
+      QSF_CU(cudaMemcpyAsync(nb, g->obs_log, g->obs_cap * sizeof(double), cudaMemcpyDeviceToDevice, g->stream));
+      QSF_CU(cudaStreamSynchronize(g->stream));
+      cudaFree(g->obs_log);
+    }
+    g->obs_log = nb;
+    g->obs_cap = cap;
+  }
+  const int nb = std::min(256, grid_blocks(g->G.m));
+  k_average<<<nb, 256, 0, g->stream>>>(g->G, rep, op, g->partials);
+  const double vol = rep == QSF_REP_X ? g->G.dV : g->G.dVm;
+  k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nb, vol, g->obs_log + slot);
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+int qsf_read_log(qsf_grid* g, double* out, int64_t n) {
+  if (!g || !out || n < 0 || (size_t)n > g->obs_cap) return fail(QSF_EINVAL, "bad argument");
+  if (n == 0) return QSF_OK;
+  QSF_CU(cudaMemcpyAsync(out, g->obs_log, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
   QSF_CU(cudaStreamSynchronize(g->stream));
   return QSF_OK;
 }

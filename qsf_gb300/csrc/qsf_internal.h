@@ -119,5 +119,8 @@ struct qsf_grid {
   int etab_mode = 0;
   double etab_delta = 0.0;
   double2* eptab = nullptr;
+  // observables log of qsf_average_log (device, grow-only)
+  double* obs_log = nullptr;
+  size_t obs_cap = 0;
   cudaEvent_t mg_event = nullptr;
 };

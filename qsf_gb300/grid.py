@@ -121,6 +121,15 @@ class Grid:
         check(lib().qsf_average(self._h, rep, op, ctypes.byref(out)), "qsf_average")
         return out.value
 
+    def average_log(self, rep: int, op: int, slot: int) -> None:
+        """average<R, Op>() into slot `slot` of the device observables log (no wait)."""
+        check(lib().qsf_average_log(self._h, rep, op, int(slot)), "qsf_average_log")
+
+    def read_log(self, n: int) -> np.ndarray:
+        out = np.empty(max(int(n), 0), dtype=np.float64)
+        check(lib().qsf_read_log(self._h, _dp(out), int(n)), "qsf_read_log")
+        return out
+
     def normalize(self) -> float:
         out = ctypes.c_double()
         check(lib().qsf_normalize(self._h, ctypes.byref(out)), "qsf_normalize")

@@ -100,6 +100,7 @@ class MultiRegionPropagator:
         self.timer = 0.0
         self.step = 0
         self.rows: List[dict] = []
+        self._slots: List[dict] = []  # per row: output -> slot of the device log
         # propagator.h:118-127
         self.max_steps = int(coupling.max_pulse_duration() / dt + 1)
 
@@ -123,22 +124,37 @@ class MultiRegionPropagator:
         self.step += 1
 
     def _compute_each(self) -> None:
+        """The main region's outputs; the averages go into the grid's device log (no
+        host wait, so the loop runs ahead of the GPU) and fill the rows at the end."""
         g = self.mg.main
-        row = {}
+        row, slots = {}, {}
+        base = 3 * len(self.rows)
         for o in self.outputs:
             if o == "step":
                 row["step"] = float(self.step)
             elif o == "time":
                 row["time"] = self.timer
             elif o == "norm":
-                row["norm"] = g.average(REP_X, OP_IDENTITY)
+                g.average_log(REP_X, OP_IDENTITY, base)
+                slots["norm"] = base
             elif o == "epot":
-                row["epot"] = g.average(REP_X, OP_POTENTIAL)
+                g.average_log(REP_X, OP_POTENTIAL, base + 1)
+                slots["epot"] = base + 1
         if "ekin" in self.outputs:
             g.fourier(REP_P)
-            row["ekin"] = g.average(REP_P, OP_KINETIC)
+            g.average_log(REP_P, OP_KINETIC, base + 2)
+            slots["ekin"] = base + 2
             g.fourier(REP_X)
         self.rows.append(row)
+        self._slots.append(slots)
+
+    def _finish_rows(self) -> None:
+        if not any(self._slots):
+            return
+        vals = self.mg.main.read_log(1 + max(k for sl in self._slots for k in sl.values()))
+        for row, slots in zip(self.rows, self._slots):
+            for o, k in slots.items():
+                row[o] = float(vals[k])
 
     def run(self) -> List[dict]:
         """The time loop of SplitPropagator::run (propagator.h:442-453)."""
@@ -151,4 +167,5 @@ class MultiRegionPropagator:
         self._compute_each()
         self.mg.post_compute()
         self.mg.synchronize()
+        self._finish_rows()
         return self.rows
