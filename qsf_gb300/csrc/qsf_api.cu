@@ -723,6 +723,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     AxisDev& a = G.ax[k];
     a.n = (int)d->n[k];
     a.n2 = a.n / 2;
+    a.shift = (a.n & (a.n - 1)) == 0 ? __builtin_ctz((unsigned)a.n) : -1;
     a.dx = d->dx[k];
     G.dV *= d->dx[k];
     const double L = d->dx[k] * (double)(d->n[k] - 1);
@@ -869,6 +870,7 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->etab);
   fr(g->eptab);
   fr(g->obs_log);
+  fr(g->vtab);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->own_stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -1022,10 +1024,26 @@ int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* c3) {
   return QSF_OK;
 }
 
+// the per-block partials of average<rep, op> into g->partials; returns the block count
+static int launch_average(qsf_grid* g, int rep, int op, int* nblocks) {
+  const int nb = std::min(256, grid_blocks(g->G.m));
+  if (rep == QSF_REP_X && op == QSF_OP_POTENTIAL) {
+    if (!g->vtab) {
+      if (int rc = dev_alloc(g->vtab, (size_t)g->G.m)) return rc;
+      k_build_vtab<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, g->vtab);
+    }
+    k_average_tab<<<nb, 256, 0, g->stream>>>(g->G, g->vtab, g->partials);
+  } else {
+    k_average<<<nb, 256, 0, g->stream>>>(g->G, rep, op, g->partials);
+  }
+  *nblocks = nb;
+  return QSF_OK;
+}
+
 int qsf_average(qsf_grid* g, int rep, int op, double* out) {
   if (!g || !out || (rep != 1 && rep != 2) || op < 0 || op > 2) return fail(QSF_EINVAL, "bad argument");
-  const int nb = std::min(256, grid_blocks(g->G.m));
-  k_average<<<nb, 256, 0, g->stream>>>(g->G, rep, op, g->partials);
+  int nb = 0;
+  if (int rc = launch_average(g, rep, op, &nb)) return rc;
   const double vol = rep == QSF_REP_X ? g->G.dV : g->G.dVm;
   k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nb, vol, g->energy + 1);
   QSF_CU(cudaGetLastError());
@@ -1050,10 +1068,10 @@ int qsf_average_log(qsf_grid* g, int rep, int op, int64_t slot) {
     g->obs_log = nb;
     g->obs_cap = cap;
   }
-  const int nb = std::min(256, grid_blocks(g->G.m));
-  k_average<<<nb, 256, 0, g->stream>>>(g->G, rep, op, g->partials);
+  int nbk = 0;
+  if (int rc = launch_average(g, rep, op, &nbk)) return rc;
   const double vol = rep == QSF_REP_X ? g->G.dV : g->G.dVm;
-  k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nb, vol, g->obs_log + slot);
+  k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nbk, vol, g->obs_log + slot);
   QSF_CU(cudaGetLastError());
   return QSF_OK;
 }

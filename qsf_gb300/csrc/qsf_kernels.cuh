@@ -54,6 +54,7 @@ constexpr int kMaxFluxBorders = 16;
 
 struct AxisDev {
   int n, n2;
+  int shift;  // log2(n) when n is a power of two, else -1
   long long stride;
   double dx, xmin, dp, inv_2dx;
   const double2* tw;     // exp(-2 pi i t / n), t < n
@@ -220,6 +221,20 @@ __device__ __forceinline__ double potential_at(const GridDev& g, const double* c
 }
 
 __device__ __forceinline__ void unflatten(const GridDev& g, long long p, int* idx) {
+  if (g.m <= 0x7fffffffLL) {  // 32-bit index arithmetic; shifts for power-of-two axes
+    unsigned q = (unsigned)p;
+    for (int d = g.dim - 1; d >= 0; --d) {
+      const AxisDev& a = g.ax[d];
+      if (a.shift >= 0) {
+        idx[d] = (int)(q & ((1u << a.shift) - 1u));
+        q >>= a.shift;
+      } else {
+        idx[d] = (int)(q % (unsigned)a.n);
+        q /= (unsigned)a.n;
+      }
+    }
+    return;
+  }
   for (int d = g.dim - 1; d >= 0; --d) {
     idx[d] = (int)(p % g.ax[d].n);
     p /= g.ax[d].n;
@@ -1425,6 +1440,31 @@ __global__ void __launch_bounds__(256) k_average(GridDev g, int rep, int op, dou
       }
     }
     acc = fma(fma(v.x, v.x, v.y * v.y), w, acc);
+  }
+  block_sum<1>(&acc, red);
+  if (threadIdx.x == 0) out_partials[blockIdx.x] = acc;
+}
+
+// potential per point (X representation), for the member averages of E_pot
+__global__ void k_build_vtab(GridDev g, double* __restrict__ vtab) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
+    int idx[kMaxDim];
+    double c[kMaxDim];
+    unflatten(g, p, idx);
+    for (int d = 0; d < g.dim; ++d) c[d] = xpos(g.ax[d], idx[d]);
+    vtab[p] = potential_at(g, c);
+  }
+}
+// sum |psi|^2 w(p) per block with the weights from a table (E_pot from the potential table)
+__global__ void __launch_bounds__(256) k_average_tab(GridDev g, const double* __restrict__ w, double* out_partials) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 4
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
+    const double2 v = g.psi[p];
+    acc = fma(fma(v.x, v.x, v.y * v.y), w[p], acc);
   }
   block_sum<1>(&acc, red);
   if (threadIdx.x == 0) out_partials[blockIdx.x] = acc;
