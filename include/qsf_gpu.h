@@ -148,9 +148,10 @@ int qsf_region_transfer(qsf_grid* dst, const qsf_grid* src, int axis, int group)
 
 /* average<R, Op>() (grid.h:425-441). */
 int qsf_average(qsf_grid* g, int rep, int op, double* out);
-/* The same average without waiting for it: the value goes into slot `slot` of the
- * grid's observables log on the device (grown as needed), so a host loop can queue
- * many steps ahead; qsf_read_log copies slots 0 .. n-1 to host memory (and waits). */
+/* The same average without waiting for it (no counterpart in the reference, whose
+ * averages return at once): the value goes into slot `slot` of the grid's observables
+ * log on the device (grown as needed), so a host loop can queue many steps ahead;
+ * qsf_read_log copies slots 0 .. n-1 to host memory (and waits). */
 int qsf_average_log(qsf_grid* g, int rep, int op, int64_t slot);
 int qsf_read_log(qsf_grid* g, double* out, int64_t n);
 /* operation<M, R, Normalize>() (grid.h:601-606); returns the norm divided out. */
