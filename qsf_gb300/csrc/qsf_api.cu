@@ -358,7 +358,7 @@ Geom geom_of(const qsf_grid* g) {
 // One step's launches for `count` solves sharing kernels K and geometry q; every
 // kernel reads its solve's descriptors (blockIdx.y) and step counter from device memory.
 int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const StepDev* dS, int count, bool ekin,
-                 int nfblk, cudaStream_t st, Prof* P) {
+                 int nfblk, cudaStream_t st, Prof* P, bool with_open = true) {
   Prof none;
   Prof& pf = P ? *P : none;
   int rc;
@@ -379,7 +379,7 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
                                                (size_t)(q.n / K.line_ctas) * sizeof(double2), st>>>(dG, dS)));
   } else {
     const dim3 gr(q.nrowblk, count);
-    QSF_TIMED(QSF_K_ROW_OPEN, (K.row_open<<<gr, K.row_threads, q.row_smem, st>>>(dG, dS, q.row_L)));
+    if (with_open) QSF_TIMED(QSF_K_ROW_OPEN, (K.row_open<<<gr, K.row_threads, q.row_smem, st>>>(dG, dS, q.row_L)));
     if (D == 3)
       QSF_TIMED(QSF_K_AXIS_FWD,
                 (K.axis_fwd<<<dim3(q.ax_blocks[1], count), K.row_threads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
@@ -399,9 +399,9 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
   return QSF_OK;
 }
 
-int launch_step(qsf_grid* g, const StepDev& S, Prof* P = nullptr) {
+int launch_step(qsf_grid* g, const StepDev& S, Prof* P = nullptr, bool with_open = true) {
   return launch_group(*g->ks, geom_of(g), g->dG, g->dS, 1, (S.obs & QSF_OBS_EKIN) != 0,
-                      S.nfterms > 0 ? g->nfblk : 1, g->stream, P);
+                      S.nfterms > 0 ? g->nfblk : 1, g->stream, P, with_open);
 }
 
 // Validates a step program and stages everything a run of it needs on the device:
@@ -1156,29 +1156,40 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
       if ((rc = launch_step(g, S))) return rc;
   } else {
     // one graph holds kGraphSteps steps (the kernels read the step index from the
-    // device, so every copy is the same), the remainder runs as single steps
-    constexpr int64_t kGraphSteps = 16;
-    const int64_t per = std::min<int64_t>(kGraphSteps, S.nsteps);
-    cudaGraphExec_t exec = nullptr;
-    if ((rc = capture_graph(
-             g->stream,
-             [&]() {
-               for (int64_t k = 0; k < per; ++k)
-                 if (int r = launch_step(g, S)) return r;
-               return QSF_OK;
-             },
-             &exec)))
-      return rc;
-    for (int64_t k = 0; k + per <= S.nsteps; k += per) {
-      const cudaError_t ce = cudaGraphLaunch(exec, g->stream);
-      if (ce != cudaSuccess) {
-        cudaGraphExecDestroy(exec);
-        return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
-      }
-    }
-    cudaGraphExecDestroy(exec);
-    for (int64_t k = S.nsteps - S.nsteps % per; k < S.nsteps; ++k)
+    // device, so every copy is the same), the remainder runs as single steps.  In a
+    // fused call only the first step's opening row pass works, so it runs once, before
+    // the graphs, which leave it out.
+    const bool skip_open = S.fused != 0;
+    int64_t first = 0;
+    if (skip_open) {
       if ((rc = launch_step(g, S))) return rc;
+      first = 1;
+    }
+    const int64_t rest = S.nsteps - first;
+    constexpr int64_t kGraphSteps = 16;
+    const int64_t per = std::max<int64_t>(1, std::min<int64_t>(kGraphSteps, rest));
+    if (rest > 0) {
+      cudaGraphExec_t exec = nullptr;
+      if ((rc = capture_graph(
+               g->stream,
+               [&]() {
+                 for (int64_t k = 0; k < per; ++k)
+                   if (int r = launch_step(g, S, nullptr, !skip_open)) return r;
+                 return QSF_OK;
+               },
+               &exec)))
+        return rc;
+      for (int64_t k = 0; k + per <= rest; k += per) {
+        const cudaError_t ce = cudaGraphLaunch(exec, g->stream);
+        if (ce != cudaSuccess) {
+          cudaGraphExecDestroy(exec);
+          return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
+        }
+      }
+      cudaGraphExecDestroy(exec);
+      for (int64_t k = rest - rest % per; k < rest; ++k)
+        if ((rc = launch_step(g, S, nullptr, !skip_open))) return rc;
+    }
   }
   return finish_step(g, d->normalize, d->nsteps, ncol, rows, steps_done);
 }
