@@ -324,8 +324,9 @@ __device__ __forceinline__ int radix_rt(int s) {
 // butterflies per thread of radix R when every thread holds PPT points of the tile
 __host__ __device__ constexpr int maxb_ppt(int r, int ppt) { return (ppt + r - 1) / r; }
 
-// main radix of the plan for PPT points per thread: radix 16 needs 16 per thread
-__host__ __device__ constexpr int plan_l2(int ppt) { return ppt >= 16 ? QSF_RADIX_LOG2 : 3; }
+// main radix of the plan for PPT points per thread: radix 16 needs 16 per thread,
+// radix 8 needs 8, radix 4 four
+__host__ __device__ constexpr int plan_l2(int ppt) { return ppt >= 16 ? QSF_RADIX_LOG2 : ppt >= 8 ? 3 : 2; }
 
 // the compile-time stages S.. of fft_fx
 template <int N, int S, int PPT>

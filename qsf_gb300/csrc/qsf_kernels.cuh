@@ -45,6 +45,11 @@ constexpr int kMaxDim = 3;
 // more than its 2D grid gains).
 __host__ __device__ constexpr int row_threads(int n) { return (n == 384 || n == 512 || n == 2048) ? 512 : 256; }
 __host__ __device__ constexpr int row_ppt(int n) { return 4096 / row_threads(n); }
+// Points per thread of the one-CTA line kernel (512 threads, one line of n points): a
+// line shorter than 8192 points leaves threads idle in radix-16 passes, and with one
+// CTA per line the per-thread work sets the step's latency, so shorter lines take
+// smaller radices (measured: 1024 points 0.041 -> 0.030 ms, 2048 0.052 -> 0.044 ms)
+__host__ __device__ constexpr int line_ppt(int n) { return n <= 1024 ? 4 : n <= 4096 ? 8 : 16; }
 constexpr int kLineThreads = 512;
 constexpr int kMaxFluxBorders = 16;
 // resident blocks per SM the FFT kernels are compiled for (caps registers per thread)
@@ -1064,11 +1069,11 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{1, N, 1, false};
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, line_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   scale += p_phase(g, S, smx, 0, N, 1, 1, nullptr, red, bits);
   sh = first_pass_shift<N>(bits);
   scale += sh;
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, line_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
   close_block<N>(g, S, smx, 0, N, 0, red, scale, bits, dacc, true, true);
   __syncthreads();
@@ -1076,7 +1081,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
     const int e1 = S.row_ptr[1];
     for (int e = threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = g.psi[S.snap_idx[e]];
   }
-  dacc[2] = (S.obs & 4u) ? ekin_rows<N, 16>(a, smx, ls, N, scale, bits, red) : 0.0;
+  dacc[2] = (S.obs & 4u) ? ekin_rows<N, line_ppt(N)>(a, smx, ls, N, scale, bits, red) : 0.0;
   const double e_n = dacc[3], e_v = dacc[4];
   block_sum<3>(dacc, dred);
   if (threadIdx.x == 0) {

@@ -29,6 +29,9 @@ WORKLOADS = {
     "2d768": (2, 768, 0.3, 77, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
     "2d4096": (2, 4096, 0.3, 410, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
     "3d128": (3, 128, 0.4, 13, 3.0, 1, 1e15, 800.0, 2.0, "ZOA_FLUX_3D", 0),
+    "1d1024": (1, 1024, 0.2, 102, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 400),
+    "1d2048": (1, 2048, 0.2, 205, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 800),
+    "1d8192": (1, 8192, 0.2, 819, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 1638),
 }
 
 
