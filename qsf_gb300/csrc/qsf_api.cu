@@ -373,6 +373,9 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
   // (kind, axis) tables (X tables only in the length gauge), ~128 entries per block
   const int tb = std::max(1, std::min(64, q.nmax / 128));
   const dim3 gt(D * 4 * tb, count);
+  // a one-CTA line kernel also ends the step itself (its fluxes, row and counters); the
+  // tables stay a kernel of their own: their FP64 phases want many SMs
+  const bool full = D == 1 && K.line_full;
   QSF_TIMED(QSF_K_TABLES, (k_tables<<<gt, 256, 0, st>>>(dG, dS, tb)));
   if (D == 1) {
     QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(K.line_ctas, count), kLineThreads,
@@ -394,7 +397,7 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
         QSF_TIMED(QSF_K_AXIS_EKIN,
                   (K.axis_ekin<<<dim3(q.ax_blocks[ax], count), K.row_threads, q.ax_smem[ax], st>>>(dG, dS, ax, q.ax_C[ax])));
   }
-  QSF_TIMED(QSF_K_FINALIZE, (k_finalize<<<dim3(nfblk, count), 256, 0, st>>>(dG, dS)));
+  if (!full) QSF_TIMED(QSF_K_FINALIZE, (k_finalize<<<dim3(nfblk, count), 256, 0, st>>>(dG, dS)));
 #undef QSF_TIMED
   return QSF_OK;
 }

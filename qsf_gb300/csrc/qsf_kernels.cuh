@@ -387,6 +387,176 @@ __device__ __forceinline__ int first_pass_shift(int bits) {
 // shift that brings `bits` to at most 61 (headroom for one complex product)
 __device__ __forceinline__ int product_headroom(int bits) { return bits > 61 ? 61 - bits : 0; }
 
+// value of one per-step table entry: kind 0 P phase (hamiltonian.h:52-58: kinetic and,
+// in the velocity gauge, A.k), kind 1 / 2 length-gauge x.E factor of the open / close
+// X half (hamiltonian.h:60-66 via DipoleCoupling), kind 3 the open half of the next
+// sub-step (coupling row `cn`)
+__device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& S, const double* cp, const double* cn,
+                                               int kind, int d, int i) {
+  const AxisDev& a = g.ax[d];
+  if (kind == 0) {
+    double A = 0.0;
+    if (g.gauge != 1 && cp && g.n_fields) {
+      int dd = d;
+      if (g.p_swap && g.dim >= 2 && d < 2) dd = 1 - d;
+      A = cp[dd];
+    }
+    const double k = kpos(a, i);
+    return expop(S.mode, S.dt * (0.5 * k * k + k * A));
+  }
+  const double* row = kind == 3 ? cn : cp;
+  const double E = (row && g.n_fields) ? row[(kind == 2 ? 3 : 0) + d] : 0.0;
+  return expop(S.mode, (S.dt * 0.5) * (xpos(a, i) * E));
+}
+
+// One (kind, axis) table of a step's per-step tables, or its slice `part` of `tb` (all
+// threads of the block call it; red: 32 doubles of shared memory, e_sh: one shared int)
+__device__ __forceinline__ void tables_one(const GridDev& g, const StepDev& S, int kind, int d, int part, int tb,
+                                           double* red, int* e_sh) {
+  const int D = g.dim;
+  const long long sub = S.ctl[0];
+  if (kind > 0 && g.gauge != 1) return;
+  if (kind == 3 && (!S.fused || sub + 1 >= S.nsteps)) return;
+  const double* cp = S.coupling ? S.coupling + sub * S.coup_stride : nullptr;
+  const double* cn = (S.coupling && sub + 1 < S.nsteps) ? S.coupling + (sub + 1) * S.coup_stride : nullptr;
+  const int n = g.ax[d].n;
+  double mant = 1.0;
+  if (kind == 0 && d == 0) {
+    mant = S.m_mant;
+    if (S.fused && S.normalize) mant *= *S.scale;
+  }
+  double mx = mant;  // real time: phases of modulus 1 times the mantissa
+  if (S.mode == 1) {  // imaginary time: real factors, maximum over the table
+    mx = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, table_entry(g, S, cp, cn, kind, d, i).x * mant);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
+  }
+  if (threadIdx.x == 0) {
+    int e = 0;
+    if (mx > 1.0) frexp(mx, &e);  // mx < 2^e
+    *e_sh = e;
+    if (part == 0) S.texp[kind * 3 + d] = e;
+  }
+  __syncthreads();
+  const double sc = ldexp(mant, -*e_sh);
+  longlong2* out = kind == 0 ? S.ptab + (size_t)d * S.nmax : S.xdyn + ((size_t)(kind - 1) * D + d) * S.nmax;
+  const int chunk = (n + tb - 1) / tb;
+  const int i1 = min(n, (part + 1) * chunk);
+  for (int i = part * chunk + threadIdx.x; i < i1; i += blockDim.x) {
+    const double2 f = table_entry(g, S, cp, cn, kind, d, i);
+    out[i] = to_fx62(make_double2(fmin(fmax(f.x * sc, -1.0), 1.0), fmin(fmax(f.y * sc, -1.0), 1.0)));
+  }
+}
+
+__device__ __forceinline__ void flux_block(const GridDev& g, const FluxPoint* __restrict__ fpts, const FluxTerm* __restrict__ fterms,
+                           int t0, int t1, const double2* __restrict__ snap, const double* A, int nb, double* red,
+                           double* out) {
+  double fl[kMaxFluxBorders];
+#pragma unroll
+  for (int b = 0; b < kMaxFluxBorders; ++b) fl[b] = 0.0;
+  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+    const FluxTerm ft = fterms[t];
+    const FluxPoint fp = fpts[ft.point];
+    const double2 c = snap[fp.c];
+    double dot = 0.0;
+    for (int d = 0; d < g.dim; ++d) {
+      if (ft.w[d] == 0.0) continue;
+      double j = 0.0;
+      if (fp.p[d] >= 0) {
+        const double2 tt = csub(snap[fp.p[d]], snap[fp.q[d]]);
+        j = g.ax[d].inv_2dx * (c.x * tt.y + (-c.y) * tt.x);
+      }
+      if (A) j += A[d] * (c.x * c.x + c.y * c.y);
+      dot += j * ft.w[d];
+    }
+#pragma unroll
+    for (int b = 0; b < kMaxFluxBorders; ++b)
+      if (b == ft.border) fl[b] += dot;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int b = 0; b < kMaxFluxBorders; ++b) {
+    if (b < nb) {
+      const double v = warp_sum(fl[b]);
+      if (lane == 0) red[b * 32 + wid] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nb) {
+    double v = 0.0;
+    for (int w = 0; w < nw; ++w) v += red[threadIdx.x * 32 + w];
+    out[threadIdx.x] = v;
+  }
+  __syncthreads();
+}
+
+// End of a (sub-)step, run by one block once every block's partials and flux partials
+// (nfb blocks of them) are in memory: fixed-order sums, the observables row, the
+// Normalize factor, the convergence test and the step counters.  red: 32 *
+// kMaxFluxBorders doubles of shared memory.
+__device__ __forceinline__ void finalize_tail(const GridDev& g, const StepDev& S, long long sub, bool step_end,
+                                              long long step, int nb, int nfb, double* red) {
+  if (!step_end) {
+    if (threadIdx.x == 0) {
+      if (S.normalize) *S.scale = 1.0;  // no Normalize between sub-steps
+      S.ctl[3] = 0;
+      S.ctl[0] = sub + 1;
+    }
+    return;
+  }
+  // last block: deterministic sums in a fixed order
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < S.nrowblk; i += blockDim.x) {
+    acc[0] += S.partials[0 * S.pmax + i];
+    acc[1] += S.partials[1 * S.pmax + i];
+    acc[2 + g.dim - 1] += S.partials[(2 + g.dim - 1) * S.pmax + i];
+  }
+  if (S.obs & 4u) {
+    for (int d = 0; d < g.dim - 1; ++d)
+      for (int i = threadIdx.x; i < S.naxblk[d]; i += blockDim.x) acc[2 + d] += S.partials[(2 + d) * S.pmax + i];
+  }
+  __shared__ double fsum[kMaxFluxBorders];
+  if (threadIdx.x < nb) {  // per border, the blocks' partials in block order
+    double v = 0.0;
+    for (int k = 0; k < nfb; ++k) v += S.fpartials[k * kMaxFluxBorders + threadIdx.x];
+    fsum[threadIdx.x] = v;
+  }
+  block_sum<5>(acc, red);  // its barriers also publish fsum
+  if (threadIdx.x == 0) {
+    const double norm = acc[0] * g.dV;
+    const double epot = acc[1] * g.dV;
+    double ekin = 0.0;
+    if (S.obs & 4u) {
+      for (int d = 0; d < g.dim; ++d) ekin += (double)(g.m / g.ax[d].n) * acc[2 + d];
+      ekin = 0.5 * g.dVm * ekin;
+    }
+    const int ncol = 3 + nb;
+    double* row = S.rows + step * ncol;
+    row[0] = norm;
+    row[1] = epot;
+    row[2] = ekin;
+    for (int b = 0; b < nb; ++b) row[3 + b] = fsum[b] * g.dV / g.ax[0].dx;
+    if (!(norm > 0.0) || isnan(epot) || isnan(ekin)) S.ctl[4] = 1;
+    if (S.normalize && norm > 0.0) *S.scale = sqrt(1.0 / norm);
+    if (S.mode == 1 && S.state_accuracy > 0.0) {
+      const double se = (S.energy_after_normalize & 1) ? 1.0 / norm : 1.0;
+      const double sk = (S.energy_after_normalize & 2) ? 1.0 / norm : 1.0;
+      const double E = epot * se + ekin * sk;
+      const double dE = E - S.energy_state[0];
+      S.energy_state[0] = E;
+      // converged: one more step runs (its last sub-step is sub + substeps)
+      if (S.ctl[1] >= S.nsteps && fabs(dE) <= S.state_accuracy) S.ctl[1] = sub + S.substeps;
+    }
+    S.ctl[2] = step + 1;
+    S.ctl[3] = 0;
+    S.ctl[0] = sub + 1;
+  }
+}
+
 #ifdef QSF_DEFINE_KERNELS
 // ------------------------------------------------------------ tables
 // Range of the potential (for its fixed-point scale and the imaginary-time X factor
@@ -447,28 +617,6 @@ __global__ void k_build_static(GridDev g, int mode, double delta, int xs_exp, lo
   }
 }
 
-// value of one per-step table entry: kind 0 P phase (hamiltonian.h:52-58: kinetic and,
-// in the velocity gauge, A.k), kind 1 / 2 length-gauge x.E factor of the open / close
-// X half (hamiltonian.h:60-66 via DipoleCoupling), kind 3 the open half of the next
-// sub-step (coupling row `cn`)
-__device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& S, const double* cp, const double* cn,
-                                               int kind, int d, int i) {
-  const AxisDev& a = g.ax[d];
-  if (kind == 0) {
-    double A = 0.0;
-    if (g.gauge != 1 && cp && g.n_fields) {
-      int dd = d;
-      if (g.p_swap && g.dim >= 2 && d < 2) dd = 1 - d;
-      A = cp[dd];
-    }
-    const double k = kpos(a, i);
-    return expop(S.mode, S.dt * (0.5 * k * k + k * A));
-  }
-  const double* row = kind == 3 ? cn : cp;
-  const double E = (row && g.n_fields) ? row[(kind == 2 ? 3 : 0) + d] : 0.0;
-  return expop(S.mode, (S.dt * 0.5) * (xpos(a, i) * E));
-}
-
 // Per-step tables: `tb` blocks per (kind, axis) table, each storing a contiguous slice.
 // A table whose values exceed 1 in magnitude (imaginary time, or a Normalize factor
 // folded in) is stored times 2^-e, e from its maximum (every block of the table
@@ -492,41 +640,7 @@ __global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, 
     S.gmin[gmin_slot(0, sub + 1)] = 0x7fffffff;               // produced by this sub-step's closing pass
     if (!S.fused || sub == 0) S.gmin[gmin_slot(0, sub)] = 0x7fffffff;  // produced by this sub-step's opening pass
   }
-  if (kind > 0 && g.gauge != 1) return;
-  if (kind == 3 && (!S.fused || sub + 1 >= S.nsteps)) return;
-  const double* cp = S.coupling ? S.coupling + sub * S.coup_stride : nullptr;
-  const double* cn = (S.coupling && sub + 1 < S.nsteps) ? S.coupling + (sub + 1) * S.coup_stride : nullptr;
-  const int n = g.ax[d].n;
-  double mant = 1.0;
-  if (kind == 0 && d == 0) {
-    mant = S.m_mant;
-    if (S.fused && S.normalize) mant *= *S.scale;
-  }
-  double mx = mant;  // real time: phases of modulus 1 times the mantissa
-  if (S.mode == 1) {  // imaginary time: real factors, maximum over the table
-    mx = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, table_entry(g, S, cp, cn, kind, d, i).x * mant);
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-    __syncthreads();
-    if (threadIdx.x == 0)
-      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mx = fmax(mx, red[w]);
-  }
-  if (threadIdx.x == 0) {
-    int e = 0;
-    if (mx > 1.0) frexp(mx, &e);  // mx < 2^e
-    e_sh = e;
-    if (part == 0) S.texp[kind * 3 + d] = e;
-  }
-  __syncthreads();
-  const double sc = ldexp(mant, -e_sh);
-  longlong2* out = kind == 0 ? S.ptab + (size_t)d * S.nmax : S.xdyn + ((size_t)(kind - 1) * D + d) * S.nmax;
-  const int chunk = (n + tb - 1) / tb;
-  const int i1 = min(n, (part + 1) * chunk);
-  for (int i = part * chunk + threadIdx.x; i < i1; i += blockDim.x) {
-    const double2 f = table_entry(g, S, cp, cn, kind, d, i);
-    out[i] = to_fx62(make_double2(fmin(fmax(f.x * sc, -1.0), 1.0), fmin(fmax(f.y * sc, -1.0), 1.0)));
-  }
+  tables_one(g, S, kind, d, part, tb, red, &e_sh);
 }
 
 #endif  // QSF_DEFINE_KERNELS
@@ -1054,7 +1168,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
 
 // ------------------------------------------------------------ 1D whole step
 // One block per line: X open . FFT . P . IFFT . X close . observables, line in smem.
-template <int N>
+template <int N, bool FULL>
 __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_line_step(const GridDev* __restrict__ Gs,
                                                             const StepDev* __restrict__ Ss) {
   const GridDev& g = Gs[blockIdx.y];
@@ -1062,7 +1176,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   if (!step_active(S)) return;
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
-  __shared__ double dred[32 * 3];
+  __shared__ double dred[32 * kMaxFluxBorders];
   const AxisDev& a = g.ax[0];
   int bits = 0;
   int scale = open_block<N>(g, S, smx, 0, N, 0, red, bits);
@@ -1088,6 +1202,18 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
     S.partials[0 * S.pmax] = ldexp(dacc[0], (int)e_n);
     S.partials[1 * S.pmax] = ldexp(dacc[1], (int)e_v);
     S.partials[2 * S.pmax] = dacc[2];
+  }
+  if constexpr (FULL) {  // the end of the step in this block: fluxes, row, counters
+    __syncthreads();
+    const long long sub = S.ctl[0];
+    const bool step_end = (sub + 1) % S.substeps == 0;
+    const long long step = sub / S.substeps;
+    const int nb = S.nborders;
+    if (S.nfterms > 0 && step_end) {
+      const double* A = (g.gauge == 0 && S.coupling && g.n_fields) ? S.coupling + sub * S.coup_stride : nullptr;
+      flux_block(g, S.fpts, S.fterms, 0, S.nfterms, S.snap, A, nb, dred, S.fpartials);
+    }
+    finalize_tail(g, S, sub, step_end, step, nb, 1, dred);
   }
 }
 
@@ -1179,48 +1305,6 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis_fft
 // and one border type; j_d = inv_2dx Im(conj(psi) (psi_+ - psi_-)) (0 where the
 // reference's flat-index bounds test fails, grid.h:470-472) + A_d |psi|^2 (velocity
 // gauge), dotted with the normalised border vector.  out[b] written by thread b.
-__device__ void flux_block(const GridDev& g, const FluxPoint* __restrict__ fpts, const FluxTerm* __restrict__ fterms,
-                           int t0, int t1, const double2* __restrict__ snap, const double* A, int nb, double* red,
-                           double* out) {
-  double fl[kMaxFluxBorders];
-#pragma unroll
-  for (int b = 0; b < kMaxFluxBorders; ++b) fl[b] = 0.0;
-  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-    const FluxTerm ft = fterms[t];
-    const FluxPoint fp = fpts[ft.point];
-    const double2 c = snap[fp.c];
-    double dot = 0.0;
-    for (int d = 0; d < g.dim; ++d) {
-      if (ft.w[d] == 0.0) continue;
-      double j = 0.0;
-      if (fp.p[d] >= 0) {
-        const double2 tt = csub(snap[fp.p[d]], snap[fp.q[d]]);
-        j = g.ax[d].inv_2dx * (c.x * tt.y + (-c.y) * tt.x);
-      }
-      if (A) j += A[d] * (c.x * c.x + c.y * c.y);
-      dot += j * ft.w[d];
-    }
-#pragma unroll
-    for (int b = 0; b < kMaxFluxBorders; ++b)
-      if (b == ft.border) fl[b] += dot;
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int b = 0; b < kMaxFluxBorders; ++b) {
-    if (b < nb) {
-      const double v = warp_sum(fl[b]);
-      if (lane == 0) red[b * 32 + wid] = v;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < nb) {
-    double v = 0.0;
-    for (int w = 0; w < nw; ++w) v += red[threadIdx.x * 32 + w];
-    out[threadIdx.x] = v;
-  }
-  __syncthreads();
-}
-
 __global__ void __launch_bounds__(256) k_flux(GridDev g, const FluxPoint* fpts, const FluxTerm* fterms, int nfterms,
                                               const double2* snap, double A0, double A1, double A2, int useA, int nb,
                                               double* out_partials) {
@@ -1261,61 +1345,7 @@ __global__ void __launch_bounds__(256) k_finalize(const GridDev* __restrict__ Gs
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  if (!step_end) {
-    if (threadIdx.x == 0) {
-      if (S.normalize) *S.scale = 1.0;  // no Normalize between sub-steps
-      S.ctl[3] = 0;
-      S.ctl[0] = sub + 1;
-    }
-    return;
-  }
-  // last block: deterministic sums in a fixed order
-  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int i = threadIdx.x; i < S.nrowblk; i += blockDim.x) {
-    acc[0] += S.partials[0 * S.pmax + i];
-    acc[1] += S.partials[1 * S.pmax + i];
-    acc[2 + g.dim - 1] += S.partials[(2 + g.dim - 1) * S.pmax + i];
-  }
-  if (S.obs & 4u) {
-    for (int d = 0; d < g.dim - 1; ++d)
-      for (int i = threadIdx.x; i < S.naxblk[d]; i += blockDim.x) acc[2 + d] += S.partials[(2 + d) * S.pmax + i];
-  }
-  __shared__ double fsum[kMaxFluxBorders];
-  if (threadIdx.x < nb) {  // per border, the blocks' partials in block order
-    double v = 0.0;
-    for (int k = 0; k < (int)gridDim.x; ++k) v += S.fpartials[k * kMaxFluxBorders + threadIdx.x];
-    fsum[threadIdx.x] = v;
-  }
-  block_sum<5>(acc, red);  // its barriers also publish fsum
-  if (threadIdx.x == 0) {
-    const double norm = acc[0] * g.dV;
-    const double epot = acc[1] * g.dV;
-    double ekin = 0.0;
-    if (S.obs & 4u) {
-      for (int d = 0; d < g.dim; ++d) ekin += (double)(g.m / g.ax[d].n) * acc[2 + d];
-      ekin = 0.5 * g.dVm * ekin;
-    }
-    const int ncol = 3 + nb;
-    double* row = S.rows + step * ncol;
-    row[0] = norm;
-    row[1] = epot;
-    row[2] = ekin;
-    for (int b = 0; b < nb; ++b) row[3 + b] = fsum[b] * g.dV / g.ax[0].dx;
-    if (!(norm > 0.0) || isnan(epot) || isnan(ekin)) S.ctl[4] = 1;
-    if (S.normalize && norm > 0.0) *S.scale = sqrt(1.0 / norm);
-    if (S.mode == 1 && S.state_accuracy > 0.0) {
-      const double se = (S.energy_after_normalize & 1) ? 1.0 / norm : 1.0;
-      const double sk = (S.energy_after_normalize & 2) ? 1.0 / norm : 1.0;
-      const double E = epot * se + ekin * sk;
-      const double dE = E - S.energy_state[0];
-      S.energy_state[0] = E;
-      // converged: one more step runs (its last sub-step is sub + substeps)
-      if (S.ctl[1] >= S.nsteps && fabs(dE) <= S.state_accuracy) S.ctl[1] = sub + S.substeps;
-    }
-    S.ctl[2] = step + 1;
-    S.ctl[3] = 0;
-    S.ctl[0] = sub + 1;
-  }
+  finalize_tail(g, S, sub, step_end, step, nb, (int)gridDim.x, red);
 }
 
 // apply a pending Normalize factor (end of a qsf_step call / qsf_normalize)
@@ -1618,6 +1648,7 @@ struct KernelSet {
   void (*axis_fft_b)(GridDev, int, int, double);
   int line_ctas;  // CTAs holding one 1D line (2: a cluster pair, lines above 8192 points)
   int row_threads;  // threads per block of the row / axis passes
+  bool line_full;   // line_step also ends the step (fluxes, row, counters: no k_finalize)
 };
 
 // kernel table of the supported sizes (qsf_sizes_*.cu); nullptr when n is not built
@@ -1637,6 +1668,7 @@ KernelSet make_kernel_set() {
   k.n = N;
   k.line_ctas = 1;
   k.row_threads = row_threads(N);
+  k.line_full = false;
   if constexpr (N > 8192) {
     k.line_ctas = 2;
     k.line_step = k_line_step_cl<N>;
@@ -1654,7 +1686,8 @@ KernelSet make_kernel_set() {
     k.axis_fft_f = k_axis_fft<N, true>;
     k.axis_fft_b = k_axis_fft<N, false>;
   }
-  k.line_step = k_line_step<N>;
+  k.line_step = k_line_step<N, true>;
+  k.line_full = true;
   k.row_fft_f = k_row_fft<N, true>;
   k.row_fft_b = k_row_fft<N, false>;
   return k;
