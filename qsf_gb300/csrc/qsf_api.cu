@@ -874,6 +874,7 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->eptab);
   fr(g->obs_log);
   fr(g->vtab);
+  fr(g->mtab);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->own_stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -911,6 +912,15 @@ int qsf_download(qsf_grid* g, double* host, int64_t m) {
 int qsf_synchronize(qsf_grid* g) {
   if (!g) return fail(QSF_EINVAL, "null argument");
   QSF_CU(cudaStreamSynchronize(g->stream));
+  return QSF_OK;
+}
+
+// the per-axis one-node mask table (k_mask_tab), built once per grid
+static int ensure_mtab(qsf_grid* g) {
+  if (g->mtab) return QSF_OK;
+  if (int rc = dev_alloc(g->mtab, (size_t)g->G.dim * g->nmax)) return rc;
+  k_mask_tab<<<(g->G.dim * g->nmax + 255) / 256, 256, 0, g->stream>>>(g->G, g->nmax, g->mtab);
+  QSF_CU(cudaGetLastError());
   return QSF_OK;
 }
 
@@ -988,7 +998,9 @@ int qsf_region_transfer(qsf_grid* dst, const qsf_grid* src, int axis, int group)
   QSF_CU(cudaStreamWaitEvent(dst->stream, s->mg_event, 0));
   // boxes of nCAP planes along the sliding axis (multigrid.h:184, 296-317): n / nCAP of them
   const long long slide_lim = G.dim == 3 ? (G.ax[0].n / G.nCAP) * G.nCAP : 0;
-  k_mg_slice<<<grid_blocks(G.m), 256, 0, dst->stream>>>(G, H.psi, dst->mg_slice, axis, group, slide_lim);
+  if (int rc = ensure_mtab(dst)) return rc;
+  k_mg_slice<<<grid_blocks(G.m), 256, 0, dst->stream>>>(G, H.psi, dst->mg_slice, axis, group, slide_lim, dst->mtab,
+                                                        dst->nmax);
   GridDev Gs = G;
   Gs.psi = dst->mg_slice;
   axis_fft(dst, Gs, axis, true, 1.0);
@@ -1124,7 +1136,10 @@ int qsf_flux(qsf_grid* g, const double* A3, int nb, const int* types, int64_t bo
 
 int qsf_mask_region(qsf_grid* g, const int* b3) {
   if (!g || !b3) return fail(QSF_EINVAL, "null argument");
-  k_mask<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, b3[0], g->G.dim > 1 ? b3[1] : 1, g->G.dim > 2 ? b3[2] : 1);
+  if (g->G.nCAP <= 0) return QSF_OK;  // no absorber: the mask is 1 everywhere
+  if (int rc = ensure_mtab(g)) return rc;
+  k_mask<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, b3[0], g->G.dim > 1 ? b3[1] : 1, g->G.dim > 2 ? b3[2] : 1,
+                                                     g->mtab, g->nmax);
   QSF_CU(cudaGetLastError());
   return QSF_OK;
 }

@@ -121,7 +121,8 @@ struct qsf_grid {
   double2* eptab = nullptr;
   // observables log of qsf_average_log (device, grow-only)
   double* obs_log = nullptr;
-  double* vtab = nullptr;  // potential per point for member E_pot averages (built on first use)
+  double* vtab = nullptr;
+  double* mtab = nullptr;  // per-axis one-node absorber masks [dim][nmax] (built on first use)  // potential per point for member E_pot averages (built on first use)
   size_t obs_cap = 0;
   cudaEvent_t mg_event = nullptr;
 };

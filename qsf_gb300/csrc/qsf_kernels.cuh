@@ -1530,13 +1530,23 @@ __device__ __forceinline__ long long neg_dist(const GridDev& g, int d, int i) {
   return i < g.ax[d].n2 ? -(long long)i : (long long)i - g.ax[d].n + 1;
 }
 
+// Per-axis values of the one-node absorber mask, mtab[d * nmax + i] = CAP::mask of axis
+// d's node i (absorbers.h:48-54).  The mask of several nodes, exp(-eta sum_d n_d^4), is
+// the product of these (to rounding), so the region masks and transfers below need no exp.
+__global__ void k_mask_tab(GridDev g, int nmax, double* __restrict__ mtab) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.dim * nmax; e += gridDim.x * blockDim.x) {
+    const int d = e / nmax, i = e % nmax;
+    mtab[e] = i < g.ax[d].n ? mask1(g, neg_dist(g, d, i)) : 1.0;
+  }
+}
+
 // Slice of a region transfer (getBox + maskSlice, multigrid.h:454-569): src in the
 // margins along fc times 1 - mask(fc) and, for a destination in group 1, the corner
 // correction (mask_correction, multigrid.h:519-530); zero elsewhere, except in 1D,
 // where the whole line is copied and only its margins are masked.  In 3D the sliding
 // axis is limited to the n / nCAP boxes (slide_lim planes).
 __global__ void k_mg_slice(GridDev g, const double2* __restrict__ src, double2* __restrict__ slice, int fc, int group,
-                           long long slide_lim) {
+                           long long slide_lim, const double* __restrict__ mtab, int nmax) {
   const int D = g.dim;
   const int slide = D == 3 ? (fc == 1 ? 2 : 1) : -1;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -1549,19 +1559,19 @@ __global__ void k_mg_slice(GridDev g, const double2* __restrict__ src, double2* 
       slice[p] = (D == 1 && !band) ? src[p] : make_double2(0.0, 0.0);
       continue;
     }
-    const double mv = 1.0 - mask1(g, neg_dist(g, fc, i));
+    const double mv = 1.0 - mtab[fc * nmax + i];
     double f = mv;
     if (group == 1) {
       double corr = 1.0;
       if (D == 2) {
         const int o = 1 - fc;
-        const double b0 = fc == 0 ? 1.0 : 1.0 - mask1(g, neg_dist(g, o, idx[o]));
-        const double b1 = fc == 1 ? 1.0 : 1.0 - mask1(g, neg_dist(g, o, idx[o]));
+        const double b0 = fc == 0 ? 1.0 : 1.0 - mtab[o * nmax + idx[o]];
+        const double b1 = fc == 1 ? 1.0 : 1.0 - mtab[o * nmax + idx[o]];
         corr = 1 - 0.5 * (b0 * b1);
       } else if (D == 3) {
         double a[3], b[3];
         for (int d = 0; d < 3; ++d) {
-          const double mk = mask1(g, neg_dist(g, d, idx[d]));
+          const double mk = mtab[d * nmax + idx[d]];
           a[d] = d == fc ? 0 : mk;
           b[d] = d == fc ? 1.0 : mk;
         }
@@ -1583,31 +1593,18 @@ __global__ void k_add_slice(double2* __restrict__ dst, const double2* __restrict
   }
 }
 
-__global__ void k_mask(GridDev g, int b0, int b1, int b2) {
+// maskRegion_ (grid.h:582-597): psi *= the mask of the bounded axes' nodes, as the
+// product of the per-axis one-node masks (a free axis contributes 1)
+__global__ void k_mask(GridDev g, int b0, int b1, int b2, const double* __restrict__ mtab, int nmax) {
   const int bounded[3] = {b0, b1, b2};
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < g.m; p += stride) {
     int idx[kMaxDim];
     unflatten(g, p, idx);
-    long long nodes[kMaxDim];
-    bool all_neg = true;
-    for (int d = 0; d < g.dim; ++d) {
-      const int i = idx[d];
-      const long long nd = bounded[d] ? (i < g.ax[d].n2 ? -(long long)i : (long long)i - g.ax[d].n + 1)
-                                      : -(long long)g.ax[d].n2;
-      nodes[d] = g.nCAP + nd;
-      if (!(nodes[d] < 0)) all_neg = false;
-    }
     double mk = 1.0;
-    if (!all_neg) {
-      long long s = 0;
-      for (int d = g.dim - 1; d >= 0; --d) {
-        const long long v = nodes[d] > 0 ? nodes[d] * (nodes[d] * (nodes[d] * nodes[d])) : 0;
-        s = v + s;
-      }
-      mk = exp(-(double)s * g.eta);
-    }
-    g.psi[p] = cscale(g.psi[p], mk);
+    for (int d = 0; d < g.dim; ++d)
+      if (bounded[d]) mk *= mtab[d * nmax + idx[d]];
+    if (mk != 1.0) g.psi[p] = cscale(g.psi[p], mk);
   }
 }
 
