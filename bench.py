@@ -278,14 +278,14 @@ def run_batched(steps, warmup, nsolves=256, seed=0):
                         "lambda U[400,1600] nm, 3-cycle sin^2 VG, norm+E_pot+ZOA_FLUX_2D every step, seed 0"}
 
 
-def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128):
+def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, steps_per_round=16):
     """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N in 1024..16384) and 2D
     (edge in 256..1024) solves with seeded pulses; each solve runs its first
     `steps_per_solve` steps.  Returns throughput and p50/p99 submit->completion."""
     import qsf_gb300 as Q
     from qsf_gb300 import serve as S
     rng = np.random.default_rng(seed)
-    srv = S.Server(max_slots=max_slots, hbm_reserve_gb=16.0, steps_per_round=16)
+    srv = S.Server(max_slots=max_slots, hbm_reserve_gb=16.0, steps_per_round=steps_per_round)
     tickets, pts = [], 0.0
     t0 = time.perf_counter()
     t_next = t0
