@@ -355,10 +355,20 @@ Geom geom_of(const qsf_grid* g) {
   return q;
 }
 
+// k_finalize on a second stream (`side`): it forks from `st` after the sub-step's last
+// pass, and the next sub-step waits for it (`done`) only before its pass that rewrites
+// the partials and the flux snapshot.  Valid when k_finalize writes nothing the next
+// sub-step's earlier kernels read: no pending Normalize factor, no convergence stop.
+struct FinOverlap {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  bool pending = false;
+};
+
 // One step's launches for `count` solves sharing kernels K and geometry q; every
 // kernel reads its solve's descriptors (blockIdx.y) and step counter from device memory.
 int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const StepDev* dS, int count, bool ekin,
-                 int nfblk, cudaStream_t st, Prof* P, bool with_open = true) {
+                 int nfblk, cudaStream_t st, Prof* P, bool with_open = true, FinOverlap* ov = nullptr) {
   Prof none;
   Prof& pf = P ? *P : none;
   int rc;
@@ -377,7 +387,9 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
   // tables stay a kernel of their own: their FP64 phases want many SMs
   const bool full = D == 1 && K.line_full;
   QSF_TIMED(QSF_K_TABLES, (k_tables<<<gt, 256, 0, st>>>(dG, dS, tb)));
+  const bool wait_fin = ov && ov->pending;
   if (D == 1) {
+    if (wait_fin) QSF_CU(cudaStreamWaitEvent(st, ov->done, 0));
     QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(K.line_ctas, count), kLineThreads,
                                                (size_t)(q.n / K.line_ctas) * sizeof(double2), st>>>(dG, dS)));
   } else {
@@ -391,20 +403,46 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
     if (D == 3)
       QSF_TIMED(QSF_K_AXIS_INV,
                 (K.axis_inv<<<dim3(q.ax_blocks[1], count), K.row_threads, q.ax_smem[1], st>>>(dG, dS, 1, q.ax_C[1])));
+    if (wait_fin) QSF_CU(cudaStreamWaitEvent(st, ov->done, 0));
     QSF_TIMED(QSF_K_ROW_CLOSE, (K.row_close<<<gr, K.row_threads, q.row_smem, st>>>(dG, dS, q.row_L)));
     if (ekin)
       for (int ax = 0; ax < D - 1; ++ax)
         QSF_TIMED(QSF_K_AXIS_EKIN,
                   (K.axis_ekin<<<dim3(q.ax_blocks[ax], count), K.row_threads, q.ax_smem[ax], st>>>(dG, dS, ax, q.ax_C[ax])));
   }
-  if (!full) QSF_TIMED(QSF_K_FINALIZE, (k_finalize<<<dim3(nfblk, count), 256, 0, st>>>(dG, dS)));
+  if (ov) ov->pending = false;
+  if (!full && ov) {
+    QSF_CU(cudaEventRecord(ov->fork, st));
+    QSF_CU(cudaStreamWaitEvent(ov->side, ov->fork, 0));
+    k_finalize<<<dim3(nfblk, count), 256, 0, ov->side>>>(dG, dS);
+    QSF_CU(cudaGetLastError());
+    QSF_CU(cudaEventRecord(ov->done, ov->side));
+    ov->pending = true;
+  } else if (!full) {
+    QSF_TIMED(QSF_K_FINALIZE, (k_finalize<<<dim3(nfblk, count), 256, 0, st>>>(dG, dS)));
+  }
 #undef QSF_TIMED
   return QSF_OK;
 }
 
-int launch_step(qsf_grid* g, const StepDev& S, Prof* P = nullptr, bool with_open = true) {
+int launch_step(qsf_grid* g, const StepDev& S, Prof* P = nullptr, bool with_open = true, FinOverlap* ov = nullptr) {
   return launch_group(*g->ks, geom_of(g), g->dG, g->dS, 1, (S.obs & QSF_OBS_EKIN) != 0,
-                      S.nfterms > 0 ? g->nfblk : 1, g->stream, P, with_open);
+                      S.nfterms > 0 ? g->nfblk : 1, g->stream, P, with_open, ov);
+}
+
+// Whether k_finalize may run beside the next sub-step (FinOverlap), and its stream.
+bool fin_overlap_ok(const StepDev& S) { return !S.normalize && !(S.mode == 1 && S.state_accuracy > 0.0); }
+int ensure_fin_stream(qsf_grid* g, FinOverlap* ov) {
+  if (!g->fin_stream) {
+    QSF_CU(cudaStreamCreateWithFlags(&g->fin_stream, cudaStreamNonBlocking));
+    QSF_CU(cudaEventCreateWithFlags(&g->fin_fork, cudaEventDisableTiming));
+    QSF_CU(cudaEventCreateWithFlags(&g->fin_done, cudaEventDisableTiming));
+  }
+  ov->side = g->fin_stream;
+  ov->fork = g->fin_fork;
+  ov->done = g->fin_done;
+  ov->pending = false;
+  return QSF_OK;
 }
 
 // Validates a step program and stages everything a run of it needs on the device:
@@ -876,6 +914,9 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->vtab);
   fr(g->mtab);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
+  if (g->fin_fork) cudaEventDestroy(g->fin_fork);
+  if (g->fin_done) cudaEventDestroy(g->fin_done);
+  if (g->fin_stream) cudaStreamDestroy(g->fin_stream);
   if (g->own_stream) cudaStreamDestroy(g->stream);
   delete g;
   return QSF_OK;
@@ -1188,11 +1229,15 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
     const int64_t per = std::max<int64_t>(1, std::min<int64_t>(kGraphSteps, rest));
     if (rest > 0) {
       cudaGraphExec_t exec = nullptr;
+      FinOverlap ov;
+      const bool overlap = fin_overlap_ok(S);
+      if (overlap && (rc = ensure_fin_stream(g, &ov))) return rc;
       if ((rc = capture_graph(
                g->stream,
                [&]() {
                  for (int64_t k = 0; k < per; ++k)
-                   if (int r = launch_step(g, S, nullptr, !skip_open)) return r;
+                   if (int r = launch_step(g, S, nullptr, !skip_open, overlap ? &ov : nullptr)) return r;
+                 if (ov.pending) QSF_CU(cudaStreamWaitEvent(g->stream, ov.done, 0));  // join
                  return QSF_OK;
                },
                &exec)))

@@ -109,7 +109,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   cg::cluster_group cl = cg::this_cluster();
-  if (!step_active(S)) return;  // uniform over the pair
+  if (!pass_active(S)) return;  // uniform over the pair
+  if (blockIdx.x % 2 == 0 && threadIdx.x == 0) S.ctl[6] = S.ctl[5] + 1;  // the sub-step's only pass
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32 * 3];

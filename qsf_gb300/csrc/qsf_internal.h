@@ -121,8 +121,12 @@ struct qsf_grid {
   double2* eptab = nullptr;
   // observables log of qsf_average_log (device, grow-only)
   double* obs_log = nullptr;
-  double* vtab = nullptr;
-  double* mtab = nullptr;  // per-axis one-node absorber masks [dim][nmax] (built on first use)  // potential per point for member E_pot averages (built on first use)
   size_t obs_cap = 0;
+  double* vtab = nullptr;  // potential per point for member E_pot averages (built on first use)
+  double* mtab = nullptr;  // per-axis one-node absorber masks [dim][nmax] (built on first use)
   cudaEvent_t mg_event = nullptr;
+  // k_finalize of graph-replayed steps on a second stream, beside the next sub-step's
+  // first passes: the stream and its fork / join events (created on first use)
+  cudaStream_t fin_stream = nullptr;
+  cudaEvent_t fin_fork = nullptr, fin_done = nullptr;
 };

@@ -134,8 +134,12 @@ struct StepDev {
   const FluxTerm* fterms;
   int nfterms;
   double* fpartials;  // [nblk][kMaxFluxBorders]
-  // control (device): ctl[0] sub-step within call, ctl[1] stop after this sub-step
-  // (or nsteps), ctl[2] steps done, ctl[3] finalize block counter, ctl[4] NaN flag.
+  // control (device): ctl[0] sub-step within call (k_finalize's), ctl[1] stop after
+  // this sub-step (or nsteps), ctl[2] steps done, ctl[3] finalize block counter,
+  // ctl[4] NaN flag, ctl[5] sub-step of the pass kernels (k_tables copies it from
+  // ctl[6]), ctl[6] next sub-step of the pass kernels (advanced by the sub-step's last
+  // pass).  The two counters let k_finalize of one sub-step run beside the next
+  // sub-step's tables and first passes.
   // nsteps counts sub-steps: steps * substeps (MultiProductSplit order).
   int substeps;
   long long* ctl;
@@ -145,6 +149,7 @@ struct StepDev {
 };
 
 __device__ __forceinline__ bool step_active(const StepDev& S) { return S.ctl[0] <= S.ctl[1] && S.ctl[0] < S.nsteps; }
+__device__ __forceinline__ bool pass_active(const StepDev& S) { return S.ctl[5] <= S.ctl[1] && S.ctl[5] < S.nsteps; }
 
 // ------------------------------------------------------------ reductions
 __device__ __forceinline__ double warp_sum(double v) {
@@ -411,10 +416,9 @@ __device__ __forceinline__ double2 table_entry(const GridDev& g, const StepDev& 
 
 // One (kind, axis) table of a step's per-step tables, or its slice `part` of `tb` (all
 // threads of the block call it; red: 32 doubles of shared memory, e_sh: one shared int)
-__device__ __forceinline__ void tables_one(const GridDev& g, const StepDev& S, int kind, int d, int part, int tb,
-                                           double* red, int* e_sh) {
+__device__ __forceinline__ void tables_one(const GridDev& g, const StepDev& S, long long sub, int kind, int d, int part,
+                                           int tb, double* red, int* e_sh) {
   const int D = g.dim;
-  const long long sub = S.ctl[0];
   if (kind > 0 && g.gauge != 1) return;
   if (kind == 3 && (!S.fused || sub + 1 >= S.nsteps)) return;
   const double* cp = S.coupling ? S.coupling + sub * S.coup_stride : nullptr;
@@ -628,19 +632,22 @@ __global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, 
                                                 int tb) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
-  if (!step_active(S)) return;
+  // the sub-step of this step's passes; every block stores the same value, also when
+  // the step is inactive (its passes then read an inactive sub-step too)
+  const long long sub = S.ctl[6];
+  if (threadIdx.x == 0) S.ctl[5] = sub;
+  if (!(sub <= S.ctl[1] && sub < S.nsteps)) return;
   __shared__ double red[32];
   __shared__ int e_sh;
   const int D = g.dim;
   const int table = blockIdx.x / tb, part = blockIdx.x % tb;
   const int kind = table / D, d = table % D;
-  const long long sub = S.ctl[0];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     S.gmin[1] = S.gmin[2] = S.gmin[3] = 0x7fffffff;
     S.gmin[gmin_slot(0, sub + 1)] = 0x7fffffff;               // produced by this sub-step's closing pass
     if (!S.fused || sub == 0) S.gmin[gmin_slot(0, sub)] = 0x7fffffff;  // produced by this sub-step's opening pass
   }
-  tables_one(g, S, kind, d, part, tb, red, &e_sh);
+  tables_one(g, S, sub, kind, d, part, tb, red, &e_sh);
 }
 
 #endif  // QSF_DEFINE_KERNELS
@@ -873,8 +880,8 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_open
                                                           const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
-  if (!step_active(S)) return;
-  const long long sub = S.ctl[0];
+  if (!pass_active(S)) return;
+  const long long sub = S.ctl[5];
   if (S.fused && sub > 0) return;  // the previous sub-step's closing pass produced pass 0
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
@@ -907,7 +914,7 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
                                             long long obase, long long inner, int rows, int Ch, int ldc, int* red,
                                             int& bits, bool conj, const int* dtab = nullptr,
                                             bool tab_by_row = false) {
-  const int gm = S.gmin[gmin_slot(in_pass, S.ctl[0])];
+  const int gm = S.gmin[gmin_slot(in_pass, S.ctl[5])];
   const int* sc = S.sc + (size_t)in_pass * S.scmax;
   const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
   const int cnt = rows * Ch;
@@ -939,7 +946,7 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
 template <int N>
 __device__ __forceinline__ void build_dtab(const StepDev& S, int in_pass, int* dtab, long long base_block,
                                            long long kbase, int div) {
-  const int gm = S.gmin[gmin_slot(in_pass, S.ctl[0])];
+  const int gm = S.gmin[gmin_slot(in_pass, S.ctl[5])];
   const int* sc = S.sc + (size_t)in_pass * S.scmax;
   for (int k = threadIdx.x; k < N; k += blockDim.x) dtab[k] = gm - sc[base_block + (kbase + k) / div];
   __syncthreads();
@@ -956,12 +963,13 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
                                                            const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
-  if (!step_active(S)) return;
+  if (!pass_active(S)) return;
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32 * 3];
   const AxisDev& a = g.ax[g.dim - 1];
-  const long long sub = S.ctl[0];
+  const long long sub = S.ctl[5];
+  if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl[6] = sub + 1;  // the sub-step's last pass
   const bool last = !S.fused || sub >= S.ctl[1] || sub + 1 >= S.nsteps;
   const long long row0 = (long long)blockIdx.x * L;
   const int Lh = (int)min((long long)L, g.m / N - row0);
@@ -1076,7 +1084,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
                                                       int ax, int C) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
-  if (!step_active(S)) return;
+  if (!pass_active(S)) return;
   if (MODE == 3 && !(S.obs & 4u)) return;
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
@@ -1173,7 +1181,8 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
                                                             const StepDev* __restrict__ Ss) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
-  if (!step_active(S)) return;
+  if (!pass_active(S)) return;
+  if (threadIdx.x == 0) S.ctl[6] = S.ctl[5] + 1;  // the sub-step's only pass
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32 * kMaxFluxBorders];
@@ -1205,7 +1214,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   }
   if constexpr (FULL) {  // the end of the step in this block: fluxes, row, counters
     __syncthreads();
-    const long long sub = S.ctl[0];
+    const long long sub = S.ctl[5];
     const bool step_end = (sub + 1) % S.substeps == 0;
     const long long step = sub / S.substeps;
     const int nb = S.nborders;

@@ -62,6 +62,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--ekin", action="store_true", help="also compute the kinetic energy every step")
     ap.add_argument("--fourier", type=int, default=0, help="instead time this many forward+backward transforms")
+    ap.add_argument("--timed", action="store_true",
+                    help="instead time one call of --steps steps as a user runs it (graph-replayed, wall clock "
+                         "around the call after a warm-up call)")
     args = ap.parse_args()
     import time
     import qsf_gb300 as Q
@@ -81,6 +84,15 @@ def main():
     obs = Q.OBS_NORM | Q.OBS_EPOT | (Q.OBS_EKIN if args.ekin else 0)
     prof = {}
     sched = prop._schedule(args.steps)
+    if args.timed:
+        g.step(Q.MODE_RE, 0.05, args.steps, sched, obs=obs, borders=borders, box_size=box)
+        g.synchronize()
+        t0 = time.perf_counter()
+        g.step(Q.MODE_RE, 0.05, args.steps, sched, obs=obs, borders=borders, box_size=box)
+        g.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        print(json.dumps({"workload": args.workload, "steps": args.steps, "timed_ms_per_step": ms}))
+        return
     g.step(Q.MODE_RE, 0.05, args.steps, sched, obs=obs, borders=borders, box_size=box, profile=prof)
     tot = sum(v[0] for v in prof.values())
     print(json.dumps({"workload": args.workload, "steps": args.steps, "ms_per_step": tot / args.steps,
