@@ -58,6 +58,10 @@ extern "C" {
  * the length gauge couples x.E(t) in X */
 #define QSF_GAUGE_VELOCITY 0
 #define QSF_GAUGE_LENGTH 1
+
+/* absorber kinds (qsf_grid_desc.absorber) */
+#define QSF_ABS_CAP 0  /* the reference's quartic CAP (absorbers.h:27-54) */
+#define QSF_ABS_COS8 1 /* cos^(1/8) mask over the same margins; no reference counterpart */
 /* averaged operators: Identity, PotentialEnergy, KineticEnergy (grid.h:7-22) */
 #define QSF_OP_IDENTITY 0
 #define QSF_OP_POTENTIAL 1
@@ -107,6 +111,15 @@ typedef struct qsf_grid_desc {
    * axes step through the member operations; qsf_step rejects them.              */
   int free_axes;
   int multi_region;
+  /* Absorber over the nCAP-node margins.  QSF_ABS_CAP (0): the reference's CAP,
+   * exp(-delta eta sum_d max(0, nodes_d)^4) per evolve<X>(delta).  QSF_ABS_COS8: the
+   * cos^(1/8) mask of the 1D plain configuration (the reference has none): with node
+   * depth nodes_d = nCAP + neg_dist_from_edge (grid.h:181-185), M = prod_d
+   * cos(pi/2 nodes_d / nCAP)^(1/8) over the margin nodes, applied once per mask_dt of
+   * propagation (evolve<X>(delta) multiplies by M^(delta / mask_dt); a Strang step of
+   * dt = mask_dt applies M once).  Needs nCAP >= 1, mask_dt > 0, multi_region = 0. */
+  int absorber;
+  double mask_dt;
 } qsf_grid_desc;
 
 typedef struct qsf_grid qsf_grid;

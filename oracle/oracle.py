@@ -30,6 +30,7 @@ MODE_IM, MODE_RE = 1, 2
 REP_X, REP_P = 1, 2
 OP_IDENTITY, OP_POTENTIAL, OP_KINETIC = 0, 1, 2
 POT_EBERLY, POT_ECKHARDT_SACHA, POT_COULOMB, POT_NONE = 0, 1, 2, 3
+ABS_CAP, ABS_COS8 = 0, 1
 GAUGE_VELOCITY, GAUGE_LENGTH = 0, 1
 PULSE_SIN, PULSE_SIN2_SIN, PULSE_CONST, PULSE_CHEMPHYS = 0, 1, 2, 3
 
@@ -90,6 +91,7 @@ def lib():
         L.orc_field_max_duration.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_field_max_duration.restype = ctypes.c_double
         L.orc_grid_set_region.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.orc_grid_set_absorber.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
         L.orc_mg_transfer.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_int, ctypes.c_int]
     return _LIB
 
@@ -249,6 +251,12 @@ class Grid:
     def mask_region(self, bounded):
         b = (ctypes.c_int * 3)(*(list(bounded) + [1] * (3 - len(bounded))))
         lib().orc_mask_region(self._buf, self._p(), b)
+
+    def set_absorber(self, kind: int, mask_dt: float = 0.0):
+        """Absorber kind: ABS_CAP (absorbers.h, the default) or ABS_COS8, the cos^(1/8)
+        mask over the same nCAP-node margins applied once per mask_dt of propagation
+        (orc_grid_set_absorber)."""
+        lib().orc_grid_set_absorber(self._buf, int(kind), float(mask_dt))
 
     def set_region(self, free_mask: int, multi: bool = True):
         """Make this grid region `free_mask` (bit d: axis d kept in P space) of a

@@ -191,6 +191,8 @@ typedef struct {
   int p_swap;   /* emulate the transposed P layout (coupling of axes 0 and 1 swapped) */
   int free_mask; /* region of a multi-region grid: axes kept in P space (bit d = axis d) */
   int multi;     /* multi-region grid: partial potentials, no absorber in evolve */
+  int abs_kind;    /* 0 quartic CAP (absorbers.h), 1 cos^(1/8) mask (orc_grid_set_absorber) */
+  double abs_rate; /* cos^(1/8) mask: applications per unit time (1 / mask_dt) */
 } orc_grid;
 
 /* coords.h:55-93 (CartesianGrid_::init), absorbers.h:27-33 (eta), potential.h:122-124 */
@@ -241,6 +243,18 @@ void orc_grid_set_region(orc_grid* g, int free_mask, int multi) {
   g->free_mask = free_mask;
   g->multi = multi;
   g->p_swap = (g->dim >= 2 && free_mask == 0) ? 1 : 0;
+}
+
+/* The cos^(1/8) mask absorber of the 1D plain configuration's text (no reference
+ * counterpart: the reference has only the quartic CAP of absorbers.h).  Over the same
+ * margin of nCAP nodes per side, node depth nodes = nCAP + neg_dist_from_edge (nCAP at
+ * the outermost node, 1 at the innermost margin node), the mask of one axis is
+ * M_d = cos(pi/2 * nodes / nCAP)^(1/8) and of a point the product over axes.  It is
+ * applied once per mask_dt of propagation: evolve<X>(delta) multiplies by
+ * M^(delta / mask_dt), so the two X halves of a Strang step of dt = mask_dt apply M once. */
+void orc_grid_set_absorber(orc_grid* g, int kind, double mask_dt) {
+  g->abs_kind = kind;
+  g->abs_rate = (kind == 1 && mask_dt > 0.0) ? 1.0 / mask_dt : 0.0;
 }
 
 /* coords.h:132-138 */
@@ -323,6 +337,12 @@ static inline double absorb(const orc_grid* g, double delta, const long* nodes_i
     if (!(nodes[d] < 0)) all_neg = 0;
   }
   if (all_neg) return 1.0;
+  if (g->abs_kind == 1) { /* cos^(1/8) mask to the power delta / mask_dt */
+    double lsum = 0.0;
+    for (int d = 0; d < g->dim; ++d)
+      if (nodes[d] > 0) lsum += log(cos(1.5707963267948966 * ((double)nodes[d] / (double)g->nCAP)));
+    return exp(delta * g->abs_rate * 0.125 * lsum);
+  }
   long s = 0;
   for (int d = g->dim - 1; d >= 0; --d) {
     long v = nodes[d] > 0 ? nodes[d] * (nodes[d] * (nodes[d] * nodes[d])) : 0;

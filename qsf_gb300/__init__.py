@@ -6,7 +6,7 @@ propagator / field / coupling vocabulary.  There is no CPU fallback: importing t
 grid classes requires the built library.
 """
 from ._lib import QsfError, lib  # noqa: F401
-from .grid import (BORDERS, Batch, Grid, MODE_IM, MODE_RE, OBS_EKIN, OBS_EPOT, OBS_FLUX, OBS_NORM, OP_IDENTITY,  # noqa: F401
+from .grid import (ABS_CAP, ABS_COS8, BORDERS, Batch, Grid, MODE_IM, MODE_RE, OBS_EKIN, OBS_EPOT, OBS_FLUX, OBS_NORM, OP_IDENTITY,  # noqa: F401
                    OP_KINETIC, OP_POTENTIAL, POT_COULOMB, POT_EBERLY, POT_ECKHARDT_SACHA, POT_NONE, REP_P, REP_X,
                    ZOA_FLUX_2D, ZOA_FLUX_2D_SIMPLE, ZOA_FLUX_3D, fft_radices)
 from .physics import (AXIS_X, AXIS_Y, AXIS_Z, GAUGE_LENGTH, GAUGE_VELOCITY, PULSE_CHEMPHYS, PULSE_CONST,  # noqa: F401

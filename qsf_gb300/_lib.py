@@ -39,6 +39,8 @@ class GridDesc(ctypes.Structure):
         ("border_nodes", ctypes.c_int64 * 4),
         ("free_axes", ctypes.c_int),
         ("multi_region", ctypes.c_int),
+        ("absorber", ctypes.c_int),
+        ("mask_dt", ctypes.c_double),
     ]
 
 

@@ -724,6 +724,9 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   if (d->multi_region != 0 && d->multi_region != 1) return fail(QSF_EINVAL, "multi_region must be 0 or 1");
   if (d->free_axes < 0 || d->free_axes >= (1 << d->dim) || (d->free_axes && !d->multi_region))
     return fail(QSF_EINVAL, "free_axes must be a mask of the grid's axes, on a multi-region grid");
+  if (d->absorber != QSF_ABS_CAP && d->absorber != QSF_ABS_COS8) return fail(QSF_EINVAL, "unknown absorber");
+  if (d->absorber == QSF_ABS_COS8 && (d->nCAP < 1 || 2 * d->nCAP > d->n[0] || !(d->mask_dt > 0) || d->multi_region))
+    return fail(QSF_EINVAL, "the cos^(1/8) mask needs 1 <= nCAP <= n / 2, mask_dt > 0 and a single-region grid");
   if (d->multi_region) {
     // multigrid.h:19 (an absorber is required); partial potentials exist for the
     // reduced-dimensionality interactions (potential.h:144-178)
@@ -824,6 +827,8 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   G.p_swap = d->p_axis_swap ? 1 : 0;
   G.free_mask = d->free_axes;
   G.multi = d->multi_region;
+  G.abs_kind = d->absorber;
+  G.abs_rate = d->absorber == QSF_ABS_COS8 ? 1.0 / d->mask_dt : 0.0;
   if (d->border_nodes[0] > 0) g->bn.NS = d->border_nodes[0];
   if (d->border_nodes[1] > 0) g->bn.SD = d->border_nodes[1];
   if (d->border_nodes[2] > 0) g->bn.DT = d->border_nodes[2];

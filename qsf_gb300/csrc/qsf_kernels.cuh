@@ -77,6 +77,8 @@ struct GridDev {
   int gauge, n_fields, p_swap;
   int free_mask;  // region of a multi-region grid: axes kept in momentum space (bit d)
   int multi;      // multi-region grid: partial potentials, no absorber in evolve
+  int abs_kind;     // QSF_ABS_CAP or QSF_ABS_COS8
+  double abs_rate;  // cos^(1/8) mask: applications per unit time (1 / mask_dt)
   double2* psi;
 };
 
@@ -263,6 +265,12 @@ __device__ __forceinline__ double absorb_at(const GridDev& g, double delta, cons
     if (!(nodes[d] < 0)) all_neg = false;
   }
   if (all_neg) return 1.0;
+  if (g.abs_kind == 1) {  // cos^(1/8) mask M = prod_d cos(pi/2 nodes_d / nCAP)^(1/8), to the power delta / mask_dt
+    double lsum = 0.0;
+    for (int d = 0; d < g.dim; ++d)
+      if (nodes[d] > 0) lsum += log(cos(1.5707963267948966 * ((double)nodes[d] / (double)g.nCAP)));
+    return exp(delta * g.abs_rate * 0.125 * lsum);
+  }
   long long s = 0;
   for (int d = g.dim - 1; d >= 0; --d) {
     const long long v = nodes[d] > 0 ? nodes[d] * (nodes[d] * (nodes[d] * nodes[d])) : 0;

@@ -87,7 +87,7 @@ bool same_grid(const qsf_grid_desc& a, const qsf_grid_desc& b) {
   if (a.dim != b.dim || a.nCAP != b.nCAP || a.potential != b.potential || a.gauge != b.gauge ||
       a.n_fields != b.n_fields || a.p_axis_swap != b.p_axis_swap || a.Ncharge != b.Ncharge ||
       a.Echarge != b.Echarge || a.Nsoft != b.Nsoft || a.Esoft != b.Esoft || a.free_axes != b.free_axes ||
-      a.multi_region != b.multi_region)
+      a.multi_region != b.multi_region || a.absorber != b.absorber || a.mask_dt != b.mask_dt)
     return false;
   for (int k = 0; k < a.dim; ++k)
     if (a.n[k] != b.n[k] || a.dx[k] != b.dx[k]) return false;

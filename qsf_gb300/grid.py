@@ -17,6 +17,7 @@ MODE_IM, MODE_RE = 1, 2
 REP_X, REP_P = 1, 2
 OP_IDENTITY, OP_POTENTIAL, OP_KINETIC = 0, 1, 2
 POT_EBERLY, POT_ECKHARDT_SACHA, POT_COULOMB, POT_NONE = 0, 1, 2, 3
+ABS_CAP, ABS_COS8 = 0, 1  # QSF_ABS_*: the reference's quartic CAP, the cos^(1/8) mask
 OBS_NORM, OBS_EPOT, OBS_EKIN, OBS_FLUX = 1, 2, 4, 8
 PSI_EXT = ".psi"  # io.h:25
 
@@ -38,7 +39,8 @@ class Grid:
     def __init__(self, dim: int, n, dx, nCAP: int = 0, potential: int = POT_EBERLY, Ncharge: float = 1.0,
                  Echarge: float = -1.0, Nsoft: float = 1.0, Esoft: float = 1.0, gauge: int = 0,
                  n_fields: int = 0, p_axis_swap: Optional[bool] = None, border_nodes=(25, 14, 10, 40),
-                 stream: Optional[int] = None, free_axes: int = 0, multi_region: bool = False):
+                 stream: Optional[int] = None, free_axes: int = 0, multi_region: bool = False,
+                 absorber: int = ABS_CAP, mask_dt: float = 0.0):
         n = [int(n)] * dim if np.isscalar(n) else [int(v) for v in n]
         dx = [float(dx)] * dim if np.isscalar(dx) else [float(v) for v in dx]
         d = GridDesc()
@@ -56,6 +58,8 @@ class Grid:
         d.p_axis_swap = int(p_axis_swap)
         d.free_axes = int(free_axes)
         d.multi_region = int(bool(multi_region))
+        d.absorber = int(absorber)
+        d.mask_dt = float(mask_dt)
         self.free_axes = int(free_axes)
         for k in range(4):
             d.border_nodes[k] = int(border_nodes[k])

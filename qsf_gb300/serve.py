@@ -17,7 +17,8 @@ from .grid import BORDERS, OBS_FLUX, OBS_NORM, POT_EBERLY
 
 def grid_desc(dim: int, n, dx, nCAP: int = 0, potential: int = POT_EBERLY, Ncharge: float = 1.0,
               Echarge: float = -1.0, Nsoft: float = 1.0, Esoft: float = 1.0, gauge: int = 0, n_fields: int = 0,
-              p_axis_swap: Optional[bool] = None, border_nodes=(25, 14, 10, 40)) -> GridDesc:
+              p_axis_swap: Optional[bool] = None, border_nodes=(25, 14, 10, 40), absorber: int = 0,
+              mask_dt: float = 0.0) -> GridDesc:
     n = [int(n)] * dim if np.isscalar(n) else [int(v) for v in n]
     dx = [float(dx)] * dim if np.isscalar(dx) else [float(v) for v in dx]
     d = GridDesc()
@@ -33,6 +34,8 @@ def grid_desc(dim: int, n, dx, nCAP: int = 0, potential: int = POT_EBERLY, Nchar
     d.p_axis_swap = int(dim >= 2 if p_axis_swap is None else p_axis_swap)
     for k in range(4):
         d.border_nodes[k] = int(border_nodes[k])
+    d.absorber = int(absorber)
+    d.mask_dt = float(mask_dt)
     return d
 
 
