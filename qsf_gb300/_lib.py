@@ -9,7 +9,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libqsfgpu.so")
+# QSF_LIB selects another build of the library (the autotuner's candidate builds under
+# qsf_gb300/_build/); by default the in-tree qsf_gb300/libqsfgpu.so
+LIB_PATH = os.environ.get("QSF_LIB") or os.path.join(HERE, "libqsfgpu.so")
 
 QSF_OK = 0
 ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ETIMEDOUT", 5: "ENUMERIC", 6: "ESTATE", 7: "EBUSY"}

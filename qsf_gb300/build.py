@@ -34,8 +34,14 @@ def _newest(paths) -> float:
     return max((os.path.getmtime(p) for p in paths), default=0.0)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-    os.makedirs(OUT, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, defines=(), tag: str = "") -> str:
+    """Compile and link; returns the library path.  `defines` (NAME=VALUE strings) and a
+    `tag` give a variant build in qsf_gb300/_build/<tag>/ (the autotuner's candidates);
+    the default build is qsf_gb300/libqsfgpu.so."""
+    out = os.path.join(OUT, tag) if tag else OUT
+    lib_path = os.path.join(out, "libqsfgpu.so") if tag else LIB
+    os.makedirs(out, exist_ok=True)
+    extra = ["-D" + d for d in defines]
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
         glob.glob(os.path.join(ROOT, "include", "*.h"))
@@ -43,10 +49,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     nvcc = _nvcc()
 
     def compile_one(src):
-        obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(out, os.path.basename(src)[:-3] + ".o")
         if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), hdr_time):
             return obj
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
@@ -56,13 +62,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, sources))
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
-        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
+    if force or not os.path.exists(lib_path) or os.path.getmtime(lib_path) < _newest(objs):
+        cmd = [nvcc] + ARCH + ["-shared", "-o", lib_path + ".tmp"] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
-        os.replace(LIB + ".tmp", LIB)
-    return LIB
+        os.replace(lib_path + ".tmp", lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

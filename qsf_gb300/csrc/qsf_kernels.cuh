@@ -34,16 +34,20 @@
 #pragma once
 #include "qsf_fft.cuh"
 #include "qsf_fxfft.cuh"
+#include "qsf_tuning.h"
 
 namespace qsf {
 
 constexpr int kMaxDim = 3;
 // Threads per block of the row / axis passes (tiles of 4096 points): 512 threads with
-// radix-8 plans (8 points per thread, twice the resident warps) for the line lengths
-// where that measured faster (384, 512, 2048: their radix-16 plans end in short
-// passes), 256 threads with radix-16 plans otherwise (256 included: its 3D cube loses
-// more than its 2D grid gains).
-__host__ __device__ constexpr int row_threads(int n) { return (n == 384 || n == 512 || n == 2048) ? 512 : 256; }
+// radix-8 plans (8 points per thread, twice the resident warps) or 256 threads with
+// radix-16 plans, per line length as the autotuner measured (qsf_tuning.h).  The
+// autotuner's candidate builds define QSF_ROW_THREADS to force one count everywhere.
+#ifdef QSF_ROW_THREADS
+__host__ __device__ constexpr int row_threads(int) { return QSF_ROW_THREADS; }
+#else
+__host__ __device__ constexpr int row_threads(int n) { return tuned_row_threads(n); }
+#endif
 __host__ __device__ constexpr int row_ppt(int n) { return 4096 / row_threads(n); }
 // Points per thread of the one-CTA line kernel (512 threads, one line of n points): a
 // line shorter than 8192 points leaves threads idle in radix-16 passes, and with one
