@@ -155,6 +155,8 @@ struct StepDev {
 };
 
 __device__ __forceinline__ bool step_active(const StepDev& S) { return S.ctl[0] <= S.ctl[1] && S.ctl[0] < S.nsteps; }
+// hint: move the 128-byte line holding p from DRAM into L2 (p must be in an allocation)
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 __device__ __forceinline__ bool pass_active(const StepDev& S) { return S.ctl[5] <= S.ctl[1] && S.ctl[5] < S.nsteps; }
 
 // ------------------------------------------------------------ reductions
@@ -987,6 +989,15 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
   const int Lh = (int)min((long long)L, g.m / N - row0);
   const long long base = row0 * N;
   const int cnt = Lh * N;
+  // 3D: the sweep after the inverse transform reads this block's slice of the X table
+  // (16 B per point) and of the potential (8 B per point, E_pot): start moving it into
+  // L2 now, one prefetch per 128-byte line, so that those loads do not wait on DRAM
+  // (256^3 step 2.11 -> 2.08 ms; no gain for the 2D passes, so they skip it)
+  if (g.dim == 3) {
+    for (int e = threadIdx.x * 8; e < cnt; e += blockDim.x * 8) prefetch_l2(S.xs + base + e);
+    if (S.obs & 2u)
+      for (int e = threadIdx.x * 16; e < cnt; e += blockDim.x * 16) prefetch_l2(S.Vx + base + e);
+  }
   int bits = 0;
   // producer of element (row, j): axis-0 tile j / C (2D) or axis-1 tile (i0, j / C) (3D,
   // when the block's rows share i0)
