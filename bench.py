@@ -168,8 +168,10 @@ def _ncu_traffic(kernel_kind):
 
 
 # ------------------------------------------------------------------ CPU legs
-def _oracle_sample(nsteps):
-    """Time `nsteps` steps of the CPU oracle (C restatement) on the full workload."""
+def _oracle_sample(nsteps, barrier=None):
+    """Time `nsteps` steps of the CPU oracle (C restatement) on the full workload; the
+    grid, its tables and the start state are built before the timed region.  Returns
+    (seconds, monotonic start, monotonic end)."""
     from oracle import oracle as O
     O.set_border_nodes(25, 14, 10, 40)
     pa = _pulse_args()
@@ -177,40 +179,55 @@ def _oracle_sample(nsteps):
     g = O.Grid(2, N_EDGE, DX, nCAP=NCAP, Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT, Esoft=ESOFT, coupling=c)
     g.psi[...] = _initial_psi()
     prop = O.Propagator(O.MODE_RE, DT, 0, g, ["norm", "epot", ("flux", O.ZOA_FLUX_2D, 0)])
-    t0 = time.perf_counter()
+    prop.make_step()  # untimed: first-touch of every table
+    prop.compute_each()
+    if barrier is not None:
+        barrier.wait()
+    t0 = time.monotonic()
     for _ in range(nsteps):
         prop.make_step()
         prop.compute_each()
-    return time.perf_counter() - t0
+    t1 = time.monotonic()
+    return t1 - t0, t0, t1
 
 
-def _cpu_worker(args):
-    nsteps = args
-    return _oracle_sample(nsteps)
+_BARRIER = None
+
+
+def _cpu_init(barrier):
+    global _BARRIER
+    _BARRIER = barrier
+
+
+def _cpu_worker(nsteps):
+    return _oracle_sample(nsteps, _BARRIER)
 
 
 def cpu_baseline(all_cores: bool, budget_s: float = 20.0):
     """The oracle port timed on host cores over a bounded sample of the workload."""
     from oracle import oracle as O
     O.build()
-    t1 = _oracle_sample(1)
+    t1 = _oracle_sample(1)[0]
     nsteps = max(1, min(8, int(budget_s / max(t1, 1e-3))))
     m = N_EDGE * N_EDGE
+    what = ("the reference's split step as the oracle restates it (oracle/qsf_oracle.c, gcc -O2, its own FP64 "
+            "mixed-radix FFT in place of FFTW, which neither machine has)")
     if not all_cores:
-        t = _oracle_sample(nsteps)
+        t = _oracle_sample(nsteps)[0]
         return {"value": m * nsteps / t, "unit": UNIT, "cores": 1, "kind": "port",
                 "sample": f"{nsteps} Strang steps of the 2048^2 workload (norm, E_pot, 7 ZOA_FLUX_2D fluxes) "
-                          f"on one core, after one untimed step"}
+                          f"on one core, after one untimed step; {what}"}
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        t0 = time.perf_counter()
-        pool.map(_cpu_worker, [nsteps] * cores)
-        wall = time.perf_counter() - t0
+    barrier = ctx.Barrier(cores)
+    with ctx.Pool(cores, initializer=_cpu_init, initargs=(barrier,)) as pool:
+        res = pool.map(_cpu_worker, [nsteps] * cores)
+    wall = max(r[2] for r in res) - min(r[1] for r in res)
     return {"value": m * nsteps * cores / wall, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{cores} independent single-core replicas x {nsteps} Strang steps of the 2048^2 workload "
-                      f"(wall clock incl. process start)"}
+            "sample": f"{cores} independent single-core replicas x {nsteps} Strang steps of the 2048^2 workload, "
+                      f"started together after their set-up; wall clock from the first replica's first timed "
+                      f"step to the last one's end (process start, grid and table set-up excluded); {what}"}
 
 
 # ------------------------------------------------------------------ batched / served
@@ -237,16 +254,38 @@ def _schedule(Q, dim, inten, lam, ncycles, nsteps):
     return coupling_schedule(c, DT, nsteps)[0]
 
 
-def run_batched(steps, warmup, nsolves=256, seed=0):
-    """256 independent 2-electron solves, edges uniform over {256..1024}, intensity
-    log-uniform 1e14-1e15 W/cm^2, wavelength uniform 400-1600 nm, 3-cycle sin^2, VG,
-    advanced together through qsf_batch; grid-point-steps/s over `steps` steps."""
-    import torch
-    import qsf_gb300 as Q
+def batch_specs(nsolves=256, seed=0):
+    """The batched workload's solve list: (edge, intensity W/cm^2, wavelength nm) per
+    solve, edges uniform over {256..1024}, intensity log-uniform 1e14-1e15, wavelength
+    uniform 400-1600 nm (numpy PCG64, seed 0)."""
     rng = np.random.default_rng(seed)
     edges = rng.choice(BATCH_EDGES, nsolves)
     inten = 10.0 ** rng.uniform(14.0, 15.0, nsolves)
     lam = rng.uniform(400.0, 1600.0, nsolves)
+    return [(int(e), float(i), float(l)) for e, i, l in zip(edges, inten, lam)]
+
+
+def batch_share(specs, steps, world_size, rank):
+    """Indices of the solves this rank runs: shard.partition on grid points x steps
+    (every rank computes the same split; no communication)."""
+    from qsf_gb300 import shard
+    return shard.my_share([shard.cost(e * e, steps) for e, _, _ in specs], world_size, rank)
+
+
+def run_batched(steps, warmup, nsolves=256, seed=0, plain_arm=True, ws=1, rank=0):
+    """256 independent 2-electron solves, edges uniform over {256..1024}, intensity
+    log-uniform 1e14-1e15 W/cm^2, wavelength uniform 400-1600 nm, 3-cycle sin^2, VG,
+    advanced together through qsf_batch; grid-point-steps/s over `steps` steps.  With
+    several ranks each rank runs its share of the solve list (weak in the solves per
+    GPU only through the split: the list is fixed) and `value` is the sum over ranks
+    divided by the slowest rank's time."""
+    import torch
+    import qsf_gb300 as Q
+    specs = batch_specs(nsolves, seed)
+    mine = batch_share(specs, warmup + steps, ws, rank)
+    edges = [specs[i][0] for i in mine]
+    inten = [specs[i][1] for i in mine]
+    lam = [specs[i][2] for i in mine]
     stream = torch.cuda.Stream()
     batch = Q.Batch(stream=stream.cuda_stream)
     grids, states = [], {}
@@ -255,7 +294,7 @@ def run_batched(steps, warmup, nsolves=256, seed=0):
     for e, I, L in zip(edges, inten, lam):
         e = int(e)
         g = Q.Grid(2, e, DX, nCAP=e // 10, potential=Q.POT_EBERLY, Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT,
-                   Esoft=ESOFT, gauge=Q.GAUGE_VELOCITY, n_fields=1)
+                   Esoft=ESOFT, gauge=Q.GAUGE_VELOCITY, n_fields=1, stream=stream.cuda_stream)
         if e not in states:
             states[e] = _gauss_state(2, e, DX)
         g.upload(states[e])
@@ -265,27 +304,56 @@ def run_batched(steps, warmup, nsolves=256, seed=0):
         m_sum += e * e
     batch.run(warmup)
     torch.cuda.synchronize()
+    _barrier(ws)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
     batch.run(steps)
     b.record(stream)
     torch.cuda.synchronize()
-    ms = a.elapsed_time(b)
+    ms = _max_over_ranks(ws, a.elapsed_time(b))
     batch.close()
-    return {"value": m_sum * steps / (ms / 1e3), "unit": UNIT, "solves": nsolves, "steps": steps,
-            "ms_per_step": ms / steps, "grid_points": int(m_sum),
-            "workload": "batched: 256 2D solves, edges U{256,384,512,768,1024}, I log-U[1e14,1e15], "
-                        "lambda U[400,1600] nm, 3-cycle sin^2 VG, norm+E_pot+ZOA_FLUX_2D every step, seed 0"}
+    m_all = _sum_over_ranks(ws, float(m_sum))
+    out = {"value": m_all * steps / (ms / 1e3), "unit": UNIT, "solves": nsolves, "steps": steps,
+           "ms_per_step": ms / steps, "grid_points": int(m_all), "solves_this_rank": len(mine),
+           "workload": "batched: 256 2D solves, edges U{256,384,512,768,1024}, I log-U[1e14,1e15], "
+                       "lambda U[400,1600] nm, 3-cycle sin^2 VG, norm+E_pot+ZOA_FLUX_2D every step, seed 0"}
+    if plain_arm:
+        # the same solves one after another through the plain single-solve path (qsf_step,
+        # one call of `steps` steps per solve, graph-replayed), after one untimed call of
+        # `warmup` steps per solve; all grids share one stream, timed with CUDA events
+        for g, e, I, L in zip(grids, edges, inten, lam):
+            g.upload(states[int(e)])
+        scheds = [_schedule(Q, 2, I, L, NCYCLES, total) for I, L in zip(inten, lam)]
+        for g, sc in zip(grids, scheds):
+            g.step(Q.MODE_RE, DT, warmup, sc[:warmup], obs=Q.OBS_NORM | Q.OBS_EPOT, borders=Q.ZOA_FLUX_2D)
+        torch.cuda.synchronize()
+        _barrier(ws)
+        a.record(stream)
+        for g, sc in zip(grids, scheds):
+            g.step(Q.MODE_RE, DT, steps, sc[warmup:], obs=Q.OBS_NORM | Q.OBS_EPOT, borders=Q.ZOA_FLUX_2D)
+        b.record(stream)
+        torch.cuda.synchronize()
+        pms = _max_over_ranks(ws, a.elapsed_time(b))
+        out["plain_same_solves"] = {
+            "value": m_all * steps / (pms / 1e3), "unit": UNIT, "ms_per_step_all_solves": pms / steps,
+            "method": "each of the 256 solves alone through qsf_step (one call of the timed steps per solve), "
+                      "one after another on one stream"}
+        out["batched_vs_plain_same_solves"] = out["value"] / out["plain_same_solves"]["value"]
+    for g in grids:
+        g.close()
+    return out
 
 
-def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, steps_per_round=16):
+def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, steps_per_round=16, ws=1, rank=0):
     """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N in 1024..16384) and 2D
     (edge in 256..1024) solves with seeded pulses; each solve runs its first
-    `steps_per_solve` steps.  Returns throughput and p50/p99 submit->completion."""
+    `steps_per_solve` steps.  Returns throughput and p50/p99 submit->completion.  With
+    several ranks every rank follows the same seeded stream and serves the requests
+    shard.StreamAssigner gives it (serve.ShardedServer)."""
     import qsf_gb300 as Q
     from qsf_gb300 import serve as S
     rng = np.random.default_rng(seed)
-    srv = S.Server(max_slots=max_slots, hbm_reserve_gb=16.0, steps_per_round=steps_per_round)
+    srv = S.ShardedServer(rank, ws, max_slots=max_slots, hbm_reserve_gb=16.0, steps_per_round=steps_per_round)
     tickets, pts = [], 0.0
     t0 = time.perf_counter()
     t_next = t0
@@ -309,20 +377,29 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, ste
             states[key] = _gauss_state(dim, n, dx)
         borders = ["BOX"] if dim == 1 else Q.ZOA_FLUX_2D
         box = int(0.4 * n) if dim == 1 else 0
-        tickets.append(srv.submit(gd, Q.MODE_RE, DT, steps_per_solve,
-                                  _schedule(Q, dim, inten, lam, NCYCLES, steps_per_solve), psi0=states[key],
-                                  obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box))
-        pts += float(n ** dim) * steps_per_solve
+        t = srv.submit(gd, Q.MODE_RE, DT, steps_per_solve, coupling=_schedule(Q, dim, inten, lam, NCYCLES,
+                                                                              steps_per_solve),
+                       psi0=states[key], obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box)
+        if t is not None:
+            tickets.append(t)
+            pts += float(n ** dim) * steps_per_solve
     lat = []
     for t in tickets:
         r = srv.wait(t, 3600)
         if r["status"] == 0:
             lat.append(r["latency_s"])
-    wall = time.perf_counter() - t0
+    wall = _max_over_ranks(ws, time.perf_counter() - t0)
     srv.stop()
+    pts = _sum_over_ranks(ws, pts)
+    if ws > 1:  # latencies of every rank's solves
+        import torch.distributed as dist
+        allv = [None] * ws
+        dist.all_gather_object(allv, lat)
+        lat = [v for part in allv for v in part]
     lat.sort()
     pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
-    return {"rate_per_s": rate, "submitted": len(tickets), "completed": len(lat), "value": pts / wall, "unit": UNIT,
+    return {"rate_per_s": rate, "submitted": _sum_over_ranks(ws, len(tickets)), "completed": len(lat),
+            "value": pts / wall, "unit": UNIT,
             "p50_s": pct(0.50), "p99_s": pct(0.99), "wall_s": wall,
             "workload": f"served: Poisson {rate}/s for {duration_s}s, 50/50 1D N in [1024,16384] / 2D edge in "
                         f"[256,1024] (2^a 3^b 5^c sizes), I log-U[1e14,1e15], lambda U[400,1600] nm, "
@@ -389,6 +466,112 @@ def run_multigrid(steps, warmup, cpu=True):
                                          f"(oracle, one core)"}
     mg.close()
     return out
+
+
+def _timed_steps(Q, grid, stream, mode, dt, steps, warmup, sched, obs, borders, box, flush):
+    """One warm-up call, then one call of `steps` graph-replayed steps timed with CUDA
+    events on the grid's stream (L2 flushed before it); then a profiled call of the
+    same steps for the per-kernel split.  Returns (ms per step, {kind: (ms, launches)})."""
+    import torch
+    grid.step(mode, dt, warmup, sched[:warmup], obs=obs, borders=borders, box_size=box)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        flush.zero_()
+        e0.record(stream)
+        grid.step(mode, dt, steps, sched[warmup:warmup + steps], obs=obs, borders=borders, box_size=box)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    prof = {}
+    with torch.cuda.stream(stream):
+        flush.zero_()
+        grid.step(mode, dt, steps, sched[warmup:warmup + steps], obs=obs, borders=borders, box_size=box,
+                  profile=prof)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, {k: v for k, v in prof.items() if v[1] > 0}
+
+
+def _roofline(bytes_per_pt_step, m, steps, prof, note):
+    peak, peak_kind = _peaks()
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms = prof[dom][0] / prof[dom][1]
+    # bytes per launch of the dominant kernel: one pass over psi (32 B per point), or the
+    # whole step's psi traffic for a one-kernel 1D step
+    per_launch = (32 if bytes_per_pt_step > 32 else bytes_per_pt_step) * m
+    ach = per_launch / (dom_ms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "traffic": None, "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": per_launch,
+            "avg_launch_ms": dom_ms, "note": note}
+
+
+def run_c1(steps, warmup, flush):
+    """The 1D plain configuration: 4096 points, dx 0.2, soft-core H, length gauge,
+    2-cycle 800 nm 1e14 W/cm^2 pulse, cos^(1/8) mask on the outer 10%, norm + E_pot +
+    BOX flux every step.  Step timing of the real-time propagation, plus the wall time
+    of the whole job as a user runs it (2000 imaginary-time steps with Normalize, then
+    the full real-time run) through SplitPropagator."""
+    import torch
+    import qsf_gb300 as Q
+    n, dx, ncap, box = 4096, 0.2, 410, 1638
+    stream = torch.cuda.Stream()
+    common = dict(nCAP=ncap, potential=Q.POT_EBERLY, Ncharge=1.0, Echarge=-1.0, Nsoft=1.0, absorber=Q.ABS_COS8,
+                  mask_dt=DT, stream=stream.cuda_stream)
+    pulse = dict(field=Q.field_from_intensity(1e14), omega=Q.omega_from_wavelength(800.0), ncycles=2.0)
+    t0 = time.perf_counter()
+    gi = Q.Grid(1, n, dx, gauge=Q.GAUGE_VELOCITY, n_fields=0, **common)
+    gi.add_gaussian(0.0, 1.0)
+    Q.SplitPropagator(Q.MODE_IM, 0.01, 2000, gi, Q.Coupling(Q.GAUGE_VELOCITY),
+                      ["step", "norm", "normalize", "epot", "etot", "ediff"]).run()
+    psi0 = gi.download()
+    gr = Q.Grid(1, n, dx, gauge=Q.GAUGE_LENGTH, n_fields=1, **common)
+    gr.upload(psi0)
+    c = Q.Coupling(Q.GAUGE_LENGTH, [Q.Field(1, [Q.Pulse(**pulse)])])
+    prop = Q.SplitPropagator(Q.MODE_RE, DT, 0, gr, c, ["step", "time", "norm", "epot", ("flux", ["BOX"], box)])
+    rows = prop.run()
+    torch.cuda.synchronize()
+    job_s = time.perf_counter() - t0
+    gr.upload(psi0)
+    from qsf_gb300.propagator import coupling_schedule
+    sched, _ = coupling_schedule(Q.Coupling(Q.GAUGE_LENGTH, [Q.Field(1, [Q.Pulse(**pulse)])]), DT, warmup + steps)
+    ms, prof = _timed_steps(Q, gr, stream, Q.MODE_RE, DT, steps, warmup, sched, Q.OBS_NORM | Q.OBS_EPOT, ["BOX"],
+                            box, flush)
+    value = n * 1000.0 / ms
+    return {"value": value, "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "roofline": _roofline(32, n, steps, prof, "1D: the line is held on chip for the whole step (one "
+                                  "pass, 32 B per point-step); latency-bound on one SM, not HBM-bound"),
+            "kernels_ms_per_step": {k: v[0] / steps for k, v in prof.items()},
+            "job_s": job_s, "job_steps": 2000 + len(rows) - 1,
+            "yield_1_minus_norm": 1.0 - rows[-1]["norm"],
+            "workload": "1D plain: 4096 points, dx 0.2, soft-core H (e-n charge 1, eps 1), IM ground state "
+                        "(dt 0.01, 2000 steps) then RE dt 0.05, LG 2-cycle sin^2 800 nm 1e14 W/cm^2, cos^(1/8) "
+                        "mask on the outer 10%, norm + E_pot + BOX flux every step"}
+
+
+def run_c4(steps, warmup, flush):
+    """The 3D plain configuration: 256^3, dx 0.4, three electrons (e-n charge 3, all
+    e-e pairs), length gauge, 2-cycle 800 nm 1e15 W/cm^2, CAP over 26 nodes, norm +
+    E_pot + the eight ZOA_FLUX_3D fluxes every step."""
+    import torch
+    import qsf_gb300 as Q
+    n, dx, ncap = 256, 0.4, 26
+    stream = torch.cuda.Stream()
+    g = Q.Grid(3, n, dx, nCAP=ncap, potential=Q.POT_EBERLY, Ncharge=3.0, gauge=Q.GAUGE_LENGTH, n_fields=1,
+               stream=stream.cuda_stream)
+    g.upload(_gauss_state(3, n, dx))
+    c = Q.Coupling(Q.GAUGE_LENGTH, [Q.Field(7, [Q.Pulse(field=Q.field_from_intensity(1e15),
+                                                        omega=Q.omega_from_wavelength(800.0), ncycles=2.0)])])
+    prop = Q.SplitPropagator(Q.MODE_RE, DT, 0, g, c, ["norm", "epot", ("flux", Q.ZOA_FLUX_3D, 0)])
+    sched = prop._schedule(warmup + steps)
+    ms, prof = _timed_steps(Q, g, stream, Q.MODE_RE, DT, steps, warmup, sched, Q.OBS_NORM | Q.OBS_EPOT,
+                            Q.ZOA_FLUX_3D, 0, flush)
+    m = n ** 3
+    g.close()
+    return {"value": m * 1000.0 / ms, "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "roofline": _roofline(128, m, steps, prof, "3D: 4 passes over psi per step (128 B per point-step)"),
+            "hbm_gbs_step": 128 * m * 1000.0 / ms / 1e9,
+            "kernels_ms_per_step": {k: v[0] / steps for k, v in prof.items()},
+            "workload": "3D plain: 256^3, dx 0.4, 3 electrons (e-n charge 3, all e-e pairs), LG 2-cycle sin^2 "
+                        "800 nm 1e15 W/cm^2, CAP 26 nodes, norm + E_pot + ZOA_FLUX_3D every step"}
 
 
 def run_gpu(args):
@@ -473,9 +656,11 @@ def run_gpu(args):
     # step) once
     launches = sum(v[1] for v in kinds.values()) - max(0, kinds.get("row_open", (0.0, 1))[1] - 1)
 
-    batched = run_batched(steps=20, warmup=3)
-    served = run_served(rate=100.0, duration_s=3.0)
+    batched = run_batched(steps=20, warmup=3, ws=ws, rank=rank)
+    served = [run_served(rate=r, duration_s=2.0, ws=ws, rank=rank) for r in (10.0, 100.0, 1000.0)]
     multigrid = run_multigrid(steps=20, warmup=3, cpu=rank == 0)
+    c1 = run_c1(steps=max(args.steps, 200), warmup=args.warmup, flush=flush)
+    c4 = run_c4(steps=max(args.steps, 10), warmup=args.warmup, flush=flush)
 
     if rank == 0:
         cpu = cpu_baseline(all_cores=False)
@@ -503,7 +688,10 @@ def run_gpu(args):
             "batched": batched,
             "served": served,
             "multigrid": multigrid,
-            "batched_vs_plain": batched["value"] / value * ws,
+            "c1": c1,
+            "c4": c4,
+            "batched_vs_plain": batched["value"] / value,
+            "batched_vs_plain_same_solves": batched.get("batched_vs_plain_same_solves"),
         }
         print(json.dumps(line))
     if ws > 1:

@@ -41,6 +41,7 @@ extern "C" {
 #define QSF_ENUMERIC 5   /* NaN/Inf or a non-positive norm in a reduction           */
 #define QSF_ESTATE 6     /* call not valid in the handle's current state            */
 #define QSF_EBUSY 7      /* admission refused (no slot or not enough free HBM)      */
+#define QSF_ECANCELED 8  /* a served request was cancelled (qsf_server_cancel)      */
 
 /* ------------------------------------------------------ reference enums */
 /* MODE (basics/enums.h:15-21), REP (36-42) */
@@ -232,6 +233,14 @@ typedef struct qsf_step_desc {
   float* kernel_ms;
   int64_t* kernel_launches;
   int substeps;             /* MultiProductSplit order K (0 or 1: plain Strang) */
+  /* QSF_OBS_EKIN on every k-th step only (k = ekin_interval; 0 or 1: every step), as
+   * the reference's comp_interval records rows every k steps (wf/buffer.h:6, 391):
+   * E_kin (rows' column 2) is computed at the end of steps k-1, 2k-1, ... of the call
+   * and of its last step, and is 0 in the other rows.  E_kin needs psi_n in memory for
+   * its extra transforms, so those steps end in complex128 while the steps between
+   * them stay in fixed point.  With a convergence threshold in imaginary time the
+   * energy test runs on the steps that have E_kin (E_n minus the previous such E). */
+  int ekin_interval;
 } qsf_step_desc;
 /* kernel kinds of the fused step (for qsf_step_desc.kernel_ms) */
 #define QSF_K_TABLES 0
@@ -262,9 +271,12 @@ int qsf_batch_destroy(qsf_batch* b);
 int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot);
 /* Removes a member; applies its pending Normalize factor first. */
 int qsf_batch_remove(qsf_batch* b, int64_t slot);
-/* Advances every member by up to `steps` steps; *active = members with steps left. */
+/* Advances every member by up to `steps` steps; *active = members with steps left.
+ * Returns QSF_ENUMERIC when any member's wavefunction held an Inf / NaN or its norm
+ * became non-positive (the other members are unaffected: qsf_batch_result says which). */
 int qsf_batch_run(qsf_batch* b, int64_t steps, int64_t* active);
-/* Observables rows (nsteps x (3 + nborders)) and steps done of one member. */
+/* Observables rows (nsteps x (3 + nborders)) and steps done of one member; returns
+ * QSF_ENUMERIC (rows still filled) for a member flagged as above. */
 int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_done);
 
 /* -------------------------------------------------------------- serving */
@@ -313,10 +325,24 @@ typedef struct qsf_server_stats {
 typedef struct qsf_server qsf_server;
 int qsf_server_start(const qsf_server_config* cfg, qsf_server** out);
 int qsf_server_submit(qsf_server* s, const qsf_request* r, int64_t* ticket);
+/* Admission: a request is admitted while a slot is free and its device bytes fit in
+ * the free HBM minus hbm_reserve_gb; one that fits on the device but not now waits in
+ * the queue (requests behind it wait too); one larger than the device's total memory
+ * minus the reserve finishes at once with status QSF_ENOMEM.  A solve whose
+ * wavefunction holds an Inf / NaN (or whose norm turns non-positive) finishes with
+ * QSF_ENUMERIC without affecting the others.
+ * A finished solve's result is handed out once, by qsf_server_poll (done = 1) or
+ * qsf_server_wait, and then forgotten (the server keeps no unbounded result history);
+ * later calls for that ticket see it as unknown (poll: done = 0; wait: timeout). */
 /* non-blocking: *done = 1 and *out filled once the solve has finished */
 int qsf_server_poll(qsf_server* s, int64_t ticket, qsf_result* out, int* done);
 /* bounded wait for one solve; QSF_ETIMEDOUT when timeout_s runs out */
 int qsf_server_wait(qsf_server* s, int64_t ticket, double timeout_s, qsf_result* out);
+/* Cancels a submitted solve: a queued one leaves the queue at once, a running one
+ * leaves the batch after the current round; its result (status QSF_ECANCELED, the
+ * observables of the steps done) is then collected as usual.  QSF_EINVAL for a ticket
+ * that is unknown or already finished. */
+int qsf_server_cancel(qsf_server* s, int64_t ticket);
 int qsf_server_stats_get(qsf_server* s, qsf_server_stats* out);
 /* finishes the solves in flight, drops the queued ones (status QSF_ESTATE), joins */
 int qsf_server_stop(qsf_server* s);

@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("QSF_LIB") or os.path.join(HERE, "libqsfgpu.so")
 
 QSF_OK = 0
-ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ETIMEDOUT", 5: "ENUMERIC", 6: "ESTATE", 7: "EBUSY"}
+ERRORS = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ETIMEDOUT", 5: "ENUMERIC", 6: "ESTATE", 7: "EBUSY",
+          8: "ECANCELED"}
 MAX_BORDERS = 16
 
 
@@ -111,6 +112,7 @@ class StepDesc(ctypes.Structure):
         ("kernel_ms", ctypes.POINTER(ctypes.c_float)),
         ("kernel_launches", ctypes.POINTER(ctypes.c_int64)),
         ("substeps", ctypes.c_int),
+        ("ekin_interval", ctypes.c_int),
     ]
 
 
@@ -174,6 +176,7 @@ def lib():
         "qsf_server_wait": [vp, i64, ctypes.c_double, ctypes.POINTER(Result)],
         "qsf_server_stats_get": [vp, ctypes.POINTER(ServerStats)],
         "qsf_server_stop": [vp],
+        "qsf_server_cancel": [vp, i64],
         "qsf_save": [vp, ctypes.c_char_p, ctypes.POINTER(DumpFormat), ctypes.c_char_p, ctypes.c_char_p,
                      ctypes.c_size_t],
         "qsf_load": [vp, ctypes.c_char_p, ctypes.c_char_p, ip, dp],

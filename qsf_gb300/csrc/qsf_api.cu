@@ -26,6 +26,16 @@ int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+int device_sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 152;
+  if (dev < 64 && cache[dev] > 0) return cache[dev];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+  if (dev < 64) cache[dev] = n;
+  return n;
+}
 }  // namespace qsf
 
 namespace {
@@ -107,7 +117,30 @@ int init_kernel_table() {
 
 int grid_blocks(long long m) {
   long long b = (m + 255) / 256;
-  return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 16);
+  return (int)std::min<long long>(std::max<long long>(b, 1), (long long)device_sm_count() * 16);
+}
+
+// One twiddle as the fixed-point FFT reads it.  With pre-split tables (QSF_TWQ) each
+// component w becomes its signed 32-bit halves {lo = (int)w, hi} (the bytes of an int4
+// {re lo, re hi, im lo, im hi}); a component whose low half would be -2^31 moves one
+// unit (2^-62) so that the kernels can negate the halves.
+longlong2 split_twiddle(longlong2 w) {
+#if QSF_TWQ
+  int q[4];
+  const long long c[2] = {w.x, w.y};
+  for (int k = 0; k < 2; ++k) {
+    long long v = c[k];
+    if ((v & 0xffffffffLL) == 0x80000000LL) v += 1;
+    const int lo = k_lo(v), hi = k_hi(v);
+    q[2 * k] = lo;
+    q[2 * k + 1] = hi;
+  }
+  longlong2 out;
+  std::memcpy(&out, q, sizeof out);
+  return out;
+#else
+  return w;
+#endif
 }
 
 double decode_ordered(long long i) {
@@ -453,6 +486,7 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   if (d->nsteps < 1) return fail(QSF_EINVAL, "nsteps < 1");
   if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
   if (d->substeps < 0 || d->substeps > 64) return fail(QSF_EINVAL, "substeps must be in [0, 64]");
+  if (d->ekin_interval < 0) return fail(QSF_EINVAL, "ekin_interval must be >= 0");
   if (g->G.free_mask)
     return fail(QSF_EINVAL, "a region with free axes keeps them in momentum space: step it with the member operations");
   const GridDev& G = g->G;
@@ -506,8 +540,10 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   for (int ax = 0; ax < 3; ++ax) S.naxblk[ax] = g->ax_blocks[ax];
   S.obs = d->obs | QSF_OBS_NORM;
   if (nb == 0) S.obs &= ~QSF_OBS_FLUX;
-  // steps of a call stay in fixed point between steps unless E_kin needs psi_n in memory
-  S.fused = (G.dim >= 2 && !(S.obs & QSF_OBS_EKIN)) ? 1 : 0;
+  // steps of a call stay in fixed point between steps, except after the steps whose
+  // E_kin needs psi_n in memory (every ekin_interval-th step and the last one)
+  S.fused = G.dim >= 2 ? 1 : 0;
+  S.ekin_every = d->ekin_interval > 1 ? d->ekin_interval : 1;
   S.normalize = d->normalize;
   S.energy_after_normalize = d->energy_after_normalize;
   S.state_accuracy = d->mode == QSF_MODE_IM ? d->state_accuracy : 0.0;
@@ -762,7 +798,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     s *= d->n[k];
   }
   std::map<int64_t, double2*> tws;
-  std::map<int64_t, longlong2*> twxs;
+  std::map<int64_t, longlong2*> twxs, twfs;
   for (int k = 0; k < d->dim; ++k) {
     AxisDev& a = G.ax[k];
     a.n = (int)d->n[k];
@@ -777,7 +813,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     auto it = tws.find(a.n);
     if (it == tws.end()) {
       std::vector<double2> h((size_t)a.n);
-      std::vector<longlong2> hx((size_t)a.n);
+      std::vector<longlong2> hx((size_t)a.n), hf((size_t)a.n);
       const long double twopi = 6.283185307179586476925286766559005768L;
       const long double q62 = 4611686018427387904.0L;
       for (int t = 0; t < a.n; ++t) {
@@ -785,9 +821,10 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
         const long double c = cosl(ang), sn = -sinl(ang);
         h[(size_t)t] = make_double2((double)c, (double)sn);
         hx[(size_t)t] = make_longlong2(llroundl(c * q62), llroundl(sn * q62));
+        hf[(size_t)t] = split_twiddle(hx[(size_t)t]);
       }
       double2* dptr = nullptr;
-      longlong2* xptr = nullptr;
+      longlong2 *xptr = nullptr, *fptr = nullptr;
       if (int rc = dev_alloc(dptr, h.size())) {
         qsf_grid_destroy(g);
         return rc;
@@ -797,17 +834,28 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
         qsf_grid_destroy(g);
         return rc;
       }
+      if (int rc = dev_alloc(fptr, hf.size())) {
+        cudaFree(dptr);
+        cudaFree(xptr);
+        qsf_grid_destroy(g);
+        return rc;
+      }
       cudaMemcpy(dptr, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice);
       cudaMemcpy(xptr, hx.data(), hx.size() * sizeof(longlong2), cudaMemcpyHostToDevice);
+      cudaMemcpy(fptr, hf.data(), hf.size() * sizeof(longlong2), cudaMemcpyHostToDevice);
       g->tw_owned.push_back(dptr);
       g->twx_owned.push_back(xptr);
+      g->twx_owned.push_back(fptr);
       tws[a.n] = dptr;
       twxs[a.n] = xptr;
+      twfs[a.n] = fptr;
       a.tw = dptr;
       a.twx = xptr;
+      a.twf = reinterpret_cast<decltype(a.twf)>(fptr);
     } else {
       a.tw = it->second;
       a.twx = twxs[a.n];
+      a.twf = reinterpret_cast<decltype(a.twf)>(twfs[a.n]);
     }
   }
   G.inv_m = 1.0 / (double)G.m;
@@ -918,6 +966,7 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->obs_log);
   fr(g->vtab);
   fr(g->mtab);
+  for (const qsf_grid::StepGraph& sg : g->step_graphs) cudaGraphExecDestroy(sg.exec);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->fin_fork) cudaEventDestroy(g->fin_fork);
   if (g->fin_done) cudaEventDestroy(g->fin_done);
@@ -1222,8 +1271,9 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
     // one graph holds kGraphSteps steps (the kernels read the step index from the
     // device, so every copy is the same), the remainder runs as single steps.  In a
     // fused call only the first step's opening row pass works, so it runs once, before
-    // the graphs, which leave it out.
-    const bool skip_open = S.fused != 0;
+    // the graphs, which leave it out.  The executable graph stays with the grid and
+    // is replayed by later calls of the same launch shape (no capture per call).
+    const bool skip_open = S.fused != 0 && !(S.obs & QSF_OBS_EKIN);
     int64_t first = 0;
     if (skip_open) {
       if ((rc = launch_step(g, S))) return rc;
@@ -1237,24 +1287,28 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
       FinOverlap ov;
       const bool overlap = fin_overlap_ok(S);
       if (overlap && (rc = ensure_fin_stream(g, &ov))) return rc;
-      if ((rc = capture_graph(
-               g->stream,
-               [&]() {
-                 for (int64_t k = 0; k < per; ++k)
-                   if (int r = launch_step(g, S, nullptr, !skip_open, overlap ? &ov : nullptr)) return r;
-                 if (ov.pending) QSF_CU(cudaStreamWaitEvent(g->stream, ov.done, 0));  // join
-                 return QSF_OK;
-               },
-               &exec)))
-        return rc;
+      const int ekin = (S.obs & QSF_OBS_EKIN) ? 1 : 0, nfblk = S.nfterms > 0 ? g->nfblk : 1;
+      for (const qsf_grid::StepGraph& sg : g->step_graphs)
+        if (sg.per == per && sg.skip_open == (int)skip_open && sg.overlap == (int)overlap && sg.ekin == ekin &&
+            sg.nfblk == nfblk)
+          exec = sg.exec;
+      if (!exec) {
+        if ((rc = capture_graph(
+                 g->stream,
+                 [&]() {
+                   for (int64_t k = 0; k < per; ++k)
+                     if (int r = launch_step(g, S, nullptr, !skip_open, overlap ? &ov : nullptr)) return r;
+                   if (ov.pending) QSF_CU(cudaStreamWaitEvent(g->stream, ov.done, 0));  // join
+                   return QSF_OK;
+                 },
+                 &exec)))
+          return rc;
+        g->step_graphs.push_back({per, (int)skip_open, (int)overlap, ekin, nfblk, exec});
+      }
       for (int64_t k = 0; k + per <= rest; k += per) {
         const cudaError_t ce = cudaGraphLaunch(exec, g->stream);
-        if (ce != cudaSuccess) {
-          cudaGraphExecDestroy(exec);
-          return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
-        }
+        if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
       }
-      cudaGraphExecDestroy(exec);
       for (int64_t k = rest - rest % per; k < rest; ++k)
         if ((rc = launch_step(g, S, nullptr, !skip_open))) return rc;
     }
@@ -1386,6 +1440,7 @@ int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_do
   if (rows)
     QSF_CU(cudaMemcpy(rows, mb.g->rows_dev, (size_t)mb.nsteps * mb.ncol * sizeof(double), cudaMemcpyDeviceToHost));
   if (steps_done) *steps_done = ctl_h[2];
+  if (ctl_h[4]) return fail(QSF_ENUMERIC, "non-finite psi, NaN or non-positive norm in this member's reductions");
   return QSF_OK;
 }
 

@@ -110,6 +110,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
   const StepDev& S = Ss[blockIdx.y];
   cg::cluster_group cl = cg::this_cluster();
   if (!pass_active(S)) return;  // uniform over the pair
+  const bool ek = ekin_at(S, S.ctl[5]);  // read before any block advances the counters
   if (blockIdx.x % 2 == 0 && threadIdx.x == 0) S.ctl[6] = S.ctl[5] + 1;  // the sub-step's only pass
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
@@ -128,6 +129,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
     em = max(em, max(dexp(v.x), dexp(v.y)));
   }
   em = cluster_max_int(em, red, cl);
+  if (em >= 0x7ff && threadIdx.x == 0) S.ctl[4] = 1;  // Inf or NaN in psi: QSF_ENUMERIC
   const int s_in = scale_from_exponent<N>(em);
   int scale = s_in;
   long long F = 0;
@@ -202,7 +204,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
   }
   double dacc[3] = {acc_value(an), acc_value(av), 0.0};
   const int e_n = 2 * q - 2 * scale, e_v = 2 * q - 2 * scale + 50 - S.vshift;
-  if (S.obs & 4u) {  // E_kin: forward transform of psi_n over the pair
+  if (ek) {  // E_kin: forward transform of psi_n over the pair
     cl.sync();
     int b2 = bits, sc2 = scale + first_pass_shift<N>(bits);
     fft_fx_split<N>(line, a.twx, gid, gth, sc2, b2, red, cl, first_pass_shift<N>(bits));

@@ -47,6 +47,88 @@ __device__ __forceinline__ longlong2 fmul62(longlong2 a, longlong2 w) {
   const i64 k3 = mulq62(a.y, w.x + w.y);
   return make_longlong2(k1 - k3, k1 + k2);
 }
+// Twiddle products from pre-split tables (QSF_TWQ, the default).  A twiddle w in 2^62
+// fixed point is stored as the signed 32-bit halves of each component, w = wh 2^32 + wl
+// with wl = (int)w (int4 {re lo, re hi, im lo, im hi}; the host keeps every low half
+// away from -2^31 so that it can be negated).  The complex product a * w / 2^64 takes
+// the four high x high products exactly, sums the eight middle products of each output
+// component in one 64-bit word (rounded at bit 32) and drops the four low x low ones:
+// within 1 unit of the exact quotient, from twelve 32 x 32 -> 64-bit multiply-adds and
+// no 64-bit shifts.  Callers pre-scale a by 4 (components below 2^61), so the product
+// comes out at the scale of an untwiddled element.
+#ifndef QSF_TWQ
+#define QSF_TWQ 1
+#endif
+// the high half of the signed split x = hi 2^32 + (int)x
+__device__ __forceinline__ int split_hi(i64 x) { return (int)(x >> 32) + (int)((unsigned)x >> 31); }
+__device__ __forceinline__ longlong2 fmul_tw(longlong2 a, int4 w) {
+  const int axl = (int)a.x, axh = split_hi(a.x), ayl = (int)a.y, ayh = split_hi(a.y);
+  const int nyl = -w.z, nyh = -w.w;
+  i64 rm = (1LL << 31), im = (1LL << 31);
+  rm += (i64)axh * w.x;
+  rm += (i64)axl * w.y;
+  rm += (i64)ayh * nyl;
+  rm += (i64)ayl * nyh;
+  im += (i64)axh * w.z;
+  im += (i64)axl * w.w;
+  im += (i64)ayh * w.x;
+  im += (i64)ayl * w.y;
+  i64 re = rm >> 32, ii = im >> 32;
+  re += (i64)axh * w.y;
+  re += (i64)ayh * nyh;
+  ii += (i64)axh * w.w;
+  ii += (i64)ayh * w.y;
+  return make_longlong2(re, ii);
+}
+// the signed 32-bit halves of a compile-time 64-bit constant
+__host__ __device__ constexpr int k_lo(i64 c) {
+  return (int)((c & 0xffffffffLL) >= 0x80000000LL ? (c & 0xffffffffLL) - 0x100000000LL : (c & 0xffffffffLL));
+}
+__host__ __device__ constexpr int k_hi(i64 c) { return (int)((c - (i64)k_lo(c)) >> 32); }
+// a * C / 2^64 for a compile-time C (|C| < 2^63, |a| < 2^62): three multiply-adds,
+// within 0.75 units
+template <i64 C>
+__device__ __forceinline__ i64 mulk64(i64 a) {
+  constexpr int cl = k_lo(C), ch = k_hi(C);
+  const int al = (int)a, ah = split_hi(a);
+  const i64 m = (i64)ah * cl + (i64)al * ch + (1LL << 31);
+  return (m >> 32) + (i64)ah * ch;
+}
+// a * c for a constant c = C / 2^63 (|c| < 1): within 1.5 units
+template <i64 C>
+__device__ __forceinline__ i64 mulk63(i64 a) { return (i64)((u64)mulk64<C>(a) << 1); }
+// a * (CR + i CI) / 2^63 for compile-time constants: the complex form of mulk64 (merged
+// middle words), doubled; within 2 units per component
+template <i64 CR, i64 CI>
+__device__ __forceinline__ longlong2 fmulk63(longlong2 a) {
+  constexpr int rl = k_lo(CR), rh = k_hi(CR), il = k_lo(CI), ih = k_hi(CI), nl = k_lo(-CI), nh = k_hi(-CI);
+  const int axl = (int)a.x, axh = split_hi(a.x), ayl = (int)a.y, ayh = split_hi(a.y);
+  i64 rm = (1LL << 31), im = (1LL << 31);
+  rm += (i64)axh * rl;
+  rm += (i64)axl * rh;
+  rm += (i64)ayh * nl;
+  rm += (i64)ayl * nh;
+  im += (i64)axh * il;
+  im += (i64)axl * ih;
+  im += (i64)ayh * rl;
+  im += (i64)ayl * rh;
+  i64 re = rm >> 32, ii = im >> 32;
+  re += (i64)axh * rh;
+  re += (i64)ayh * nh;
+  ii += (i64)axh * ih;
+  ii += (i64)ayh * rh;
+  return make_longlong2((i64)((u64)re << 1), (i64)((u64)ii << 1));
+}
+// butterfly constants in 2^63 fixed point (|c| < 1)
+#define QSF_K63_SQRT1_2 6521908912666391106LL   /* round(2^63 / sqrt(2)) */
+#define QSF_K63_C16_1 8521284645587064995LL     /* round(2^63 cos(pi/8)) */
+#define QSF_K63_S16_1 3529631669043774883LL     /* round(2^63 sin(pi/8)) */
+#define QSF_K63_SQRT3_2 7987674492471257551LL   /* round(2^63 sqrt(3)/2) */
+#define QSF_K63_C5_1 2850178704830799621LL      /* round(2^63 cos(2pi/5)) */
+#define QSF_K63_C5_2 (-7461864723258187525LL)   /* round(2^63 cos(4pi/5)) */
+#define QSF_K63_S5_1 8771948077865237882LL      /* round(2^63 sin(2pi/5)) */
+#define QSF_K63_S5_2 5421362059670026167LL      /* round(2^63 sin(4pi/5)) */
+
 // OR of the component magnitudes (x ^ (x >> 63) is |x| or |x| - 1): its bit length is
 // the block maximum's bit length, or one less when that maximum is a negative power of two
 __device__ __forceinline__ u64 fmag(longlong2 x) { return (u64)(x.x ^ (x.x >> 63)) | (u64)(x.y ^ (x.y >> 63)); }
@@ -87,13 +169,18 @@ __device__ __forceinline__ void fbfly4(longlong2& x0, longlong2& x1, longlong2& 
   x3 = fsub(t1, t3);
 }
 // w8^1 * a and w8^3 * a, w8 = exp(sign 2 pi i / 8)
+#if QSF_TWQ
+__device__ __forceinline__ i64 mul_sqrt1_2(i64 a) { return mulk63<QSF_K63_SQRT1_2>(a); }
+#else
+__device__ __forceinline__ i64 mul_sqrt1_2(i64 a) { return mulq62(a, QSF_FX_SQRT1_2); }
+#endif
 template <bool FWD> __device__ __forceinline__ longlong2 fw8_1(longlong2 a) {
-  return FWD ? make_longlong2(mulq62(a.x + a.y, QSF_FX_SQRT1_2), mulq62(a.y - a.x, QSF_FX_SQRT1_2))
-             : make_longlong2(mulq62(a.x - a.y, QSF_FX_SQRT1_2), mulq62(a.x + a.y, QSF_FX_SQRT1_2));
+  return FWD ? make_longlong2(mul_sqrt1_2(a.x + a.y), mul_sqrt1_2(a.y - a.x))
+             : make_longlong2(mul_sqrt1_2(a.x - a.y), mul_sqrt1_2(a.x + a.y));
 }
 template <bool FWD> __device__ __forceinline__ longlong2 fw8_3(longlong2 a) {
-  return FWD ? make_longlong2(mulq62(a.y - a.x, QSF_FX_SQRT1_2), -mulq62(a.x + a.y, QSF_FX_SQRT1_2))
-             : make_longlong2(-mulq62(a.x + a.y, QSF_FX_SQRT1_2), mulq62(a.x - a.y, QSF_FX_SQRT1_2));
+  return FWD ? make_longlong2(mul_sqrt1_2(a.y - a.x), -mul_sqrt1_2(a.x + a.y))
+             : make_longlong2(-mul_sqrt1_2(a.x + a.y), mul_sqrt1_2(a.x - a.y));
 }
 template <bool FWD> __device__ __forceinline__ void fbfly8(longlong2* v) {
   longlong2 a0 = fadd(v[0], v[4]), a4 = fsub(v[0], v[4]);
@@ -111,8 +198,13 @@ template <bool FWD> __device__ __forceinline__ void fbfly8(longlong2* v) {
 template <bool FWD> __device__ __forceinline__ void fbfly3(longlong2* v) {
   const longlong2 t1 = fadd(v[1], v[2]), t2 = fsub(v[1], v[2]);
   // m1 = v0 - t1/2 ; X1 = m1 + i k t2, X2 = m1 - i k t2, k = sign * sqrt(3)/2
+#if QSF_TWQ
+  const longlong2 m1 = make_longlong2(v[0].x - ((t1.x + 1) >> 1), v[0].y - ((t1.y + 1) >> 1));
+  const i64 kx = mulk63<QSF_K63_SQRT3_2>(t2.x), ky = mulk63<QSF_K63_SQRT3_2>(t2.y);
+#else
   const longlong2 m1 = make_longlong2(v[0].x - mulq62(t1.x, QSF_FX_HALF), v[0].y - mulq62(t1.y, QSF_FX_HALF));
   const i64 kx = mulq62(t2.x, QSF_FX_SQRT3_2), ky = mulq62(t2.y, QSF_FX_SQRT3_2);
+#endif
   v[0] = fadd(v[0], t1);
   if (FWD) {  // k = -sqrt3/2
     v[1] = make_longlong2(m1.x + ky, m1.y - kx);
@@ -125,15 +217,19 @@ template <bool FWD> __device__ __forceinline__ void fbfly3(longlong2* v) {
 template <bool FWD> __device__ __forceinline__ void fbfly5(longlong2* v) {
   const longlong2 t1 = fadd(v[1], v[4]), t2 = fadd(v[2], v[3]), t3 = fsub(v[1], v[4]), t4 = fsub(v[2], v[3]);
   const longlong2 x0 = v[0];
-  const longlong2 a1 = make_longlong2(x0.x + mulq62(t1.x, QSF_FX_C5_1) + mulq62(t2.x, QSF_FX_C5_2),
-                                      x0.y + mulq62(t1.y, QSF_FX_C5_1) + mulq62(t2.y, QSF_FX_C5_2));
-  const longlong2 a2 = make_longlong2(x0.x + mulq62(t1.x, QSF_FX_C5_2) + mulq62(t2.x, QSF_FX_C5_1),
-                                      x0.y + mulq62(t1.y, QSF_FX_C5_2) + mulq62(t2.y, QSF_FX_C5_1));
+#if QSF_TWQ
+#define QSF_M5(x, K) mulk63<QSF_K63_##K>(x)
+#else
+#define QSF_M5(x, K) mulq62(x, QSF_FX_##K)
+#endif
+  const longlong2 a1 = make_longlong2(x0.x + QSF_M5(t1.x, C5_1) + QSF_M5(t2.x, C5_2),
+                                      x0.y + QSF_M5(t1.y, C5_1) + QSF_M5(t2.y, C5_2));
+  const longlong2 a2 = make_longlong2(x0.x + QSF_M5(t1.x, C5_2) + QSF_M5(t2.x, C5_1),
+                                      x0.y + QSF_M5(t1.y, C5_2) + QSF_M5(t2.y, C5_1));
   // b1 = s1 t3 + s2 t4, b2 = s2 t3 - s1 t4 with s = sign * sin
-  longlong2 b1 = make_longlong2(mulq62(t3.x, QSF_FX_S5_1) + mulq62(t4.x, QSF_FX_S5_2),
-                                mulq62(t3.y, QSF_FX_S5_1) + mulq62(t4.y, QSF_FX_S5_2));
-  longlong2 b2 = make_longlong2(mulq62(t3.x, QSF_FX_S5_2) - mulq62(t4.x, QSF_FX_S5_1),
-                                mulq62(t3.y, QSF_FX_S5_2) - mulq62(t4.y, QSF_FX_S5_1));
+  longlong2 b1 = make_longlong2(QSF_M5(t3.x, S5_1) + QSF_M5(t4.x, S5_2), QSF_M5(t3.y, S5_1) + QSF_M5(t4.y, S5_2));
+  longlong2 b2 = make_longlong2(QSF_M5(t3.x, S5_2) - QSF_M5(t4.x, S5_1), QSF_M5(t3.y, S5_2) - QSF_M5(t4.y, S5_1));
+#undef QSF_M5
   if (FWD) {
     b1 = make_longlong2(-b1.x, -b1.y);
     b2 = make_longlong2(-b2.x, -b2.y);
@@ -159,15 +255,23 @@ template <bool FWD> __device__ __forceinline__ void fbfly16(longlong2* v) {
     a[r * 4 + 2] = x2;
     a[r * 4 + 3] = x3;
   }
+#if QSF_TWQ
+  constexpr i64 sg = FWD ? -1 : 1;
+  a[1 * 4 + 1] = fmulk63<QSF_K63_C16_1, sg * QSF_K63_S16_1>(a[1 * 4 + 1]);     // w^1
+  a[1 * 4 + 3] = fmulk63<QSF_K63_S16_1, sg * QSF_K63_C16_1>(a[1 * 4 + 3]);     // w^3
+  a[3 * 4 + 1] = fmulk63<QSF_K63_S16_1, sg * QSF_K63_C16_1>(a[3 * 4 + 1]);     // w^3
+  a[3 * 4 + 3] = fmulk63<-QSF_K63_C16_1, -sg * QSF_K63_S16_1>(a[3 * 4 + 3]);   // w^9
+#else
   a[1 * 4 + 1] = frot<FWD>(a[1 * 4 + 1], QSF_FX_C16_1, QSF_FX_S16_1);    // w^1
-  a[1 * 4 + 2] = fw8_1<FWD>(a[1 * 4 + 2]);                              // w^2
   a[1 * 4 + 3] = frot<FWD>(a[1 * 4 + 3], QSF_FX_S16_1, QSF_FX_C16_1);    // w^3
+  a[3 * 4 + 1] = frot<FWD>(a[3 * 4 + 1], QSF_FX_S16_1, QSF_FX_C16_1);    // w^3
+  a[3 * 4 + 3] = frot<FWD>(a[3 * 4 + 3], -QSF_FX_C16_1, -QSF_FX_S16_1);  // w^9
+#endif
+  a[1 * 4 + 2] = fw8_1<FWD>(a[1 * 4 + 2]);                              // w^2
   a[2 * 4 + 1] = fw8_1<FWD>(a[2 * 4 + 1]);                              // w^2
   a[2 * 4 + 2] = fmul_si<FWD>(a[2 * 4 + 2]);                            // w^4
   a[2 * 4 + 3] = fw8_3<FWD>(a[2 * 4 + 3]);                              // w^6
-  a[3 * 4 + 1] = frot<FWD>(a[3 * 4 + 1], QSF_FX_S16_1, QSF_FX_C16_1);    // w^3
   a[3 * 4 + 2] = fw8_3<FWD>(a[3 * 4 + 2]);                              // w^6
-  a[3 * 4 + 3] = frot<FWD>(a[3 * 4 + 3], -QSF_FX_C16_1, -QSF_FX_S16_1);  // w^9
 #pragma unroll
   for (int k1 = 0; k1 < 4; ++k1) {
     longlong2 x0 = a[0 * 4 + k1], x1 = a[1 * 4 + k1], x2 = a[2 * 4 + k1], x3 = a[3 * 4 + k1];
@@ -235,16 +339,38 @@ __device__ __forceinline__ int block_max_int(int v, int* red) {
 // radices; a runtime value, so that passes of equal radix share one code body).
 // Inputs are scaled by 2^shift_in on load; returns, valid in every thread after the
 // call, the bit length of the block's largest output component (see fmag).
-template <int R, int MAXB, int N>
-__device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const LineSet& L,
-                                           const longlong2* __restrict__ tw, int tid, int nth, int shift_in, int* red,
-                                           int parity, int NS) {
+template <class TW>
+struct tw_is_split {
+  static constexpr bool value = false;
+};
+template <>
+struct tw_is_split<int4> {
+  static constexpr bool value = true;
+};
+// a pre-split twiddle back in one 64-bit word per component
+__device__ __forceinline__ longlong2 tw_join(int4 w) {
+  return make_longlong2((i64)((u64)(i64)w.y << 32) + (i64)w.x, (i64)((u64)(i64)w.w << 32) + (i64)w.z);
+}
+
+template <int R, int MAXB, int N, class TW>
+__device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const LineSet& L, const TW* __restrict__ tw,
+                                           int tid, int nth, int shift_in, int* red, int parity, int NS) {
   constexpr int nr = N / R;
+  constexpr bool kSplit = tw_is_split<TW>::value && R > 2;
   const int twstep = N / (NS * R);
   const int total = nr * L.nlines;
-  // the load-time scaling 2^shift_in without branches: (x << sl + half) >> sr
+  // the load-time scaling 2^shift_in without branches: (x << sl + half) >> sr; with
+  // pre-split twiddles the elements that get one (q >= 1 of a pass after the first)
+  // are loaded 2 bits higher (sl2 / sr2), since their product is a * w / 2^64
   const int sl = shift_in > 0 ? shift_in : 0, sr = shift_in < 0 ? min(-shift_in, 63) : 0;
   const i64 half = sr ? (i64)1 << (sr - 1) : 0;
+  const int shift_q = (kSplit && NS > 1) ? shift_in + 2 : shift_in;
+  const int sl2 = shift_q > 0 ? shift_q : 0, sr2 = shift_q < 0 ? min(-shift_q, 63) : 0;
+  const i64 half2 = sr2 ? (i64)1 << (sr2 - 1) : 0;
+  // index maps without divisions where the counts are powers of two
+  const bool ns_pow2 = (NS & (NS - 1)) == 0;
+  const bool nl_pow2 = (L.nlines & (L.nlines - 1)) == 0;
+  const int nl_sh = __ffs(L.nlines) - 1;
   longlong2 v[MAXB][R];
   int dsto[MAXB];
 #pragma unroll
@@ -254,8 +380,8 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
     if (w < total) {
       int line, j;
       if (L.line_fastest) {
-        line = w % L.nlines;
-        j = w / L.nlines;
+        line = nl_pow2 ? (w & (L.nlines - 1)) : w % L.nlines;
+        j = nl_pow2 ? (w >> nl_sh) : w / L.nlines;
       } else {
         j = w % nr;
         line = w / nr;
@@ -264,12 +390,19 @@ __device__ __forceinline__ int fx_stockham(longlong2* __restrict__ buf, const Li
 #pragma unroll
       for (int q = 0; q < R; ++q) {
         const longlong2 x = src[(j + q * nr) * L.es];
-        v[b][q] = make_longlong2(((i64)((u64)x.x << sl) + half) >> sr, ((i64)((u64)x.y << sl) + half) >> sr);
+        if (q == 0)
+          v[b][q] = make_longlong2(((i64)((u64)x.x << sl) + half) >> sr, ((i64)((u64)x.y << sl) + half) >> sr);
+        else
+          v[b][q] = make_longlong2(((i64)((u64)x.x << sl2) + half2) >> sr2, ((i64)((u64)x.y << sl2) + half2) >> sr2);
       }
-      const int jm = j % NS;
+      const int jm = ns_pow2 ? (j & (NS - 1)) : j % NS;
       if (NS > 1) {
 #pragma unroll
-        for (int q = 1; q < R; ++q) v[b][q] = fmul62(v[b][q], tw[jm * q * twstep]);
+        for (int q = 1; q < R; ++q) {
+          if constexpr (kSplit) v[b][q] = fmul_tw(v[b][q], tw[jm * q * twstep]);
+          else if constexpr (tw_is_split<TW>::value) v[b][q] = fmul62(v[b][q], tw_join(tw[jm * q * twstep]));
+          else v[b][q] = fmul62(v[b][q], tw[jm * q * twstep]);
+        }
       }
       dsto[b] = line * L.ls + ((j - jm) * R + jm) * L.es;
     }
@@ -329,8 +462,8 @@ __host__ __device__ constexpr int maxb_ppt(int r, int ppt) { return (ppt + r - 1
 __host__ __device__ constexpr int plan_l2(int ppt) { return ppt >= 16 ? QSF_RADIX_LOG2 : ppt >= 8 ? 3 : 2; }
 
 // the compile-time stages S.. of fft_fx
-template <int N, int S, int PPT>
-__device__ __forceinline__ void fft_fx_tail(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw,
+template <int N, int S, int PPT, class TW>
+__device__ __forceinline__ void fft_fx_tail(longlong2* buf, const LineSet& L, const TW* __restrict__ tw,
                                             int tid, int nth, int& scale, int& bits, int* red, int shift_in) {
   constexpr int L2 = plan_l2(PPT);
   if constexpr (S < nstages(N, L2)) {
@@ -347,8 +480,8 @@ __device__ __forceinline__ void fft_fx_tail(longlong2* buf, const LineSet& L, co
 }
 // PPT: points of the tile per thread (tile points / threads), which sets the butterflies
 // each thread carries per pass.
-template <int N, int PPT = 16>
-__device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const longlong2* __restrict__ tw, int tid,
+template <int N, int PPT = 16, class TW = longlong2>
+__device__ __forceinline__ void fft_fx(longlong2* buf, const LineSet& L, const TW* __restrict__ tw, int tid,
                                        int nth, int& scale, int& bits, int* red, int shift_in = 0) {
   // the leading passes of the plan's main radix share one code body (a loop); the rest
   // are unrolled

@@ -17,6 +17,10 @@ namespace qsf {
 // records msg as the text qsf_last_error() returns on this thread and returns code
 int fail(int code, const std::string& msg);
 
+// multiprocessor count of the current device (queried once per device); grid-stride
+// kernels size their grids as a multiple of it
+int device_sm_count();
+
 template <class T>
 int dev_alloc(T*& p, size_t count) {
   if (p) cudaFree(p);
@@ -129,4 +133,12 @@ struct qsf_grid {
   // first passes: the stream and its fork / join events (created on first use)
   cudaStream_t fin_stream = nullptr;
   cudaEvent_t fin_fork = nullptr, fin_done = nullptr;
+  // executable step graphs of qsf_step, kept per launch shape and replayed by later
+  // calls (the kernels read every per-call value from the device descriptors)
+  struct StepGraph {
+    int64_t per;
+    int skip_open, overlap, ekin, nfblk;
+    cudaGraphExec_t exec;
+  };
+  std::vector<StepGraph> step_graphs;
 };

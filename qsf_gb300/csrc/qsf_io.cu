@@ -24,7 +24,7 @@ size_t header_bytes(int dim) { return kHeaderFixed + (size_t)dim * (8 + 8 + 1); 
 
 int io_blocks(long long m) {
   long long b = (m + 255) / 256;
-  return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 16);
+  return (int)std::min<long long>(std::max<long long>(b, 1), (long long)device_sm_count() * 16);
 }
 
 // psi *= (-1)^(i0 + i1 + ...)  (phaseShiftTrick, grid.h:1074-1085)

@@ -68,6 +68,11 @@ struct AxisDev {
   double dx, xmin, dp, inv_2dx;
   const double2* tw;     // exp(-2 pi i t / n), t < n
   const longlong2* twx;  // the same twiddles in 2^62 fixed point
+#if QSF_TWQ
+  const int4* twf;  // the 2^62 twiddles as signed 32-bit halves (fmul_tw), read by fft_fx
+#else
+  const longlong2* twf;
+#endif
 };
 
 struct GridDev {
@@ -121,6 +126,10 @@ struct StepDev {
   // and forward transform (ψ stays in fixed point between the steps of a call); the
   // pending Normalize factor then folds into the next sub-step's axis-0 P table
   int fused;
+  // E_kin (QSF_OBS_EKIN) at the end of every ekin_every-th step of the call and of its
+  // last step; such a step ends with psi_n stored as complex128 (its other transforms
+  // need it) and the next one opens from there, the steps between stay fused
+  int ekin_every;
   int nmax;
   // reductions
   double* partials;  // [5][pmax]: norm, epot, ekin axis 0..2
@@ -155,6 +164,12 @@ struct StepDev {
 };
 
 __device__ __forceinline__ bool step_active(const StepDev& S) { return S.ctl[0] <= S.ctl[1] && S.ctl[0] < S.nsteps; }
+// whether sub-step `sub` ends a step whose observables include E_kin
+__device__ __forceinline__ bool ekin_at(const StepDev& S, long long sub) {
+  if (!(S.obs & 4u) || (sub + 1) % S.substeps) return false;
+  const long long step = sub / S.substeps;
+  return (step + 1) % S.ekin_every == 0 || sub + 1 >= S.nsteps || sub >= S.ctl[1];
+}
 // hint: move the 128-byte line holding p from DRAM into L2 (p must be in an allocation)
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 __device__ __forceinline__ bool pass_active(const StepDev& S) { return S.ctl[5] <= S.ctl[1] && S.ctl[5] < S.nsteps; }
@@ -527,13 +542,14 @@ __device__ __forceinline__ void finalize_tail(const GridDev& g, const StepDev& S
     return;
   }
   // last block: deterministic sums in a fixed order
+  const bool ek = ekin_at(S, sub);
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < S.nrowblk; i += blockDim.x) {
     acc[0] += S.partials[0 * S.pmax + i];
     acc[1] += S.partials[1 * S.pmax + i];
     acc[2 + g.dim - 1] += S.partials[(2 + g.dim - 1) * S.pmax + i];
   }
-  if (S.obs & 4u) {
+  if (ek) {
     for (int d = 0; d < g.dim - 1; ++d)
       for (int i = threadIdx.x; i < S.naxblk[d]; i += blockDim.x) acc[2 + d] += S.partials[(2 + d) * S.pmax + i];
   }
@@ -548,7 +564,7 @@ __device__ __forceinline__ void finalize_tail(const GridDev& g, const StepDev& S
     const double norm = acc[0] * g.dV;
     const double epot = acc[1] * g.dV;
     double ekin = 0.0;
-    if (S.obs & 4u) {
+    if (ek) {
       for (int d = 0; d < g.dim; ++d) ekin += (double)(g.m / g.ax[d].n) * acc[2 + d];
       ekin = 0.5 * g.dVm * ekin;
     }
@@ -560,7 +576,9 @@ __device__ __forceinline__ void finalize_tail(const GridDev& g, const StepDev& S
     for (int b = 0; b < nb; ++b) row[3 + b] = fsum[b] * g.dV / g.ax[0].dx;
     if (!(norm > 0.0) || isnan(epot) || isnan(ekin)) S.ctl[4] = 1;
     if (S.normalize && norm > 0.0) *S.scale = sqrt(1.0 / norm);
-    if (S.mode == 1 && S.state_accuracy > 0.0) {
+    // the convergence test needs E = E_pot + E_kin: with E_kin on every k-th step only,
+    // it runs on those steps (comparing with the previous one that had it)
+    if (S.mode == 1 && S.state_accuracy > 0.0 && (ek || !(S.obs & 4u))) {
       const double se = (S.energy_after_normalize & 1) ? 1.0 / norm : 1.0;
       const double sk = (S.energy_after_normalize & 2) ? 1.0 / norm : 1.0;
       const double E = epot * se + ekin * sk;
@@ -728,6 +746,9 @@ __device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, lo
     em = max(em, max(dexp(v.x), dexp(v.y)));
   }
   em = block_max_int(em, red);
+  // an Inf or NaN component (exponent field all ones) has no fixed-point image: flag
+  // the solve (QSF_ENUMERIC) instead of converting garbage
+  if (em >= 0x7ff && threadIdx.x == 0) S.ctl[4] = 1;
   const int s_in = scale_from_exponent<N>(em);
   int scale = s_in;
   long long F = 0;
@@ -875,7 +896,7 @@ __device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, co
                                             int bits, int* red) {
   const int sh = first_pass_shift<N>(bits);
   int sc = scale + sh, b = 0;
-  fft_fx<N, PPT>(smx, ls, a.twx, threadIdx.x, blockDim.x, sc, b, red, sh);
+  fft_fx<N, PPT>(smx, ls, a.twf, threadIdx.x, blockDim.x, sc, b, red, sh);
   double ek = 0.0;
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const double kk = kpos(a, e % N);
@@ -896,7 +917,9 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_open
   const StepDev& S = Ss[blockIdx.y];
   if (!pass_active(S)) return;
   const long long sub = S.ctl[5];
-  if (S.fused && sub > 0) return;  // the previous sub-step's closing pass produced pass 0
+  // the previous sub-step's closing pass produced pass 0, unless it ended with psi_n in
+  // memory for E_kin
+  if (S.fused && sub > 0 && !ekin_at(S, sub - 1)) return;
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
   const long long row0 = (long long)blockIdx.x * L;
@@ -908,7 +931,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_open
   const int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_fx<N, row_ppt(N)>(smx, ls, g.ax[g.dim - 1].twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, g.ax[g.dim - 1].twf, threadIdx.x, blockDim.x, scale, bits, red, sh);
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
 #pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
@@ -984,7 +1007,10 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
   const AxisDev& a = g.ax[g.dim - 1];
   const long long sub = S.ctl[5];
   if (blockIdx.x == 0 && threadIdx.x == 0) S.ctl[6] = sub + 1;  // the sub-step's last pass
-  const bool last = !S.fused || sub >= S.ctl[1] || sub + 1 >= S.nsteps;
+  // the step ends here, psi_n stored as complex128: the call's last sub-step, and steps
+  // whose E_kin needs psi_n in memory
+  const bool ek = ekin_at(S, sub);
+  const bool last = !S.fused || sub >= S.ctl[1] || sub + 1 >= S.nsteps || ek;
   const long long row0 = (long long)blockIdx.x * L;
   const int Lh = (int)min((long long)L, g.m / N - row0);
   const long long base = row0 * N;
@@ -1014,9 +1040,9 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
   int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{Lh, N, 1, false};
-  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
-  const bool fuse_x = !last && !(S.obs & 4u);
+  const bool fuse_x = !last;
   if (fuse_x) {
     close_open_block<N>(g, S, smx, base, cnt, row0, Lh, red, scale, bits, dacc);
     dacc[2] = 0.0;
@@ -1029,7 +1055,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
         S.snap[e] = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
       }
     }
-    dacc[2] = (S.obs & 4u) ? ekin_rows<N, row_ppt(N)>(a, smx, ls, cnt, scale, bits, red) : 0.0;
+    dacc[2] = ek ? ekin_rows<N, row_ppt(N)>(a, smx, ls, cnt, scale, bits, red) : 0.0;
   }
   const double e_n = dacc[3], e_v = dacc[4];
   block_sum<3>(dacc, dred);  // its barriers also end the snapshot reads of smx
@@ -1059,7 +1085,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
   }
   sh = first_pass_shift<N>(bits);
   scale += sh;
-  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red, sh);
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
 #pragma unroll 4
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) out[base + e] = smx[e];
@@ -1108,7 +1134,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!pass_active(S)) return;
-  if (MODE == 3 && !(S.obs & 4u)) return;
+  if (MODE == 3 && !ekin_at(S, S.ctl[5])) return;
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32];
@@ -1140,7 +1166,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
       smx[i * C + c] = make_longlong2(d2fx(v.x, scale), d2fx(v.y, scale));
     }
     __syncthreads();
-    fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+    fft_fx<N, row_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red);
     double acc = 0.0;
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       const int i = e / Ch, c = e % Ch;
@@ -1175,12 +1201,12 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
   }
   int sh = first_pass_shift<N>(bits);
   scale += sh;
-  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red, sh);
   if (MODE == 2) {
     scale += p_phase(g, S, smx, ax, N, Ch, C, multi_col ? pcol : nullptr, red, bits);
     sh = first_pass_shift<N>(bits);
     scale += sh;
-    fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+    fft_fx<N, row_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red, sh);
   }
   longlong2* out = reinterpret_cast<longlong2*>(g.psi);
   const bool conj_out = MODE != 0;
@@ -1215,11 +1241,11 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   int sh = first_pass_shift<N>(bits);
   scale += sh;
   const LineSet ls{1, N, 1, false};
-  fft_fx<N, line_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, line_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red, sh);
   scale += p_phase(g, S, smx, 0, N, 1, 1, nullptr, red, bits);
   sh = first_pass_shift<N>(bits);
   scale += sh;
-  fft_fx<N, line_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red, sh);
+  fft_fx<N, line_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red, sh);
   double dacc[5];
   close_block<N>(g, S, smx, 0, N, 0, red, scale, bits, dacc, true, true);
   __syncthreads();
@@ -1227,7 +1253,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
     const int e1 = S.row_ptr[1];
     for (int e = threadIdx.x; e < e1; e += blockDim.x) S.snap[e] = g.psi[S.snap_idx[e]];
   }
-  dacc[2] = (S.obs & 4u) ? ekin_rows<N, line_ppt(N)>(a, smx, ls, N, scale, bits, red) : 0.0;
+  dacc[2] = ekin_at(S, S.ctl[5]) ? ekin_rows<N, line_ppt(N)>(a, smx, ls, N, scale, bits, red) : 0.0;
   const double e_n = dacc[3], e_v = dacc[4];
   block_sum<3>(dacc, dred);
   if (threadIdx.x == 0) {
@@ -1281,7 +1307,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   __syncthreads();
   const LineSet ls{Lh, N, 1, false};
   int bits = 0;
-  fft_fx<N>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+  fft_fx<N>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const longlong2 x = FWD ? smx[e] : fconj(smx[e]);
     double2 v = make_double2(fx2d(x.x, scale), fx2d(x.y, scale));
@@ -1321,7 +1347,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis_fft
   __syncthreads();
   const LineSet ls{Ch, 1, C, true};
   int bits = 0;
-  fft_fx<N, row_ppt(N)>(smx, ls, a.twx, threadIdx.x, blockDim.x, scale, bits, red);
+  fft_fx<N, row_ppt(N)>(smx, ls, a.twf, threadIdx.x, blockDim.x, scale, bits, red);
   for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
     const int i = e / Ch, c = e % Ch;
     const longlong2 x = FWD ? smx[i * C + c] : fconj(smx[i * C + c]);

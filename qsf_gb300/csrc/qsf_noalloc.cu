@@ -93,9 +93,15 @@ double* scratch_for_current_device(int* rc) {
   static double* ptrs[64] = {nullptr};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+  if (e != cudaSuccess) {
     qsf::set_error_message(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     *rc = QSF_ECUDA;
+    return nullptr;
+  }
+  if (dev < 0 || dev >= 64) {
+    qsf::set_error_message("qsf_norm_noalloc: device index " + std::to_string(dev) +
+                           " exceeds the 64 devices whose scratch address is cached");
+    *rc = QSF_EINVAL;
     return nullptr;
   }
   std::lock_guard<std::mutex> lk(mu);
@@ -133,6 +139,8 @@ int qsf_norm_noalloc(const double* psi_dev, int64_t m, double dV, double* out_de
   if (rc) return rc;
   const int nblocks = (int)((m + kNoAllocChunk - 1) / kNoAllocChunk);
   cudaStream_t st = (cudaStream_t)stream;
+  // clear an earlier, unrelated launch error so that the check below reports this call's own
+  cudaGetLastError();
   k_norm_partials<<<nblocks, kNoAllocThreads, 0, st>>>((const double2*)psi_dev, (long long)m, scratch);
   k_norm_finish<<<1, kNoAllocThreads, 0, st>>>(scratch, nblocks, dV, out_dev);
   const cudaError_t e = cudaGetLastError();

@@ -13,7 +13,7 @@ namespace {
 
 int ops_blocks(long long m) {
   long long b = (m + 255) / 256;
-  return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 8);
+  return (int)std::min<long long>(std::max<long long>(b, 1), (long long)device_sm_count() * 8);
 }
 
 // per-block sums of |psi|^2 (V(x + dx e_dir) - V(x - dx e_dir)); the shifted positions

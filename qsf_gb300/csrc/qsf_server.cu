@@ -45,6 +45,7 @@ struct Running {
   qsf_grid_desc desc{};          // for returning the grid to the pool
   std::vector<double> coupling;  // kept alive while in the batch
   clk::time_point submitted, admitted;
+  bool cancel = false;           // qsf_server_cancel: leave after this round
 };
 
 int64_t grid_points(const qsf_grid_desc& d) {
@@ -68,8 +69,10 @@ struct qsf_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Pending> queue;
-  std::map<int64_t, qsf_result> results;
-  std::map<int64_t, Running> running;
+  std::map<int64_t, qsf_result> results;  // finished, not yet handed out
+  std::map<int64_t, Running> running;     // worker thread only
+  std::vector<int64_t> cancel_running;    // cancels of admitted solves (under mu)
+  std::map<int64_t, bool> admitted_set;   // tickets admitted and not finished (under mu)
   int64_t next_ticket = 1;
   bool stopping = false;
   std::thread worker;
@@ -164,6 +167,7 @@ void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t s
   res.latency_s = std::chrono::duration<double>(now - r.submitted).count();
   std::lock_guard<std::mutex> lk(s->mu);
   s->results[r.ticket] = res;
+  s->admitted_set.erase(r.ticket);
   s->stats.completed++;
   s->stats.in_flight--;
   if (status == QSF_OK) s->stats.grid_point_steps += (double)r.m * (double)steps;
@@ -230,16 +234,42 @@ void worker_loop(qsf_server* s) {
       cudaMemGetInfo(&free_b, &total_b);
       const double reserve = s->cfg.hbm_reserve_gb * 1e9;
       double budget = (double)free_b - reserve + (double)pooled_bytes(s);  // pooled grids can be freed
+      const double capacity = (double)total_b - reserve;  // what an otherwise empty device could give
       while (!s->queue.empty() && (int)(s->running.size() + take.size()) < s->cfg.max_slots) {
         const double need = (double)solve_bytes(s->queue.front().req);
-        if (need > budget) break;
+        if (need > capacity) {  // can never be admitted: finish it now, do not block the queue
+          Pending p = std::move(s->queue.front());
+          s->queue.pop_front();
+          s->stats.queued--;
+          s->stats.completed++;
+          qsf_result res{};
+          res.status = QSF_ENOMEM;
+          res.latency_s = res.queue_s = std::chrono::duration<double>(clk::now() - p.submitted).count();
+          s->results[p.ticket] = res;
+          s->cv_done.notify_all();
+          continue;
+        }
+        if (need > budget) break;  // fits later: stays queued
         budget -= need;
         take.push_back(std::move(s->queue.front()));
         s->queue.pop_front();
+        s->admitted_set[take.back().ticket] = true;
         s->stats.queued--;
         s->stats.admitted++;
         s->stats.in_flight++;
       }
+      // nothing resident and the queue head has to wait for memory: sleep until a
+      // submit, a cancel or a stop (or 20 ms) instead of spinning on cudaMemGetInfo
+      if (take.empty() && s->running.empty()) {
+        if (s->stopping) break;
+        s->cv_work.wait_for(lk, std::chrono::milliseconds(20));
+        continue;
+      }
+      for (int64_t t : s->cancel_running) {
+        auto it = s->running.find(t);
+        if (it != s->running.end()) it->second.cancel = true;
+      }
+      s->cancel_running.clear();
     }
     for (Pending& p : take) {
       Running r;
@@ -257,19 +287,28 @@ void worker_loop(qsf_server* s) {
     // one round of steps for every resident solve
     int64_t active = 0;
     const int rc_run = qsf_batch_run(s->batch, s->cfg.steps_per_round, &active);
-    // retire finished solves
+    // retire finished, cancelled and failed solves.  A numeric failure (QSF_ENUMERIC)
+    // belongs to single members, which qsf_batch_result names; any other error of the
+    // round ends every resident solve.
+    const bool fatal = rc_run && rc_run != QSF_ENUMERIC;
     std::vector<int64_t> done;
     for (auto& kv : s->running) {
       kv.second.remaining -= s->cfg.steps_per_round;
-      if (kv.second.remaining <= 0 || rc_run) done.push_back(kv.first);
+      bool bad = false;
+      if (rc_run == QSF_ENUMERIC) {
+        int64_t st = 0;
+        bad = qsf_batch_result(s->batch, kv.second.slot, nullptr, &st) == QSF_ENUMERIC;
+      }
+      if (kv.second.remaining <= 0 || fatal || bad || kv.second.cancel) done.push_back(kv.first);
     }
     for (int64_t t : done) {
       Running& r = s->running[t];
       rows.assign((size_t)r.nsteps * (3 + r.nb), 0.0);
       int64_t steps = 0;
-      int rc = rc_run ? rc_run : qsf_batch_result(s->batch, r.slot, rows.data(), &steps);
+      int rc = fatal ? rc_run : qsf_batch_result(s->batch, r.slot, rows.data(), &steps);
+      if (rc == QSF_OK && r.cancel && r.remaining > 0) rc = QSF_ECANCELED;
       qsf_batch_remove(s->batch, r.slot);
-      if (rc) qsf_grid_destroy(r.grid);
+      if (rc && rc != QSF_ECANCELED) qsf_grid_destroy(r.grid);
       else release_grid(s, r.desc, r.grid);
       finish(s, r, rc, rows.data(), steps);
       s->running.erase(t);
@@ -323,7 +362,10 @@ int qsf_server_poll(qsf_server* s, int64_t ticket, qsf_result* out, int* done) {
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->results.find(ticket);
   *done = it != s->results.end();
-  if (*done) *out = it->second;
+  if (*done) {
+    *out = it->second;
+    s->results.erase(it);  // handed out once
+  }
   return QSF_OK;
 }
 
@@ -335,8 +377,33 @@ int qsf_server_wait(qsf_server* s, int64_t ticket, double timeout_s, qsf_result*
     if (s->cv_done.wait_until(lk, until) == std::cv_status::timeout && s->results.find(ticket) == s->results.end())
       return QSF_ETIMEDOUT;
   }
-  *out = s->results[ticket];
+  auto it = s->results.find(ticket);
+  *out = it->second;
+  s->results.erase(it);  // handed out once
   return QSF_OK;
+}
+
+int qsf_server_cancel(qsf_server* s, int64_t ticket) {
+  if (!s) return QSF_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+    if (it->ticket != ticket) continue;
+    qsf_result res{};
+    res.status = QSF_ECANCELED;
+    res.latency_s = res.queue_s = std::chrono::duration<double>(clk::now() - it->submitted).count();
+    s->results[ticket] = res;
+    s->queue.erase(it);
+    s->stats.queued--;
+    s->stats.completed++;
+    s->cv_done.notify_all();
+    return QSF_OK;
+  }
+  if (s->admitted_set.count(ticket)) {
+    s->cancel_running.push_back(ticket);
+    s->cv_work.notify_one();
+    return QSF_OK;
+  }
+  return QSF_EINVAL;
 }
 
 int qsf_server_stats_get(qsf_server* s, qsf_server_stats* out) {

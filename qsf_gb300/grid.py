@@ -224,7 +224,8 @@ class Grid:
     # ------------------------------------------------------------ fused steps
     def step_desc(self, mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None,
                   obs: int = OBS_NORM, normalize: bool = False, borders: Sequence[str] = (), box_size: int = 0,
-                  state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0):
+                  state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0,
+                  ekin_interval: int = 1):
         """A qsf_step_desc (and the coupling array it points to, which must stay alive)."""
         d = StepDesc()
         d.mode = mode
@@ -244,23 +245,27 @@ class Grid:
         d.state_accuracy = state_accuracy
         d.last_energy = last_energy
         d.energy_after_normalize = int(energy_after_normalize)
+        d.ekin_interval = int(ekin_interval)
         return d, cp
 
     def step(self, mode: int, dt: float, nsteps: int, coupling: Optional[np.ndarray] = None, obs: int = OBS_NORM,
              normalize: bool = False, borders: Sequence[str] = (), box_size: int = 0,
              state_accuracy: float = 0.0, last_energy: float = 0.0, energy_after_normalize: int = 0,
-             profile: Optional[dict] = None, substeps: int = 1):
+             profile: Optional[dict] = None, substeps: int = 1, ekin_interval: int = 1):
         """Run nsteps fused Strang steps; returns (rows [nsteps, 3 + nb], steps_done).
 
         substeps = K > 1 runs each step as MultiProductSplit<Split3Base, K> does (K
         sub-steps of dt / K; coupling then has nsteps * K rows, one per sub-step).
         With `profile` (a dict), every launch is timed with CUDA events on the grid's
-        stream; per kernel kind the summed ms and launch counts are added to it."""
+        stream; per kernel kind the summed ms and launch counts are added to it.
+        ekin_interval = k > 1 computes E_kin (OBS_EKIN) on every k-th step and the last
+        one only (0 in the other rows); the steps between stay fused."""
         d = StepDesc()
         d.mode = mode
         d.dt = dt
         d.nsteps = int(nsteps)
         d.substeps = int(substeps)
+        d.ekin_interval = int(ekin_interval)
         cp = None
         if coupling is not None:
             cp = np.ascontiguousarray(coupling, dtype=np.float64)

@@ -137,9 +137,15 @@ def read_dat(path: str, outputs: list, binary: bool = False) -> np.ndarray:
 
 class SplitPropagator:
     def __init__(self, mode: int, dt: float, max_steps: int, grid: Grid, coupling: Coupling, outputs: list,
-                 state_accuracy: float = 0.0, order: int = 1):
-        """SplitPropagator<M, MultiProductSplit<Split3Base<X,P,X>, order>, Spin0<...>>."""
+                 state_accuracy: float = 0.0, order: int = 1, ekin_interval: int = 1):
+        """SplitPropagator<M, MultiProductSplit<Split3Base<X,P,X>, order>, Spin0<...>>.
+
+        ekin_interval = k > 1: the "ekin" / "etot" outputs are evaluated on every k-th
+        step of each fused call and on its last step (rows in between carry E_kin = 0),
+        so the steps between stay fused; 1 (the default) evaluates them every step as
+        the reference's computeEach does."""
         self.order = int(order)
+        self.ekin_interval = max(1, int(ekin_interval))
         if not 1 <= self.order <= 64:
             raise ValueError("order must be in [1, 64]")
         self.mode = mode
@@ -250,7 +256,8 @@ class SplitPropagator:
         rows, done = self.grid.step(self.mode, self.dt, nsteps, sched if self.coupling.size else None,
                                     obs=self._obs_mask(), normalize="normalize" in self.outputs, borders=borders,
                                     box_size=box, state_accuracy=acc, last_energy=self._last_change,
-                                    energy_after_normalize=self._energy_after_normalize(), substeps=self.order)
+                                    energy_after_normalize=self._energy_after_normalize(), substeps=self.order,
+                                    ekin_interval=self.ekin_interval)
         if done < nsteps:
             # the schedule ran ahead of the device: replay the host state to `done` steps
             self.timer = timer0

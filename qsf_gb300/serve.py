@@ -91,6 +91,10 @@ class Server:
         check(lib().qsf_server_wait(self._h, int(ticket), float(timeout_s), ctypes.byref(res)), "qsf_server_wait")
         return self._to_dict(res)
 
+    def cancel(self, ticket: int) -> None:
+        """Cancel a queued or running solve; its result then carries QSF_ECANCELED."""
+        check(lib().qsf_server_cancel(self._h, int(ticket)), "qsf_server_cancel")
+
     def stats(self):
         st = ServerStats()
         check(lib().qsf_server_stats_get(self._h, ctypes.byref(st)), "qsf_server_stats_get")
@@ -106,3 +110,37 @@ class Server:
             self.stop()
         except Exception:
             pass
+
+
+class ShardedServer:
+    """One rank's part of a request stream served by several GPUs (one process per GPU):
+    every rank sees the same ordered stream and submits to its own Server only the
+    requests that shard.StreamAssigner gives it (cost: grid points x steps), so the
+    ranks split the work without a collective.  submit() returns the local ticket, or
+    None for a request another rank serves."""
+
+    def __init__(self, rank: int, world_size: int, **server_kwargs):
+        from .shard import StreamAssigner
+        if not 0 <= rank < world_size:
+            raise ValueError("rank must be in [0, world_size)")
+        self.rank, self.world_size = rank, world_size
+        self._assign = StreamAssigner(world_size)
+        self.server = Server(**server_kwargs)
+
+    def submit(self, gdesc: GridDesc, mode: int, dt: float, nsteps: int, **kw) -> Optional[int]:
+        m = 1
+        for k in range(gdesc.dim):
+            m *= int(gdesc.n[k])
+        if self._assign.assign(float(m) * float(nsteps)) != self.rank:
+            return None
+        return self.server.submit(gdesc, mode, dt, nsteps, **kw)
+
+    def wait(self, ticket: int, timeout_s: float = 600.0):
+        return self.server.wait(ticket, timeout_s)
+
+    def stats(self):
+        return self.server.stats()
+
+    def stop(self):
+        self.server.stop()
+

@@ -43,3 +43,21 @@ def imbalance(costs: Sequence[float], parts: List[List[int]]) -> float:
     loads = [sum(costs[i] for i in p) for p in parts]
     mean = sum(loads) / len(loads)
     return max(loads) / mean if mean > 0 else 1.0
+
+
+class StreamAssigner:
+    """Online form of the same rule for a request stream: each arriving solve goes to
+    the rank with the least cost assigned so far (ties: lowest rank).  Every rank runs
+    an assigner over the same ordered stream and keeps the requests assigned to it, so
+    the ranks agree without communicating."""
+
+    def __init__(self, world_size: int):
+        if world_size < 1:
+            raise ValueError("world_size must be >= 1")
+        self.loads = [0.0] * world_size
+
+    def assign(self, c: float) -> int:
+        r = min(range(len(self.loads)), key=lambda k: (self.loads[k], k))
+        self.loads[r] += float(c)
+        return r
+

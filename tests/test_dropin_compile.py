@@ -11,11 +11,13 @@ import subprocess
 
 import pytest
 
+import oracle
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/include"
+REF = oracle.ref_include()  # $QSF_REF_INCLUDE or the oracle recipe's default
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference checkout not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="reference checkout not present")
 def test_reference_propagator_with_gpu_grid_compiles_and_links(tmp_path):
     from qsf_gb300 import build as B
     lib = B.build()

@@ -59,6 +59,14 @@ def test_primitives(Q, name):
     assert C.rel_l2(vg.download(), z["psi_norm"]) < PRIM_TOL
 
 
+def _assert_columns(got, ref):
+    """Every column at rtol OBS_TOL; the absolute floor is 1e-12 of that column's own
+    largest value (border fluxes span many decades between columns)."""
+    for c in range(ref.shape[1]):
+        scale = float(np.max(np.abs(ref[:, c])))
+        np.testing.assert_allclose(got[:, c], ref[:, c], rtol=OBS_TOL, atol=1e-12 * scale, err_msg=f"column {c}")
+
+
 @pytest.mark.parametrize("name", ["c1_vg", "c1_lg", "c2_vg", "c3_lg"])
 def test_full_runs(Q, name):
     z = C.load(name)
@@ -67,7 +75,7 @@ def test_full_runs(Q, name):
     got = np.array([C.im_dat_row(r) for r in rows])
     ref = z["im_rows"]
     assert got.shape == ref.shape
-    np.testing.assert_allclose(got, ref, rtol=OBS_TOL, atol=OBS_TOL)
+    _assert_columns(got, ref)
     assert C.rel_l2(g.download(), z["im_psi"]) < PSI_TOL
     g2, rows2 = C.gpu_re(p, dim, z["re_psi0"])
     nb = len(C.re_borders(dim))
@@ -75,7 +83,7 @@ def test_full_runs(Q, name):
     ref = z["re_rows"]
     assert got.shape == ref.shape
     np.testing.assert_allclose(got[:, :2], ref[:, :2], rtol=1e-14, atol=0)  # step and time are exact
-    np.testing.assert_allclose(got[:, 2:], ref[:, 2:], rtol=OBS_TOL, atol=OBS_TOL)
+    _assert_columns(got[:, 2:], ref[:, 2:])
     assert C.rel_l2(g2.download(), z["re_psi"]) < PSI_TOL
 
 

@@ -48,6 +48,52 @@ def _worker(rank, ws, port, q):
     dist.destroy_process_group()
 
 
+def _bench_worker(rank, ws, port, q):
+    """The batched bench's own assignment (bench.batch_specs / bench.batch_share) and
+    the served bench's stream assignment (shard.StreamAssigner), each rank on its own."""
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    specs = bench.batch_specs(256, 0)
+    mine = bench.batch_share(specs, 23, ws, rank)
+    t = torch.zeros(len(specs), dtype=torch.int64)
+    t[mine] = 1
+    dist.all_reduce(t)
+    rng = np.random.default_rng(5)
+    stream_costs = [float(rng.choice([1024, 4096, 65536, 262144])) * 256 for _ in range(500)]
+    a = shard.StreamAssigner(ws)
+    mine_s = [i for i, c in enumerate(stream_costs) if a.assign(c) == rank]
+    u = torch.zeros(len(stream_costs), dtype=torch.int64)
+    u[mine_s] = 1
+    dist.all_reduce(u)
+    load = torch.tensor([sum(stream_costs[i] for i in mine_s)], dtype=torch.float64)
+    loads = [torch.zeros(1, dtype=torch.float64) for _ in range(ws)]
+    dist.all_gather(loads, load)
+    if rank == 0:
+        q.put((t.tolist(), u.tolist(), [float(x.item()) for x in loads]))
+    dist.destroy_process_group()
+
+
+def test_two_ranks_gloo_split_the_bench_workloads():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 30500 + os.getpid() % 1000
+    procs = [ctx.Process(target=_bench_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    counts, scounts, loads = q.get(timeout=180)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert all(v == 1 for v in counts)   # every batched solve on exactly one rank
+    assert all(v == 1 for v in scounts)  # every served request on exactly one rank
+    assert max(loads) / (sum(loads) / 2) < 1.05
+
+
 def test_two_ranks_gloo_take_disjoint_shares():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
