@@ -574,6 +574,41 @@ def run_c4(steps, warmup, flush):
                         "800 nm 1e15 W/cm^2, CAP 26 nodes, norm + E_pot + ZOA_FLUX_3D every step"}
 
 
+def run_ekin(steps, flush):
+    """Imaginary-time steps with the kinetic energy as an output: every step (the
+    reference's computeEach), every 10th step (ekin_interval = 10, the steps between
+    fused) and never, on the 2D 2048^2 grid and the 1D 4096-point line (where the
+    line kernel computes it in place at no extra launch)."""
+    import torch
+    import qsf_gb300 as Q
+    out = {}
+    for name, dim, n, dx, ncap in (("2d2048", 2, N_EDGE, DX, NCAP), ("1d4096", 1, 4096, 0.2, 410)):
+        stream = torch.cuda.Stream()
+        g = Q.Grid(dim, n, dx, nCAP=ncap, potential=Q.POT_EBERLY, Ncharge=float(dim), gauge=Q.GAUGE_VELOCITY,
+                   n_fields=0, stream=stream.cuda_stream)
+        psi = _gauss_state(dim, n, dx)
+        row = {}
+        for label, obs, k in (("ekin_every_step", Q.OBS_NORM | Q.OBS_EPOT | Q.OBS_EKIN, 1),
+                              ("ekin_every_10", Q.OBS_NORM | Q.OBS_EPOT | Q.OBS_EKIN, 10),
+                              ("no_ekin", Q.OBS_NORM | Q.OBS_EPOT, 1)):
+            g.upload(psi)
+            g.step(Q.MODE_IM, 0.01, 10, None, obs=obs, normalize=True, ekin_interval=k)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0.record(stream)
+                g.step(Q.MODE_IM, 0.01, steps, None, obs=obs, normalize=True, ekin_interval=k)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            row[label + "_ms_per_step"] = e0.elapsed_time(e1) / steps
+        g.close()
+        out[name] = row
+    out["workload"] = ("imaginary time dt 0.01 with Normalize every step, norm + E_pot (+ E_kin) rows; "
+                       f"{steps} steps per timed call")
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = _dist()
     import torch
@@ -661,6 +696,7 @@ def run_gpu(args):
     multigrid = run_multigrid(steps=20, warmup=3, cpu=rank == 0)
     c1 = run_c1(steps=max(args.steps, 200), warmup=args.warmup, flush=flush)
     c4 = run_c4(steps=max(args.steps, 10), warmup=args.warmup, flush=flush)
+    ekin = run_ekin(steps=max(args.steps, 40), flush=flush)
 
     if rank == 0:
         cpu = cpu_baseline(all_cores=False)
@@ -690,6 +726,7 @@ def run_gpu(args):
             "multigrid": multigrid,
             "c1": c1,
             "c4": c4,
+            "ekin": ekin,
             "batched_vs_plain": batched["value"] / value,
             "batched_vs_plain_same_solves": batched.get("batched_vs_plain_same_solves"),
         }

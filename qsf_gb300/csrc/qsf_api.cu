@@ -194,7 +194,8 @@ int ensure_static(qsf_grid* g, int mode, double delta) {
     if (!std::isfinite(fmax)) return fail(QSF_EINVAL, "imaginary-time X factor overflows (dt * |V| too large)");
     if (fmax > 1.0) std::frexp(fmax, &g->xs_exp);
   }
-  k_build_static<<<grid_blocks(m), 256, 0, g->stream>>>(g->G, mode, delta, g->xs_exp, g->xs, g->Vx, g->vshift);
+  k_build_static<<<grid_blocks(m), 256, 0, g->stream>>>(g->G, mode, delta, g->xs_exp, reinterpret_cast<int4*>(g->xs),
+                                                        g->Vx, g->vshift);
   QSF_CU(cudaGetLastError());
   g->xs_mode = mode;
   g->xs_delta = delta;
@@ -521,10 +522,10 @@ int prepare_step(qsf_grid* g, const qsf_step_desc* d, StepDev* out, int* ncol_ou
   S.substeps = K;
   S.coupling = coup;
   S.coup_stride = cstride;
-  S.xs = g->xs;
+  S.xs = reinterpret_cast<const int4*>(g->xs);
   S.Vx = g->Vx;
-  S.ptab = g->ptab;
-  S.xdyn = g->xdyn;
+  S.ptab = reinterpret_cast<int4*>(g->ptab);
+  S.xdyn = reinterpret_cast<int4*>(g->xdyn);
   S.xs_exp = g->xs_exp;
   S.vshift = g->vshift;
   S.l2m = g->l2m;

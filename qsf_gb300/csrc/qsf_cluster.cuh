@@ -145,11 +145,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
     longlong2 x = make_longlong2(d2fx(v.x, s_in), d2fx(v.y, s_in));
     if (use_s) x = make_longlong2(mulq62(x.x, F), mulq62(x.y, F));
     const long long p = base + e;
-    x = apply_f(x, xfactor(g, S, p, 0, (int)p, 0), real_f);
+    x = xhalf(g, S, x, p, 0, (int)p, 0, real_f);
     smx[e] = x;
     mag |= fmag(x);
   }
-  scale -= xfactor_exp(g, S, 0);
+  scale -= xhalf_exp(g, S, 0);
   int bits = cluster_max_int(bitlen(mag), red, cl);
   const SplitLine line = split_line(smx, cl, H);
   const int gid = rank * blockDim.x + threadIdx.x, gth = 2 * blockDim.x;
@@ -163,11 +163,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
     for (int e = threadIdx.x; e < H; e += blockDim.x) {
       longlong2 x = smx[e];
       if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-      x = fconj(apply_f(x, S.ptab[base + e], S.mode == 1));
+      x = fconj(fapply(x, S.ptab[base + e], S.mode == 1));
       smx[e] = x;
       mag |= fmag(x);
     }
-    scale += pre - S.texp[0];
+    scale += pre - S.texp[0] - xshift(1);
     bits = cluster_max_int(bitlen(mag), red, cl);
   }
   sh = first_pass_shift<N>(bits);
@@ -180,11 +180,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
     const long long p = base + e;
     longlong2 x = fconj(smx[e]);
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    x = apply_f(x, xfactor(g, S, p, 0, (int)p, 1), real_f);
+    x = xhalf(g, S, x, p, 0, (int)p, 1, real_f);
     smx[e] = x;
     mag |= fmag(x);
   }
-  scale += pre - xfactor_exp(g, S, 1) + S.l2m;
+  scale += pre - xhalf_exp(g, S, 1) + S.l2m;
   bits = cluster_max_int(bitlen(mag), red, cl);
   const int q = bits > 56 ? bits - 56 : 0;
   Acc128 an{0ull, 0ll}, av{0ull, 0ll};

@@ -110,10 +110,11 @@ struct StepDev {
   long long nsteps;
   const double* coupling;  // device copy of the per-step coupling rows (may be null)
   int coup_stride;         // 3 (velocity gauge) or 6 (length gauge)
-  const longlong2* xs;     // static X half-step factor per point (dt/2, incl. absorber), 2^62 fixed, * 2^-xs_exp
+  // phase tables in the split form (split62: 2^62 fixed point as signed 32-bit halves)
+  const int4* xs;          // static X half-step factor per point (dt/2, incl. absorber), * 2^-xs_exp
   const long long* Vx;     // potential per point in 2^vshift fixed point
-  longlong2* ptab;         // [dim][nmax] P-phase tables of the current step (2^62 fixed, |.| <= 1)
-  longlong2* xdyn;         // [2][dim][nmax] length-gauge factors: open half, close half
+  int4* ptab;              // [dim][nmax] P-phase tables of the current step (|.| <= 1)
+  int4* xdyn;              // [3][dim][nmax] length-gauge factors: open half, close half, next open half
   int xs_exp;              // exponent taken out of xs (imaginary time: factors above 1)
   int vshift;              // Vx = round(V * 2^vshift)
   int l2m;                 // 1/m = m_mant * 2^-l2m, m_mant in (0.5, 1] (folded into axis 0's P table)
@@ -387,6 +388,18 @@ __device__ __forceinline__ double acc_value(const Acc128& a) {
 // Norm and E_pot partial sums of a block of psi_n in fixed point (components below
 // 2^56 after the block's common shift q): |x|^2 exactly, V|x|^2 with |x|^2 >> 50 and V
 // in 2^vshift fixed point (|V| < 2^50 there).
+__device__ __forceinline__ void acc_point_v(Acc128& an, Acc128& av, longlong2 x, int q, long long v, bool epot) {
+  const long long xr = q ? fshift(x.x, -q) : x.x, xi = q ? fshift(x.y, -q) : x.y;
+  const unsigned long long ar = (unsigned long long)(xr < 0 ? -xr : xr), ai = (unsigned long long)(xi < 0 ? -xi : xi);
+  const unsigned long long l1 = ar * ar, l2 = ai * ai;
+  const unsigned long long lo = l1 + l2;
+  const unsigned long long hi = __umul64hi(ar, ar) + __umul64hi(ai, ai) + (lo < l1 ? 1ull : 0ull);
+  acc_add(an, lo, (long long)hi);
+  if (epot) {
+    const long long n2 = (long long)((hi << 14) | (lo >> 50));
+    acc_add(av, (unsigned long long)n2 * (unsigned long long)v, __mul64hi(n2, v));
+  }
+}
 __device__ __forceinline__ void acc_point(Acc128& an, Acc128& av, longlong2 x, int q, const long long* Vx, long long p,
                                           bool epot) {
   const long long xr = q ? fshift(x.x, -q) : x.x, xi = q ? fshift(x.y, -q) : x.y;
@@ -402,15 +415,41 @@ __device__ __forceinline__ void acc_point(Acc128& an, Acc128& av, longlong2 x, i
   }
 }
 
-// 2^62 fixed point of a factor with |f| <= 1
-__device__ __forceinline__ longlong2 to_fx62(double2 f) {
-  return make_longlong2(__double2ll_rn(f.x * 4611686018427387904.0), __double2ll_rn(f.y * 4611686018427387904.0));
+// Phase factors (|components| <= 1) are stored in 2^62 fixed point as the signed
+// 32-bit halves of each component (int4 {re lo, re hi, im lo, im hi}, as the FFT's
+// twiddles), with every low half kept away from -2^31 so that it can be negated.  A
+// product x * f (fapply) returns x * f / 4 from twelve 32 x 32 -> 64-bit multiply-adds
+// (fmul_tw) and needs |x| < 2^61.
+__device__ __forceinline__ int4 split62(double2 f) {
+  long long a = __double2ll_rn(f.x * 4611686018427387904.0), b = __double2ll_rn(f.y * 4611686018427387904.0);
+  if ((a & 0xffffffffLL) == 0x80000000LL) ++a;
+  if ((b & 0xffffffffLL) == 0x80000000LL) ++b;
+  return make_int4((int)a, split_hi(a), (int)b, split_hi(b));
 }
-
-// x * f, f in 2^62 fixed point with |f| <= 1 (real f: imaginary-time X factors)
-__device__ __forceinline__ longlong2 apply_f(longlong2 x, longlong2 f, bool real_f) {
-  return real_f ? make_longlong2(mulq62(x.x, f.x), mulq62(x.y, f.x)) : fmul62(x, f);
+__device__ __forceinline__ int4 split_fx(longlong2 v) {
+  if ((v.x & 0xffffffffLL) == 0x80000000LL) ++v.x;
+  if ((v.y & 0xffffffffLL) == 0x80000000LL) ++v.y;
+  return make_int4((int)v.x, split_hi(v.x), (int)v.y, split_hi(v.y));
 }
+// a * w / 2^64 for a real w given as its signed halves (wl, wh)
+__device__ __forceinline__ i64 mul_re(i64 a, int wl, int wh) {
+  const int al = (int)a, ah = split_hi(a);
+  const i64 m = (i64)ah * wl + (i64)al * wh + (1LL << 31);
+  return (m >> 32) + (i64)ah * wh;
+}
+// x * f / 4 (real f: imaginary-time X factors, only f's real part is read)
+__device__ __forceinline__ longlong2 fapply(longlong2 x, int4 f, bool real_f) {
+  return real_f ? make_longlong2(mul_re(x.x, f.x, f.y), mul_re(x.y, f.x, f.y)) : fmul_tw(x, f);
+}
+// x * 4 (renormalises after two products: the data stay below 2^61)
+__device__ __forceinline__ longlong2 fshl2(longlong2 x) {
+  return make_longlong2((i64)((u64)x.x << 2), (i64)((u64)x.y << 2));
+}
+// k factors applied in a row (fapply each, fshl2 after every second one that is
+// followed by another): the exponent the value moves by and a bound on the change of
+// its bit length (each product adds at most one bit, for the complex modulus)
+__host__ __device__ constexpr int xshift(int k) { return 2 * k - 2 * ((k - 1) / 2); }
+__host__ __device__ constexpr int xbits(int k) { return 2 * ((k - 1) / 2) - k; }
 
 // Largest exponent shift that brings a block whose largest component has `bits`
 // bits below 2^(62 - guard of the first pass of an N-point transform)
@@ -418,8 +457,10 @@ template <int N>
 __device__ __forceinline__ int first_pass_shift(int bits) {
   return bits == 0 ? 0 : (62 - fguard(radix_at(N, 0))) - bits;
 }
-// shift that brings `bits` to at most 61 (headroom for one complex product)
-__device__ __forceinline__ int product_headroom(int bits) { return bits > 61 ? 61 - bits : 0; }
+// shift that brings a block's largest component to 61 bits before phase products: the
+// split products need |x| < 2^61 and return x * f / 4, so starting at the top keeps
+// their rounding (1 unit of the output) at 2^-59 of the block maximum
+__device__ __forceinline__ int product_headroom(int bits) { return bits ? 61 - bits : 0; }
 
 // value of one per-step table entry: kind 0 P phase (hamiltonian.h:52-58: kinetic and,
 // in the velocity gauge, A.k), kind 1 / 2 length-gauge x.E factor of the open / close
@@ -476,12 +517,12 @@ __device__ __forceinline__ void tables_one(const GridDev& g, const StepDev& S, l
   }
   __syncthreads();
   const double sc = ldexp(mant, -*e_sh);
-  longlong2* out = kind == 0 ? S.ptab + (size_t)d * S.nmax : S.xdyn + ((size_t)(kind - 1) * D + d) * S.nmax;
+  int4* out = kind == 0 ? S.ptab + (size_t)d * S.nmax : S.xdyn + ((size_t)(kind - 1) * D + d) * S.nmax;
   const int chunk = (n + tb - 1) / tb;
   const int i1 = min(n, (part + 1) * chunk);
   for (int i = part * chunk + threadIdx.x; i < i1; i += blockDim.x) {
     const double2 f = table_entry(g, S, cp, cn, kind, d, i);
-    out[i] = to_fx62(make_double2(fmin(fmax(f.x * sc, -1.0), 1.0), fmin(fmax(f.y * sc, -1.0), 1.0)));
+    out[i] = split62(make_double2(fmin(fmax(f.x * sc, -1.0), 1.0), fmin(fmax(f.y * sc, -1.0), 1.0)));
   }
 }
 
@@ -635,7 +676,7 @@ __global__ void k_vrange(GridDev g, long long* out) {
 
 // Static tables for X(delta): expOp(delta V) * absorb(delta) per point in 2^62 fixed
 // point times 2^-xs_exp, and the potential in 2^vshift fixed point.
-__global__ void k_build_static(GridDev g, int mode, double delta, int xs_exp, longlong2* xsx, long long* Vx,
+__global__ void k_build_static(GridDev g, int mode, double delta, int xs_exp, int4* xsx, long long* Vx,
                                int vshift) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   const double vs = ldexp(1.0, vshift), xsc = ldexp(1.0, -xs_exp);
@@ -649,7 +690,7 @@ __global__ void k_build_static(GridDev g, int mode, double delta, int xs_exp, lo
     const double2 f = expop(mode, delta * v);
     const double a = (g.multi ? 1.0 : absorb_at(g, delta, idx)) * xsc;
     const double2 fa = make_double2(f.x * a, f.y * a);
-    xsx[p] = to_fx62(make_double2(fmin(fmax(fa.x, -1.0), 1.0), fmin(fmax(fa.y, -1.0), 1.0)));
+    xsx[p] = split62(make_double2(fmin(fmax(fa.x, -1.0), 1.0), fmin(fmax(fa.y, -1.0), 1.0)));
   }
 }
 
@@ -684,41 +725,52 @@ __global__ void __launch_bounds__(256) k_tables(const GridDev* __restrict__ Gs, 
 
 #endif  // QSF_DEFINE_KERNELS
 
-// X factor (2^62 fixed point, |.| <= 1) at point p (row r of the last axis, position
-// j on it); half 0 opens the step, 1 closes it, 2 opens the next sub-step.  NA is the
-// length of the axes before the last one when known at compile time (0: read it).
+// Factors of the X half `half` (0 opens the step, 1 closes it, 2 opens the next
+// sub-step): the static factor and, in the length gauge, one x.E factor per axis.
+__device__ __forceinline__ int xfactors(const GridDev& g) { return 1 + (g.gauge == 1 ? g.dim : 0); }
+// The X half applied to x at point p (row r of the last axis, position j on it): the
+// factors one after another (fapply; fshl2 after the second when more follow), x below
+// 2^61.  NA is the length of the axes before the last one when known at compile time
+// (0: read it).  The value moves by xhalf_exp (bits <= in + xbits(xfactors(g))).
 template <int NA = 0>
-__device__ __forceinline__ longlong2 xfactor(const GridDev& g, const StepDev& S, long long p, long long r, int j,
-                                             int half) {
-  longlong2 f = S.xs[p];
+__device__ __forceinline__ longlong2 xhalf(const GridDev& g, const StepDev& S, longlong2 x, long long p, long long r,
+                                           int j, int half, bool real_f) {
+  x = fapply(x, S.xs[p], real_f);
   if (g.gauge == 1) {
     const int D = g.dim;
-    const longlong2* t = S.xdyn + (size_t)half * D * S.nmax;
-    longlong2 d = t[(D - 1) * S.nmax + j];
+    const int4* t = S.xdyn + (size_t)half * D * S.nmax;
+    x = fapply(x, t[(D - 1) * S.nmax + j], false);
     long long rr = r;
+    int k = 2;
     for (int dd = D - 2; dd >= 0; --dd) {
       const long long n = NA ? NA : g.ax[dd].n;
       const int ii = (int)(rr % n);
       rr /= n;
-      d = fmul62(d, t[dd * S.nmax + ii]);
+      if (k % 2 == 0) x = fshl2(x);
+      x = fapply(x, t[dd * S.nmax + ii], false);
+      ++k;
     }
-    f = fmul62(f, d);
   }
-  return f;
+  return x;
 }
-// exponent taken out of the X factor of one half
+// exponent taken out of the factors of one half (their table exponents) plus the
+// exponent the k products move the value by
 __device__ __forceinline__ int xfactor_exp(const GridDev& g, const StepDev& S, int half) {
   int e = S.xs_exp;
   if (g.gauge == 1)
     for (int d = 0; d < g.dim; ++d) e += S.texp[(1 + half) * 3 + d];
   return e;
 }
+__device__ __forceinline__ int xhalf_exp(const GridDev& g, const StepDev& S, int half) {
+  return xfactor_exp(g, S, half) + xshift(xfactors(g));
+}
 
 // psi (double) -> fixed point: the block exponent from the largest biased exponent
-// em of the block leaves two bits for the pending Normalize factor and the first pass
+// em of the block puts the largest component at 61 bits (below 2^61, as the phase
+// products need; the pending Normalize factor is at most 1)
 template <int N>
 __device__ __forceinline__ int scale_from_exponent(int em) {
-  return (62 - 1 - fguard(radix_at(N, 0))) - (em - 1022);
+  return 61 - (em - 1022);
 }
 
 // pending Normalize factor s = F 2^-62 * 2^k with F in [2^61, 2^62)
@@ -765,12 +817,12 @@ __device__ __forceinline__ int open_block(const GridDev& g, const StepDev& S, lo
     const double2 v = sd[e];  // written by this thread
     longlong2 x = make_longlong2(d2fx(v.x, s_in), d2fx(v.y, s_in));
     if (use_s) x = make_longlong2(mulq62(x.x, F), mulq62(x.y, F));
-    x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 0), real_f);
+    x = xhalf<N>(g, S, x, p, row0 + e / N, e % N, 0, real_f);
     smx[e] = x;
     mag |= fmag(x);
   }
   bits = block_max_int(bitlen(mag), red);
-  return scale - xfactor_exp(g, S, 0);
+  return scale - xhalf_exp(g, S, 0);
 }
 
 // psi_n from the block after the last inverse transform (held conjugated in smx when
@@ -790,11 +842,11 @@ __device__ __forceinline__ void close_block(const GridDev& g, const StepDev& S, 
     longlong2 x = smx[e];
     if (conj_in) x = fconj(x);
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 1), real_f);
+    x = xhalf<N>(g, S, x, p, row0 + e / N, e % N, 1, real_f);
     smx[e] = x;
     mag |= fmag(x);
   }
-  scale += pre - xfactor_exp(g, S, 1) + S.l2m;
+  scale += pre - xhalf_exp(g, S, 1) + S.l2m;
   bits = block_max_int(bitlen(mag), red);
   const int q = bits > 56 ? bits - 56 : 0;
   Acc128 an{0ull, 0ll}, av{0ull, 0ll};
@@ -824,69 +876,97 @@ __device__ __forceinline__ void close_open_block(const GridDev& g, const StepDev
                                                  int cnt, long long row0, int Lh, int* red, int& scale, int& bits,
                                                  double* dacc) {
   const bool real_f = S.mode == 1 && g.gauge != 1;
+  // length gauge in 3D: the x.E factors of the first two axes are constant along a row;
+  // their product per row and half is formed once, so that a half is three products
+  constexpr int kRowPre = 64;
+  __shared__ int4 rowpre[2][kRowPre];
+  const bool hoist = g.gauge == 1 && g.dim == 3 && Lh <= kRowPre;
+  const int4* t1 = S.xdyn + (size_t)1 * 3 * S.nmax;  // close half, axes 0..2
+  const int4* t2 = S.xdyn + (size_t)2 * 3 * S.nmax;  // next open half
+  if (hoist) {
+    for (int t = threadIdx.x; t < 2 * Lh; t += blockDim.x) {
+      const int h = t / Lh, rl = t % Lh;
+      const long long r = row0 + rl;
+      const int4* tab = h ? t2 : t1;
+      rowpre[h][rl] = split_fx(fmul62(tw_join(tab[S.nmax + (int)(r % N)]), tw_join(tab[(int)(r / N)])));
+    }
+    __syncthreads();
+  }
+  // half h (1: close, 2: next open) at block element e
+  auto half = [&](longlong2 x, int e, int h) -> longlong2 {
+    const long long p = base + e;
+    if (hoist) {
+      x = fapply(x, S.xs[p], false);
+      x = fapply(x, rowpre[h - 1][e / N], false);
+      x = fshl2(x);
+      return fapply(x, (h == 1 ? t1 : t2)[2 * S.nmax + e % N], false);
+    }
+    return xhalf<N>(g, S, x, p, row0 + e / N, e % N, h, real_f);
+  };
+  const int kf = hoist ? 3 : xfactors(g);  // products per half
   const int pre = product_headroom(bits);
-  const int by = min(bits + pre + 1, 62);
-  const int sy = scale + pre - xfactor_exp(g, S, 1) + S.l2m;
+  const int by = min(bits + pre + xbits(kf), 62);
+  const int sy = scale + pre - xfactor_exp(g, S, 1) - xshift(kf) + S.l2m;
   const int q = by > 56 ? by - 56 : 0;
   const int pre2 = product_headroom(by);
   if (S.row_ptr) {
     const int e0 = S.row_ptr[row0], e1 = S.row_ptr[row0 + Lh];
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-      const long long p = S.snap_idx[e];
-      const int k = (int)(p - base);
+      const int k = (int)(S.snap_idx[e] - base);
       longlong2 x = fconj(smx[k]);
       if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-      x = apply_f(x, xfactor<N>(g, S, p, row0 + k / N, k % N, 1), real_f);
+      x = half(x, k, 1);
       S.snap[e] = make_double2(fx2d(x.x, sy), fx2d(x.y, sy));
-    }
-    __syncthreads();
-  }
-  // length gauge in 3D: the x.E factors of the first two axes are constant along a row;
-  // their product per row and half is formed once
-  constexpr int kRowPre = 64;
-  __shared__ longlong2 rowpre[2][kRowPre];
-  const bool hoist = g.gauge == 1 && g.dim == 3 && Lh <= kRowPre;
-  const longlong2* t1 = S.xdyn + (size_t)1 * 3 * S.nmax;  // close half, axes 0..2
-  const longlong2* t2 = S.xdyn + (size_t)2 * 3 * S.nmax;  // next open half
-  if (hoist) {
-    for (int t = threadIdx.x; t < 2 * Lh; t += blockDim.x) {
-      const int h = t / Lh, rl = t % Lh;
-      const long long r = row0 + rl;
-      const longlong2* tab = h ? t2 : t1;
-      rowpre[h][rl] = fmul62(tab[S.nmax + (int)(r % N)], tab[(int)(r / N)]);
     }
     __syncthreads();
   }
   Acc128 an{0ull, 0ll}, av{0ull, 0ll};
   const bool epot = (S.obs & 2u) != 0;
   u64 mag = 0;
-#pragma unroll 1  // a large body: unrolling costs more in instruction fetch than it gains
-  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const long long p = base + e;
-    longlong2 x = fconj(smx[e]);
-    if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    longlong2 f1, f2;
-    if (hoist) {
-      const int rl = e / N, j = e % N;
-      const longlong2 xsv = S.xs[p];
-      f1 = fmul62(xsv, fmul62(t1[2 * S.nmax + j], rowpre[0][rl]));
-      f2 = fmul62(xsv, fmul62(t2[2 * S.nmax + j], rowpre[1][rl]));
-    } else {
-      f1 = xfactor<N>(g, S, p, row0 + e / N, e % N, 1);
-      f2 = g.gauge == 1 ? xfactor<N>(g, S, p, row0 + e / N, e % N, 2) : f1;
+  if (g.gauge != 1) {
+    // the velocity gauge and imaginary time: the static factor alone, loaded one
+    // element ahead (with the potential) so that the sweep does not wait on memory
+    int4 f_next = make_int4(0, 0, 0, 0);
+    long long v_next = 0;
+    if ((int)threadIdx.x < cnt) {
+      f_next = S.xs[base + threadIdx.x];
+      if (epot) v_next = S.Vx[base + threadIdx.x];
     }
-    x = apply_f(x, f1, real_f);
-    acc_point(an, av, x, q, S.Vx, p, epot);
-    if (pre2) x = make_longlong2(fshift(x.x, pre2), fshift(x.y, pre2));
-    x = apply_f(x, f2, real_f);
-    smx[e] = x;
-    mag |= fmag(x);
+#pragma unroll 1  // a large body: unrolling costs more in instruction fetch than it gains
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      const int4 f = f_next;
+      const long long v = v_next;
+      if (e + (int)blockDim.x < cnt) {
+        f_next = S.xs[base + e + blockDim.x];
+        if (epot) v_next = S.Vx[base + e + blockDim.x];
+      }
+      longlong2 x = fconj(smx[e]);
+      if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+      x = fapply(x, f, real_f);
+      acc_point_v(an, av, x, q, v, epot);
+      if (pre2) x = make_longlong2(fshift(x.x, pre2), fshift(x.y, pre2));
+      x = fapply(x, f, real_f);
+      smx[e] = x;
+      mag |= fmag(x);
+    }
+  } else {
+#pragma unroll 1
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+      longlong2 x = fconj(smx[e]);
+      if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
+      x = half(x, e, 1);
+      acc_point(an, av, x, q, S.Vx, base + e, epot);
+      if (pre2) x = make_longlong2(fshift(x.x, pre2), fshift(x.y, pre2));
+      x = half(x, e, 2);
+      smx[e] = x;
+      mag |= fmag(x);
+    }
   }
   dacc[0] = acc_value(an);
   dacc[1] = acc_value(av);
   dacc[3] = (double)(2 * q - 2 * sy);
   dacc[4] = (double)(2 * q - 2 * sy + 50 - S.vshift);
-  scale = sy + pre2 - xfactor_exp(g, S, 2);
+  scale = sy + pre2 - xfactor_exp(g, S, 2) - xshift(kf);
   bits = block_max_int(bitlen(mag), red);
 }
 
@@ -1076,11 +1156,11 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
       const long long p = base + e;
       longlong2 x = smx[e];
       if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-      x = apply_f(x, xfactor<N>(g, S, p, row0 + e / N, e % N, 2), real_f);
+      x = xhalf<N>(g, S, x, p, row0 + e / N, e % N, 2, real_f);
       smx[e] = x;
       mag |= fmag(x);
     }
-    scale += pre - xfactor_exp(g, S, 2);
+    scale += pre - xhalf_exp(g, S, 2);
     bits = block_max_int(bitlen(mag), red);
   }
   sh = first_pass_shift<N>(bits);
@@ -1099,7 +1179,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
 // of the tile at smx[i * ldc + c]), written conjugated so that the inverse transform
 // runs as a forward one; returns the exponent change and the new bit length.
 __device__ __forceinline__ int p_phase(const GridDev& g, const StepDev& S, longlong2* smx, int ax, int rows, int Ch,
-                                       int ldc, const longlong2* pcol, int* red, int& bits) {
+                                       int ldc, const int4* pcol, int* red, int& bits) {
   const bool real_f = S.mode == 1;
   const int pre = product_headroom(bits);
   const int cnt = rows * Ch;
@@ -1110,12 +1190,13 @@ __device__ __forceinline__ int p_phase(const GridDev& g, const StepDev& S, longl
     const int i = w.i, c = w.c;
     longlong2 x = smx[i * ldc + c];
     if (pre) x = make_longlong2(fshift(x.x, pre), fshift(x.y, pre));
-    const longlong2 f = pcol ? fmul62(S.ptab[(size_t)ax * S.nmax + i], pcol[c]) : S.ptab[(size_t)ax * S.nmax + i];
-    x = fconj(apply_f(x, f, real_f));
+    x = fapply(x, S.ptab[(size_t)ax * S.nmax + i], real_f);
+    if (pcol) x = fapply(x, pcol[c], real_f);
+    x = fconj(x);
     smx[i * ldc + c] = x;
     mag |= fmag(x);
   }
-  int pe = 0;
+  int pe = xshift(pcol ? 2 : 1);
   for (int d = 0; d < g.dim; ++d) pe += S.texp[d];
   bits = block_max_int(bitlen(mag), red);
   return pre - pe;
@@ -1138,7 +1219,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
   extern __shared__ longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32];
-  __shared__ longlong2 pcol[64];
+  __shared__ int4 pcol[64];
   const AxisDev& a = g.ax[ax];
   const long long inner = a.stride;
   const long long tiles_per_outer = (inner + C - 1) / C;
@@ -1195,9 +1276,9 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
     for (int d2 = g.dim - 1; d2 > ax; --d2) {
       const int i = (int)(cc % g.ax[d2].n);
       cc /= g.ax[d2].n;
-      f = fmul62(f, S.ptab[(size_t)d2 * S.nmax + i]);
+      f = fmul62(f, tw_join(S.ptab[(size_t)d2 * S.nmax + i]));
     }
-    pcol[threadIdx.x] = f;
+    pcol[threadIdx.x] = split_fx(f);
   }
   int sh = first_pass_shift<N>(bits);
   scale += sh;
