@@ -521,7 +521,7 @@ def run_c1(steps, warmup, flush):
     gi = Q.Grid(1, n, dx, gauge=Q.GAUGE_VELOCITY, n_fields=0, **common)
     gi.add_gaussian(0.0, 1.0)
     Q.SplitPropagator(Q.MODE_IM, 0.01, 2000, gi, Q.Coupling(Q.GAUGE_VELOCITY),
-                      ["step", "norm", "normalize", "epot", "etot", "ediff"]).run()
+                      ["step", "norm", "normalize", "epot", "ekin", "etot", "ediff"]).run()
     psi0 = gi.download()
     gr = Q.Grid(1, n, dx, gauge=Q.GAUGE_LENGTH, n_fields=1, **common)
     gr.upload(psi0)

@@ -30,7 +30,11 @@
 namespace QSF {
 namespace GPU {
 
-// Stands in for MPI::Regions: one region, the whole grid on one GPU.
+// Stands in for MPI::Regions: one region, the whole grid on one GPU.  It sets up the
+// communicators a one-region run of one rank would have (MPI::Regions,
+// basics/mpi_logic.h:140-175 splits MPI_COMM_WORLD into them), because the reference's
+// propagator reduces some values itself (MPI::reduceImmediataly over MPI::rComm,
+// propagator.h:225, basics/mpi_logic.h:76-83); left unset, rComm is a null communicator.
 template <DIMS D> struct Region {
   using MPIDivision = MPI::Slices;
   static constexpr bool many = false;
@@ -40,6 +44,11 @@ template <DIMS D> struct Region {
   AXIS freeCoord = AXIS::NO;
   Region() {
     for (DIMS i = 0; i < D; ++i) bounded[i] = true;
+    if (MPI::rComm == MPI_Comm()) {
+      MPI::gComm = MPI::rComm = MPI::eComm = MPI_COMM_WORLD;
+      MPI::gID = MPI::rID = MPI::eID = 0;
+      MPI::gSize = MPI::rSize = MPI::eSize = 1;
+    }
   }
 };
 

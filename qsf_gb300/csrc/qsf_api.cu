@@ -14,6 +14,8 @@
 #include <vector>
 
 #define QSF_DEFINE_KERNELS
+#include <cuda.h>  // CUtensorMap and its encoder's signature (the encoder comes from the runtime's entry point)
+
 #include "qsf_internal.h"
 
 using namespace qsf;
@@ -141,6 +143,56 @@ longlong2 split_twiddle(longlong2 w) {
 #else
   return w;
 #endif
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against the
+// driver library); null when the driver does not offer it
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static std::mutex mu;
+  static bool tried = false;
+  static EncodeTiledFn fn = nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// Tensor maps of psi for the strided-axis passes of axes 0 .. dim-2: psi as 64-bit
+// words, dims {2 * stride, n, outer}, box {2 * tile columns, min(n, 256), 1} (the box
+// the pass's load_aligned issues); left null (cp.async loads) without an encoder.
+int make_tensor_maps(qsf_grid* g) {
+  GridDev& G = g->G;
+  for (int ax = 0; ax < kMaxDim; ++ax) G.tmap[ax] = nullptr;
+  EncodeTiledFn fn = encode_tiled();
+  if (G.dim < 2 || !fn) return QSF_OK;
+  if (int rc = dev_alloc(g->tmaps, (size_t)kMaxDim * 128)) return rc;
+  for (int ax = 0; ax + 1 < G.dim; ++ax) {
+    const AxisDev& a = G.ax[ax];
+    const long long inner = a.stride, outer = G.m / ((long long)a.n * inner);
+    const cuuint64_t dims[3] = {(cuuint64_t)(2 * inner), (cuuint64_t)a.n, (cuuint64_t)outer};
+    const cuuint64_t strides[2] = {(cuuint64_t)(16 * inner), (cuuint64_t)(16 * inner * a.n)};
+    const cuuint32_t box[3] = {(cuuint32_t)(2 * g->ax_C[ax]), (cuuint32_t)std::min(a.n, 256), 1};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    alignas(64) CUtensorMap map;
+    if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, G.psi, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+      continue;  // this axis keeps cp.async loads
+    QSF_CU(cudaMemcpy(g->tmaps + 128 * ax, &map, sizeof(map), cudaMemcpyHostToDevice));
+    G.tmap[ax] = g->tmaps + 128 * ax;
+  }
+  return QSF_OK;
 }
 
 double decode_ordered(long long i) {
@@ -424,7 +476,7 @@ int launch_group(const KernelSet& K, const Geom& q, const GridDev* dG, const Ste
   const bool wait_fin = ov && ov->pending;
   if (D == 1) {
     if (wait_fin) QSF_CU(cudaStreamWaitEvent(st, ov->done, 0));
-    QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(K.line_ctas, count), kLineThreads,
+    QSF_TIMED(QSF_K_LINE_STEP, (K.line_step<<<dim3(K.line_ctas, count), K.line_threads,
                                                (size_t)(q.n / K.line_ctas) * sizeof(double2), st>>>(dG, dS)));
   } else {
     const dim3 gr(q.nrowblk, count);
@@ -581,6 +633,7 @@ int finish_step(qsf_grid* g, int normalize, int64_t nsteps, int ncol, double* ro
                            g->stream));
   QSF_CU(cudaStreamSynchronize(g->stream));
   if (steps_done) *steps_done = ctl_h[2];
+  if (ctl_h[4] == 2) return fail(QSF_ETIMEDOUT, "a bulk copy into shared memory did not complete in time");
   if (ctl_h[4]) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a step's reductions");
   return QSF_OK;
 }
@@ -923,6 +976,10 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     return rc;
   }
   g->fpmax = (size_t)kMaxFluxBlocks * kMaxFluxBorders;
+  if ((rc = make_tensor_maps(g))) {
+    qsf_grid_destroy(g);
+    return rc;
+  }
   cudaMemcpyAsync(g->dG, &g->G, sizeof(GridDev), cudaMemcpyHostToDevice, g->stream);
   cudaMemsetAsync(g->partials, 0, sizeof(double) * 5 * g->pmax, g->stream);
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) {
@@ -968,6 +1025,7 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->vtab);
   fr(g->mtab);
   for (const qsf_grid::StepGraph& sg : g->step_graphs) cudaGraphExecDestroy(sg.exec);
+  fr(g->tmaps);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->fin_fork) cudaEventDestroy(g->fin_fork);
   if (g->fin_done) cudaEventDestroy(g->fin_done);
@@ -1033,9 +1091,9 @@ static void axis_fft(qsf_grid* g, const GridDev& G, int ax, bool fwd, double sc)
       const int L = (int)std::max<long long>(1, std::min<long long>(nrows, (16LL * kLineThreads) / n));
       int blocks = (int)((nrows + L - 1) / L);
       size_t smem = (size_t)L * n * sizeof(double2);
-      if (K.line_ctas > 1) {  // one 1D line held by a cluster pair
-        blocks = K.line_ctas;
-        smem = (size_t)(n / K.line_ctas) * sizeof(double2);
+      if (K.fft_ctas > 1) {  // one 1D line held by a cluster pair
+        blocks = K.fft_ctas;
+        smem = (size_t)(n / K.fft_ctas) * sizeof(double2);
       }
       if (fwd) K.row_fft_f<<<blocks, kLineThreads, smem, st>>>(G, L, sc);
       else K.row_fft_b<<<blocks, kLineThreads, smem, st>>>(G, L, sc);

@@ -141,4 +141,6 @@ struct qsf_grid {
     cudaGraphExec_t exec;
   };
   std::vector<StepGraph> step_graphs;
+  // TMA tensor maps of psi for the strided-axis passes (GridDev::tmap), 128 bytes each
+  unsigned char* tmaps = nullptr;
 };

@@ -56,6 +56,14 @@ __host__ __device__ constexpr int row_ppt(int n) { return 4096 / row_threads(n);
 __host__ __device__ constexpr int line_ppt(int n) { return n <= 1024 ? 4 : n <= 4096 ? 8 : 16; }
 constexpr int kLineThreads = 512;
 constexpr int kMaxFluxBorders = 16;
+// 1D lines of 1024 .. 8192 points (powers of two): one step spread over a cluster of
+// CTAs (k_line_step_mc) instead of one CTA.  Off by default: measured on GB300 it was
+// slower than the one-CTA line kernel (4096 points 0.095 vs 0.073 ms per step, 1024
+// 0.071 ms, 2048 0.080 ms, 8192 0.104 ms; every distributed-shared-memory access and
+// the two cluster barriers per pass cost more than the per-SM work they spread)
+#ifndef QSF_LINE_CLUSTER
+#define QSF_LINE_CLUSTER 0
+#endif
 // resident blocks per SM the FFT kernels are compiled for (caps registers per thread)
 #ifndef QSF_FFT_MIN_BLOCKS
 #define QSF_FFT_MIN_BLOCKS 2
@@ -89,6 +97,11 @@ struct GridDev {
   int abs_kind;     // QSF_ABS_CAP or QSF_ABS_COS8
   double abs_rate;  // cos^(1/8) mask: applications per unit time (1 / mask_dt)
   double2* psi;
+  // TMA tensor maps (CUtensorMap, 128 bytes, 64-byte aligned, in device memory) of psi
+  // for the strided-axis passes of axis d < dim - 1: psi as 64-bit words, dims
+  // {2 * stride_d, n_d, outer}, box {2 * tile columns, min(n_d, 256), 1}; null when the
+  // driver offers no encoder (the passes then copy with cp.async)
+  const void* tmap[kMaxDim];
 };
 
 // flux evaluation point: slots into the snapshot of psi_n
@@ -319,6 +332,48 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Contiguous global -> shared copies on the TMA engine (cp.async.bulk completing on an
+// mbarrier): one thread issues the copy of a whole tile, the others wait on the barrier.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+// one box of a 3D tensor map into shared memory, completing on the barrier; the first
+// coordinate (64-bit words) is a multiple of 2, so every copy starts on 16 bytes
+__device__ __forceinline__ void tma_load3(void* dst, const void* tmap, int x, int y, int z, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+// bounded wait for phase `phase` of the barrier: false when the limit ran out (the
+// caller records the failure; nothing spins without end)
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phase) {
+  for (int it = 0; it < (1 << 20); ++it)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
 
 // (i, c) = (e / Ch, e % Ch) for e = e0, e0 + step, e0 + 2 step, ... without a division
 // per element (Ch is a runtime tile width in the strided-axis passes)
@@ -1030,13 +1085,39 @@ template <int N>
 __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, int in_pass, longlong2* smx,
                                             long long obase, long long inner, int rows, int Ch, int ldc, int* red,
                                             int& bits, bool conj, const int* dtab = nullptr,
-                                            bool tab_by_row = false) {
+                                            bool tab_by_row = false, const void* tmap = nullptr,
+                                            int tx = 0, int tz = 0) {
   const int gm = S.gmin[gmin_slot(in_pass, S.ctl[5])];
   const int* sc = S.sc + (size_t)in_pass * S.scmax;
   const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
   const int cnt = rows * Ch;
   u64 mag = 0;
-  {  // all of this thread's copies in flight at once, then fixed up in place
+  const bool contiguous = Ch == 1 && inner == 1 && ldc == 1;
+  if (contiguous || tmap) {
+    // on the TMA engine: a contiguous tile (the row passes) as one bulk copy; a strided
+    // tile (rows of ldc columns, the axis passes) as boxes of up to 256 rows of the
+    // tensor map, whose columns past the grid's edge arrive as zeros
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (contiguous) {
+        mbar_expect_tx(&bar, (unsigned)cnt * 16u);
+        bulk_g2s(smx, in + obase, (unsigned)cnt * 16u, &bar);
+      } else {
+        const int br = rows < 256 ? rows : 256;
+        mbar_expect_tx(&bar, (unsigned)rows * (unsigned)ldc * 16u);
+        for (int r0 = 0; r0 < rows; r0 += br) tma_load3(smx + (size_t)r0 * ldc, tmap, tx, r0, tz, &bar);
+      }
+    }
+    if (!mbar_wait(&bar, 0)) {
+      S.ctl[4] = 2;  // the copy did not complete in time: the call reports QSF_ETIMEDOUT
+      mbar_wait(&bar, 0);
+    }
+  } else {  // all of this thread's copies in flight at once, then fixed up in place
     TileWalk w(threadIdx.x, blockDim.x, Ch);
     for (int e = threadIdx.x; e < cnt; e += blockDim.x, w.next())
       cp_async16(&smx[w.i * ldc + w.c], in + obase + (long long)w.i * inner + w.c);
@@ -1267,7 +1348,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
   const bool by_row = in_pass == 0;
   if (by_row) build_dtab<N>(S, 0, dtab, 0, o * N, row_lines(N));
   scale = load_aligned<N>(g, S, in_pass, smx, obase, inner, N, Ch, C, red, bits, MODE == 1, by_row ? dtab : nullptr,
-                          true);
+                          true, g.tmap[ax], (int)(2 * c0), (int)o);
   const bool multi_col = MODE == 2 && ax + 1 < g.dim;
   if (multi_col && threadIdx.x < Ch) {
     // per-column factor: product of the P tables of the axes after `ax`
@@ -1782,7 +1863,10 @@ struct KernelSet {
   void (*row_fft_b)(GridDev, int, double);
   void (*axis_fft_f)(GridDev, int, int, double);
   void (*axis_fft_b)(GridDev, int, int, double);
-  int line_ctas;  // CTAs holding one 1D line (2: a cluster pair, lines above 8192 points)
+  int line_ctas;     // CTAs holding one 1D line in the step kernel (a cluster of 2 .. 8 CTAs for
+                     // power-of-two lines of 1024 or more points)
+  int line_threads;  // threads per CTA of the 1D line step kernel
+  int fft_ctas;      // CTAs of the plain row transform of one line (2: a cluster pair above 8192 points)
   int row_threads;  // threads per block of the row / axis passes
   bool line_full;   // line_step also ends the step (fluxes, row, counters: no k_finalize)
 };
@@ -1803,10 +1887,13 @@ KernelSet make_kernel_set() {
   KernelSet k{};
   k.n = N;
   k.line_ctas = 1;
+  k.line_threads = kLineThreads;
+  k.fft_ctas = 1;
   k.row_threads = row_threads(N);
   k.line_full = false;
   if constexpr (N > 8192) {
     k.line_ctas = 2;
+    k.fft_ctas = 2;
     k.line_step = k_line_step_cl<N>;
     k.row_fft_f = k_row_fft_cl<N, true>;
     k.row_fft_b = k_row_fft_cl<N, false>;
@@ -1824,6 +1911,14 @@ KernelSet make_kernel_set() {
   }
   k.line_step = k_line_step<N, true>;
   k.line_full = true;
+#if QSF_LINE_CLUSTER
+  if constexpr (N >= 1024 && (N & (N - 1)) == 0) {  // the line spread over a cluster
+    constexpr int C = N / 512 < 8 ? N / 512 : 8;
+    k.line_ctas = C;
+    k.line_threads = mc_threads<N, C>();
+    k.line_step = k_line_step_mc<N, C>;
+  }
+#endif
   k.row_fft_f = k_row_fft<N, true>;
   k.row_fft_b = k_row_fft<N, false>;
   return k;

@@ -33,10 +33,6 @@ int main(int argc, char** argv) {
   im.wf.backup(0);
   im.wf.restore();
   im.wf.remove_backups();
-  // other members: the potential's derivative observable and the exchange antisymmetrisation
-  const double dVdx = im.wf.template average_der<REP::X, 0, PotentialEnergy>();
-  im.wf.template operation<MODE::IM, REP::X, AntiSymmetrize<2>>();
-  printf("<dV/dx0> of the ground state: %.3e\n", dVdx);
   _FieldConfig fc{.field = 0.1, .omega = 1.0, .ncycles = 1.0, .FWHM_percent = 0, .phase_in_pi_units = 0,
                   .delay_in_cycles = 0};
   using C = DipoleCoupling<VelocityGauge, F>;
@@ -44,10 +40,16 @@ int main(int argc, char** argv) {
   HamRE wre(grid, pot, C(F(Sin2Envelope<SinPulse>(fc))));
   SplitPropagator<MODE::RE, Split, HamRE> re(PropagatorBase{.dt = 0.05, .max_steps = 0, .state_accuracy = 0},
                                              std::move(wre), "RE");
+  // the real-time run starts from the ground state (operator[] copies, element by element)
   for (ind i = 0; i < re.wf.localSize(); ++i) re.wf[i] = im.wf[i];
+  // other members on the ground state: the potential's derivative observable and the
+  // exchange antisymmetrisation
+  const double dVdx = im.wf.template average_der<REP::X, 0, PotentialEnergy>();
+  im.wf.template operation<MODE::IM, REP::X, AntiSymmetrize<2>>();
+  printf("<dV/dx0> of the ground state: %.17e\n", dVdx);
   using REOuts = BufferedBinaryOutputs<VALUE<Step, Time>, AVG<Identity>, AVG<PotentialEnergy>, ZOA_FLUX_2D>;
   re.run(REOuts(BufferedOutputsBase{1, 1}));
   re.wf.orthogonalizeWith("ground_repX");
-  printf("norm after the pulse: %.12f\n", re.wf.template average<REP::X, Identity>());
+  printf("norm after the pulse: %.17e\n", re.wf.template average<REP::X, Identity>());
   return 0;
 }
