@@ -86,7 +86,13 @@ static void fft_line(orc_cx* x, orc_cx* y, long n, int sign) {
   orc_cx* in = x;
   orc_cx* out = y;
   long ns = 1;
-  orc_cx v[64], u[64];
+  /* butterfly buffers: on the stack for radices up to 64, else on the heap (a prime
+   * length is one radix-n pass, a direct DFT, as FFTW plans any n) */
+  int maxr = 0;
+  for (int s = 0; s < p->nstage; ++s) maxr = p->radix[s] > maxr ? p->radix[s] : maxr;
+  orc_cx vs[64], us[64];
+  orc_cx* v = maxr <= 64 ? vs : (orc_cx*)malloc(sizeof(orc_cx) * (size_t)maxr);
+  orc_cx* u = maxr <= 64 ? us : (orc_cx*)malloc(sizeof(orc_cx) * (size_t)maxr);
   for (int s = 0; s < p->nstage; ++s) {
     int r = p->radix[s];
     long nr = n / r;
@@ -128,6 +134,8 @@ static void fft_line(orc_cx* x, orc_cx* y, long n, int sign) {
     orc_cx* t = in; in = out; out = t;
   }
   if (in != x) memcpy(x, in, sizeof(orc_cx) * (size_t)n);
+  if (v != vs) free(v);
+  if (u != us) free(u);
 }
 
 /* In-place transform along the axes d with use[d] != 0 (all axes: use == NULL) of a

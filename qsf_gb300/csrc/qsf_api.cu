@@ -169,8 +169,8 @@ EncodeTiledFn encode_tiled() {
 }
 
 // Tensor maps of psi for the strided-axis passes of axes 0 .. dim-2: psi as 64-bit
-// words, dims {2 * stride, n, outer}, box {2 * tile columns, min(n, 256), 1} (the box
-// the pass's load_aligned issues); left null (cp.async loads) without an encoder.
+// words, dims {2 * stride, n, outer}, box {2 * tile columns, tma_box_rows(n), 1} (the
+// boxes the pass's load_aligned issues); left null (cp.async loads) without an encoder.
 int make_tensor_maps(qsf_grid* g) {
   GridDev& G = g->G;
   for (int ax = 0; ax < kMaxDim; ++ax) G.tmap[ax] = nullptr;
@@ -182,7 +182,7 @@ int make_tensor_maps(qsf_grid* g) {
     const long long inner = a.stride, outer = G.m / ((long long)a.n * inner);
     const cuuint64_t dims[3] = {(cuuint64_t)(2 * inner), (cuuint64_t)a.n, (cuuint64_t)outer};
     const cuuint64_t strides[2] = {(cuuint64_t)(16 * inner), (cuuint64_t)(16 * inner * a.n)};
-    const cuuint32_t box[3] = {(cuuint32_t)(2 * g->ax_C[ax]), (cuuint32_t)std::min(a.n, 256), 1};
+    const cuuint32_t box[3] = {(cuuint32_t)(2 * g->ax_C[ax]), (cuuint32_t)tma_box_rows(a.n), 1};
     const cuuint32_t elem[3] = {1, 1, 1};
     alignas(64) CUtensorMap map;
     if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, G.psi, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -194,6 +194,41 @@ int make_tensor_maps(qsf_grid* g) {
   }
   return QSF_OK;
 }
+
+}  // namespace
+
+bool qsf::fused_length(int n) { return init_kernel_table() == QSF_OK && kernels_for(n) != nullptr; }
+
+// FP64, 2^62 fixed-point and split-form twiddles exp(-2 pi i t / n), t < n
+int qsf::make_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf) {
+  std::vector<double2> h((size_t)n);
+  std::vector<longlong2> hx((size_t)n), hf((size_t)n);
+  const long double twopi = 6.283185307179586476925286766559005768L;
+  const long double q62 = 4611686018427387904.0L;
+  for (int t = 0; t < n; ++t) {
+    const long double ang = twopi * (long double)t / (long double)n;
+    const long double c = cosl(ang), sn = -sinl(ang);
+    h[(size_t)t] = make_double2((double)c, (double)sn);
+    hx[(size_t)t] = make_longlong2(llroundl(c * q62), llroundl(sn * q62));
+    hf[(size_t)t] = split_twiddle(hx[(size_t)t]);
+  }
+  *tw = nullptr;
+  *twx = *twf = nullptr;
+  int rc;
+  if ((rc = dev_alloc(*tw, h.size())) || (rc = dev_alloc(*twx, hx.size())) || (rc = dev_alloc(*twf, hf.size()))) {
+    if (*tw) cudaFree(*tw);
+    if (*twx) cudaFree(*twx);
+    *tw = nullptr;
+    *twx = nullptr;
+    return rc;
+  }
+  QSF_CU(cudaMemcpy(*tw, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  QSF_CU(cudaMemcpy(*twx, hx.data(), hx.size() * sizeof(longlong2), cudaMemcpyHostToDevice));
+  QSF_CU(cudaMemcpy(*twf, hf.data(), hf.size() * sizeof(longlong2), cudaMemcpyHostToDevice));
+  return QSF_OK;
+}
+
+namespace {
 
 double decode_ordered(long long i) {
   if (i < 0) i ^= 0x7fffffffffffffffLL;
@@ -826,8 +861,12 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
       return fail(QSF_EINVAL, "multi-region grids need a reduced-dimensionality interaction (no partial Coulomb)");
   }
   if (int rc = init_kernel_table()) return rc;
+  // lengths without fused kernels (not in the built list, or with a prime factor above
+  // 5) take Bluestein transforms and the member-operation step
   const KernelSet* ks = kernels_for((int)d->n[0]);
-  if (!ks) return fail(QSF_EINVAL, "grid size " + std::to_string(d->n[0]) + " has no kernels in this build");
+  if (!ks && !bs_size((int)d->n[0], d->dim))
+    return fail(QSF_EINVAL, "grid size " + std::to_string(d->n[0]) + " has no kernels and no Bluestein length in "
+                            "this build (1D lines up to 8192 points, other grids up to 2048 points per axis)");
   qsf_grid* g = new qsf_grid();
   g->desc = *d;
   g->ks = ks;
@@ -866,37 +905,12 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     a.dp = 2.0 * M_PI / (double)d->n[k] / d->dx[k];
     auto it = tws.find(a.n);
     if (it == tws.end()) {
-      std::vector<double2> h((size_t)a.n);
-      std::vector<longlong2> hx((size_t)a.n), hf((size_t)a.n);
-      const long double twopi = 6.283185307179586476925286766559005768L;
-      const long double q62 = 4611686018427387904.0L;
-      for (int t = 0; t < a.n; ++t) {
-        const long double ang = twopi * (long double)t / (long double)a.n;
-        const long double c = cosl(ang), sn = -sinl(ang);
-        h[(size_t)t] = make_double2((double)c, (double)sn);
-        hx[(size_t)t] = make_longlong2(llroundl(c * q62), llroundl(sn * q62));
-        hf[(size_t)t] = split_twiddle(hx[(size_t)t]);
-      }
       double2* dptr = nullptr;
       longlong2 *xptr = nullptr, *fptr = nullptr;
-      if (int rc = dev_alloc(dptr, h.size())) {
+      if (int rc = make_twiddles(a.n, &dptr, &xptr, &fptr)) {
         qsf_grid_destroy(g);
         return rc;
       }
-      if (int rc = dev_alloc(xptr, hx.size())) {
-        cudaFree(dptr);
-        qsf_grid_destroy(g);
-        return rc;
-      }
-      if (int rc = dev_alloc(fptr, hf.size())) {
-        cudaFree(dptr);
-        cudaFree(xptr);
-        qsf_grid_destroy(g);
-        return rc;
-      }
-      cudaMemcpy(dptr, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice);
-      cudaMemcpy(xptr, hx.data(), hx.size() * sizeof(longlong2), cudaMemcpyHostToDevice);
-      cudaMemcpy(fptr, hf.data(), hf.size() * sizeof(longlong2), cudaMemcpyHostToDevice);
       g->tw_owned.push_back(dptr);
       g->twx_owned.push_back(xptr);
       g->twx_owned.push_back(fptr);
@@ -956,7 +970,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
       g->ax_smem[ax] = (size_t)a.n * C * sizeof(double2);
     }
   } else {
-    g->nrowblk = ks->line_ctas;  // partial sums per CTA of the line
+    g->nrowblk = ks ? ks->line_ctas : 1;  // partial sums per CTA of the line
   }
   g->nmax = 0;
   for (int k = 0; k < D; ++k) g->nmax = std::max(g->nmax, G.ax[k].n);
@@ -976,7 +990,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     return rc;
   }
   g->fpmax = (size_t)kMaxFluxBlocks * kMaxFluxBorders;
-  if ((rc = make_tensor_maps(g))) {
+  if ((rc = ks ? make_tensor_maps(g) : bs_setup(g))) {
     qsf_grid_destroy(g);
     return rc;
   }
@@ -1026,6 +1040,7 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->mtab);
   for (const qsf_grid::StepGraph& sg : g->step_graphs) cudaGraphExecDestroy(sg.exec);
   fr(g->tmaps);
+  bs_release(g);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
   if (g->fin_fork) cudaEventDestroy(g->fin_fork);
   if (g->fin_done) cudaEventDestroy(g->fin_done);
@@ -1122,7 +1137,12 @@ int qsf_fourier(qsf_grid* g, int to_rep) {
   const double back = G.free_mask ? partial : G.inv_m;
   for (int ax = D - 1; ax >= 0; --ax) {
     if ((G.free_mask >> ax) & 1) continue;
-    axis_fft(g, G, ax, fwd, ax == last && !fwd ? back : 1.0);
+    const double post = ax == last && !fwd ? back : 1.0;
+    if (g->ks) {
+      axis_fft(g, G, ax, fwd, post);
+    } else if (int rc = bs_axis(g, ax, fwd, post)) {
+      return rc;
+    }
   }
   QSF_CU(cudaGetLastError());
   return QSF_OK;
@@ -1305,10 +1325,13 @@ int qsf_add_gaussian(qsf_grid* g, double at, double delta) {
   return QSF_OK;
 }
 
+static int generic_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done);
+
 int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done) {
   if (!g || !d) return fail(QSF_EINVAL, "null argument");
   if (steps_done) *steps_done = 0;
   if (d->nsteps == 0) return QSF_OK;
+  if (!g->ks) return generic_step(g, d, rows, steps_done);
   StepDev S{};
   int ncol = 0, rc;
   if ((rc = prepare_step(g, d, &S, &ncol))) return rc;
@@ -1375,6 +1398,116 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
   return finish_step(g, d->normalize, d->nsteps, ncol, rows, steps_done);
 }
 
+// End of one member-operation step: the flux partials summed per border in block order
+// (the order qsf_flux sums them in), the NaN / non-positive norm flag and the Normalize
+// factor, all on the device so that the steps of a call need no host synchronisation.
+__global__ void k_generic_row(const double* __restrict__ fpart, int nfblk, int nb, double dV, double dx,
+                              double* __restrict__ row, long long* __restrict__ flag, double* __restrict__ scale,
+                              int normalize) {
+  if ((int)threadIdx.x < nb) {
+    double v = 0.0;
+    for (int k = 0; k < nfblk; ++k) v += fpart[k * kMaxFluxBorders + threadIdx.x];
+    row[3 + threadIdx.x] = v * dV / dx;
+  }
+  if (threadIdx.x == 0) {
+    const double norm = row[0];
+    if (!(norm > 0.0) || isnan(row[1]) || isnan(row[2])) *flag = 1;
+    *scale = normalize && norm > 0.0 ? sqrt(1.0 / norm) : 1.0;
+  }
+}
+
+// The Strang steps of a grid without fused kernels, through the member operations
+// (the reference's own sequence: evolve<X>(dt/2), fourier<P>, evolve<P>(dt),
+// fourier<X>, evolve<X>(dt/2), propagator.h:311-346), with the same descriptor, rows,
+// Normalize, E_kin interval and convergence rule as the fused path.  Observables
+// reduce into device rows; the host waits once per call (and once per step that runs
+// the imaginary-time convergence test).
+static int generic_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done) {
+  if (d->mode != QSF_MODE_IM && d->mode != QSF_MODE_RE) return fail(QSF_EINVAL, "mode must be IM or RE");
+  if (d->nsteps < 1) return fail(QSF_EINVAL, "nsteps < 1");
+  if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
+  if (d->substeps < 0 || d->substeps > 64) return fail(QSF_EINVAL, "substeps must be in [0, 64]");
+  if (d->ekin_interval < 0) return fail(QSF_EINVAL, "ekin_interval must be >= 0");
+  if (g->G.free_mask)
+    return fail(QSF_EINVAL, "a region with free axes keeps them in momentum space: step it with the member operations");
+  const GridDev& G = g->G;
+  const bool lg = G.gauge == QSF_GAUGE_LENGTH;
+  const int K = std::max(1, d->substeps), cs = lg ? 6 : 3;
+  const double dts = d->dt / K;
+  const bool want_flux = (d->obs & QSF_OBS_FLUX) && d->nborders > 0;
+  const int nb = want_flux ? d->nborders : 0, ncol = 3 + nb;
+  const int every = d->ekin_interval > 1 ? d->ekin_interval : 1;
+  const bool conv = d->mode == QSF_MODE_IM && d->state_accuracy > 0.0;
+  const double zero[3] = {0.0, 0.0, 0.0};
+  int rc;
+  if (nb && (rc = ensure_flux(g, nb, d->border_types, d->box_size))) return rc;
+  if ((rc = dev_reserve(g->rows_dev, g->rows_cap, (size_t)d->nsteps * ncol))) return rc;
+  QSF_CU(cudaMemsetAsync(g->rows_dev, 0, (size_t)d->nsteps * ncol * sizeof(double), g->stream));
+  QSF_CU(cudaMemsetAsync(g->ctl + 4, 0, sizeof(long long), g->stream));
+  double last_e = d->last_energy;
+  int64_t stop_after = d->nsteps;  // set by the convergence rule
+  int64_t s = 0;
+  for (; s < d->nsteps && s <= stop_after; ++s) {
+    const double* row_c = nullptr;
+    for (int k = 0; k < K; ++k) {
+      const double* cp = d->coupling ? d->coupling + (size_t)(s * K + k) * cs : nullptr;
+      row_c = cp;
+      const double* ex1 = lg && cp ? cp : zero;
+      const double* ex2 = lg && cp ? cp + 3 : zero;
+      const double* ap = !lg && cp ? cp : zero;
+      if ((rc = qsf_evolve(g, d->mode, QSF_REP_X, 0.5 * dts, ex1)) || (rc = qsf_fourier(g, QSF_REP_P)) ||
+          (rc = qsf_evolve(g, d->mode, QSF_REP_P, dts, ap)) || (rc = qsf_fourier(g, QSF_REP_X)) ||
+          (rc = qsf_evolve(g, d->mode, QSF_REP_X, 0.5 * dts, ex2)))
+        return rc;
+    }
+    double* row = g->rows_dev + (size_t)s * ncol;
+    int nbk = 0;
+    if ((rc = launch_average(g, QSF_REP_X, QSF_OP_IDENTITY, &nbk))) return rc;
+    k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dV, row + 0);
+    if (d->obs & QSF_OBS_EPOT) {
+      if ((rc = launch_average(g, QSF_REP_X, QSF_OP_POTENTIAL, &nbk))) return rc;
+      k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dV, row + 1);
+    }
+    const bool ek = (d->obs & QSF_OBS_EKIN) && ((s + 1) % every == 0 || s + 1 == d->nsteps || s == stop_after);
+    if (ek) {
+      if ((rc = qsf_fourier(g, QSF_REP_P)) || (rc = launch_average(g, QSF_REP_P, QSF_OP_KINETIC, &nbk))) return rc;
+      k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dVm, row + 2);
+      if ((rc = qsf_fourier(g, QSF_REP_X))) return rc;
+    }
+    if (nb && g->nfterms > 0) {
+      // fluxes of psi_n with the A of the step's last P sub-step (velocity gauge)
+      const double* A = !lg && row_c && G.n_fields ? row_c : nullptr;
+      k_gather<<<std::max(1, std::min(1024, (g->nsnap + 255) / 256)), 256, 0, g->stream>>>(G.psi, g->snap_idx,
+                                                                                           g->nsnap, g->snap);
+      k_flux<<<g->nfblk, 256, 0, g->stream>>>(G, g->fpts, g->fterms, g->nfterms, g->snap, A ? A[0] : 0.0,
+                                              A ? A[1] : 0.0, A ? A[2] : 0.0, A ? 1 : 0, nb, g->fpartials);
+    }
+    k_generic_row<<<1, 32, 0, g->stream>>>(g->fpartials, g->nfterms > 0 ? g->nfblk : 0, nb, G.dV, G.ax[0].dx, row,
+                                           g->ctl + 4, g->scale + 1, d->normalize);
+    if (d->normalize) k_scale<<<grid_blocks(G.m), 256, 0, g->stream>>>(G.psi, G.m, g->scale + 1);
+    QSF_CU(cudaGetLastError());
+    if (conv && (ek || !(d->obs & QSF_OBS_EKIN))) {
+      double r[3];
+      QSF_CU(cudaMemcpyAsync(r, row, sizeof(r), cudaMemcpyDeviceToHost, g->stream));
+      QSF_CU(cudaStreamSynchronize(g->stream));
+      const double se = (d->energy_after_normalize & 1) ? 1.0 / r[0] : 1.0;
+      const double sk = (d->energy_after_normalize & 2) ? 1.0 / r[0] : 1.0;
+      const double e = r[1] * se + r[2] * sk;
+      if (stop_after == d->nsteps && std::fabs(e - last_e) <= d->state_accuracy) stop_after = s + 1;
+      last_e = e;
+    }
+  }
+  long long flag = 0;
+  QSF_CU(cudaMemcpyAsync(&flag, g->ctl + 4, sizeof(flag), cudaMemcpyDeviceToHost, g->stream));
+  if (rows)
+    QSF_CU(cudaMemcpyAsync(rows, g->rows_dev, (size_t)d->nsteps * ncol * sizeof(double), cudaMemcpyDeviceToHost,
+                           g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  if (steps_done) *steps_done = s;
+  if (flag) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a step's reductions");
+  return QSF_OK;
+}
+
 int qsf_batch_create(void* stream, qsf_batch** out) {
   if (!out) return fail(QSF_EINVAL, "null argument");
   if (int rc = init_kernel_table()) return rc;
@@ -1410,6 +1543,7 @@ int qsf_batch_destroy(qsf_batch* b) {
 int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot) {
   if (!b || !g || !d || !slot) return fail(QSF_EINVAL, "null argument");
   if (d->substeps > 1) return fail(QSF_EINVAL, "batched solves run plain Strang steps (substeps <= 1)");
+  if (!g->ks) return fail(QSF_EINVAL, "batched grids need a line length with fused kernels in this build");
   for (auto& kv : b->members)
     if (kv.second.g == g) return fail(QSF_ESTATE, "grid is already in the batch");
   QSF_CU(cudaStreamSynchronize(b->stream));

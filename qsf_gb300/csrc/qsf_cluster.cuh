@@ -112,7 +112,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
   if (!pass_active(S)) return;  // uniform over the pair
   const bool ek = ekin_at(S, S.ctl[5]);  // read before any block advances the counters
   if (blockIdx.x % 2 == 0 && threadIdx.x == 0) S.ctl[6] = S.ctl[5] + 1;  // the sub-step's only pass
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32 * 3];
   constexpr int H = N / 2;
@@ -231,7 +231,7 @@ template <int N, bool FWD>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kLineThreads, 1)
     k_row_fft_cl(GridDev g, int L, double post_scale) {
   cg::cluster_group cl = cg::this_cluster();
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   constexpr int H = N / 2;
   const int rank = (int)cl.block_rank();
@@ -383,7 +383,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(mc_threads<N, C>(), 
   if (!pass_active(S)) return;  // uniform over the cluster
   const long long sub = S.ctl[5];
   const bool ek = ekin_at(S, sub);  // read before any block advances the counters
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32 * kMaxFluxBorders];
   const int rank = (int)cl.block_rank();

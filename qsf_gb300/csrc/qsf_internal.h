@@ -143,4 +143,42 @@ struct qsf_grid {
   std::vector<StepGraph> step_graphs;
   // TMA tensor maps of psi for the strided-axis passes (GridDev::tmap), 128 bytes each
   unsigned char* tmaps = nullptr;
+  // Bluestein transforms of a grid whose axis length has a prime factor above 5 (no
+  // fused kernels, ks == nullptr): chirp c[j] = exp(-i pi j^2 / n), the transform of
+  // the convolution kernel conj(c) padded to M (a length >= 2n - 1 with built
+  // kernels), the M-point kernels and twiddles, and a scratch of (m / n) * M points.
+  // A 1D line longer than 8192 points takes M = M1 * M2 above 16384 as a four-step
+  // transform: M1-point transforms along the columns of the [M1][M2] view, the twiddles
+  // exp(-2 pi i k1 n2 / M), M2-point transforms along its rows (the output in the
+  // transposed order [k1][k2] = X[k1 + M1 k2], which the convolution does not mind).
+  struct Bluestein {
+    int n = 0, M = 0;
+    int M1 = 0, M2 = 0;  // four-step factors; 0: one M-point transform per line
+    const KernelSet* ks = nullptr;   // M-point kernels (or M2-point row kernels)
+    const KernelSet* ks1 = nullptr;  // M1-point column kernels (four-step)
+    double2* chirp = nullptr;
+    double2* bhat = nullptr;
+    double2* scratch = nullptr;
+    double2* tw = nullptr;  // twiddles of M (or M2)
+    longlong2* twx = nullptr;
+    longlong2* twf = nullptr;
+    double2* tw1 = nullptr;  // twiddles of M1
+    longlong2* twx1 = nullptr;
+    longlong2* twf1 = nullptr;
+    double2* tw4 = nullptr;  // four-step twiddles [k1][n2]
+  } bs;
 };
+
+namespace qsf {
+// whether n is a line length with fused step kernels in this build
+bool fused_length(int n);
+// twiddle tables of an n-point transform (FP64, 2^62 fixed point, split form)
+int make_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf);
+// Bluestein plan of a grid without fused kernels (qsf_bluestein.cu)
+int bs_setup(qsf_grid* g);
+void bs_release(qsf_grid* g);
+// one axis of fourier<R>() by Bluestein's chirp-z convolution, scaled by post
+int bs_axis(qsf_grid* g, int ax, bool fwd, double post);
+// the smallest built size M >= 2n - 1 that a Bluestein plan of n can use (0: none)
+int bs_size(int n, int dim);
+}  // namespace qsf

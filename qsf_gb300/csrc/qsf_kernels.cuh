@@ -99,8 +99,8 @@ struct GridDev {
   double2* psi;
   // TMA tensor maps (CUtensorMap, 128 bytes, 64-byte aligned, in device memory) of psi
   // for the strided-axis passes of axis d < dim - 1: psi as 64-bit words, dims
-  // {2 * stride_d, n_d, outer}, box {2 * tile columns, min(n_d, 256), 1}; null when the
-  // driver offers no encoder (the passes then copy with cp.async)
+  // {2 * stride_d, n_d, outer}, box {2 * tile columns, tma_box_rows(n_d), 1}; null when
+  // the driver offers no encoder (the passes then copy with cp.async)
   const void* tmap[kMaxDim];
 };
 
@@ -392,6 +392,13 @@ struct TileWalk {
 };
 
 __host__ __device__ constexpr int row_lines(int n) { return n >= 4096 ? 1 : 4096 / n; }
+// rows of one TMA box of a strided-axis tile: the largest divisor of n up to 256 (the
+// box limit), so that the boxes cover the n rows exactly and none writes past the tile
+__host__ __device__ constexpr int tma_box_rows(int n) {
+  int b = n < 256 ? n : 256;
+  while (n % b) --b;
+  return b;
+}
 __host__ __device__ constexpr int tile_cols(int n) { return (4096 / n) < 64 ? (4096 / n) : 64; }
 
 // Passes that leave the wavefunction in fixed point inside a step; each block of a
@@ -1055,7 +1062,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_open
   // the previous sub-step's closing pass produced pass 0, unless it ended with psi_n in
   // memory for E_kin
   if (S.fused && sub > 0 && !ekin_at(S, sub - 1)) return;
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   const long long row0 = (long long)blockIdx.x * L;
   const int Lh = (int)min((long long)L, g.m / N - row0);
@@ -1092,11 +1099,17 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
   const longlong2* in = reinterpret_cast<const longlong2*>(g.psi);
   const int cnt = rows * Ch;
   u64 mag = 0;
-  const bool contiguous = Ch == 1 && inner == 1 && ldc == 1;
-  if (contiguous || tmap) {
-    // on the TMA engine: a contiguous tile (the row passes) as one bulk copy; a strided
-    // tile (rows of ldc columns, the axis passes) as boxes of up to 256 rows of the
-    // tensor map, whose columns past the grid's edge arrive as zeros
+  // on the TMA engine: a contiguous tile (the row passes) as one bulk copy (shared and
+  // global addresses on 16 bytes); a strided tile (rows of ldc columns, the axis passes,
+  // rows == N) as boxes of tma_box_rows(N) rows of the tensor map, whose columns past
+  // the grid's edge arrive as zeros (each box's shared address on 128 bytes).  A tile
+  // whose addresses miss those alignments takes the cp.async loads.
+  const unsigned sa = smem_u32(smx);
+  constexpr int br = tma_box_rows(N);
+  const bool contiguous = Ch == 1 && inner == 1 && ldc == 1 && (sa & 15u) == 0 &&
+                          ((reinterpret_cast<unsigned long long>(in + obase)) & 15ull) == 0;
+  const bool boxes = tmap && rows == N && (sa & 127u) == 0 && ((unsigned)br * (unsigned)ldc * 16u) % 128u == 0;
+  if (contiguous || boxes) {
     __shared__ __align__(8) unsigned long long bar;
     if (threadIdx.x == 0) {
       mbar_init(&bar, 1);
@@ -1108,7 +1121,6 @@ __device__ __forceinline__ int load_aligned(const GridDev& g, const StepDev& S, 
         mbar_expect_tx(&bar, (unsigned)cnt * 16u);
         bulk_g2s(smx, in + obase, (unsigned)cnt * 16u, &bar);
       } else {
-        const int br = rows < 256 ? rows : 256;
         mbar_expect_tx(&bar, (unsigned)rows * (unsigned)ldc * 16u);
         for (int r0 = 0; r0 < rows; r0 += br) tma_load3(smx + (size_t)r0 * ldc, tmap, tx, r0, tz, &bar);
       }
@@ -1162,7 +1174,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_clos
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
   if (!pass_active(S)) return;
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32 * 3];
   const AxisDev& a = g.ax[g.dim - 1];
@@ -1297,7 +1309,7 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(con
   const StepDev& S = Ss[blockIdx.y];
   if (!pass_active(S)) return;
   if (MODE == 3 && !ekin_at(S, S.ctl[5])) return;
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32];
   __shared__ int4 pcol[64];
@@ -1394,7 +1406,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
   const StepDev& S = Ss[blockIdx.y];
   if (!pass_active(S)) return;
   if (threadIdx.x == 0) S.ctl[6] = S.ctl[5] + 1;  // the sub-step's only pass
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   __shared__ double dred[32 * kMaxFluxBorders];
   const AxisDev& a = g.ax[0];
@@ -1444,7 +1456,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
 // forward transform between two conjugations) and converts back (times post_scale).
 template <int N, bool FWD>
 __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_row_fft(GridDev g, int L, double post_scale) {
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   const AxisDev& a = g.ax[g.dim - 1];
   const long long row0 = (long long)blockIdx.x * L;
@@ -1480,7 +1492,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
 
 template <int N, bool FWD>
 __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
-  extern __shared__ longlong2 smx[];
+  extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   const AxisDev& a = g.ax[ax];
   const long long inner = a.stride;

@@ -21,6 +21,10 @@
 
 #include "qsf_gpu.h"
 
+namespace qsf {
+bool fused_length(int n);  // qsf_api.cu
+}
+
 namespace {
 
 using clk = std::chrono::steady_clock;
@@ -337,6 +341,8 @@ int qsf_server_start(const qsf_server_config* cfg, qsf_server** out) {
 
 int qsf_server_submit(qsf_server* s, const qsf_request* r, int64_t* ticket) {
   if (!s || !r || !ticket || r->nsteps < 1 || r->nborders < 0 || r->nborders > QSF_MAX_BORDERS) return QSF_EINVAL;
+  // solves advance in the batch, whose launches need fused kernels of the line length
+  if (r->grid.dim < 1 || r->grid.dim > 3 || !qsf::fused_length((int)r->grid.n[0])) return QSF_EINVAL;
   Pending p;
   p.req = *r;
   const int stride = r->grid.gauge == QSF_GAUGE_LENGTH ? 6 : 3;

@@ -1,0 +1,158 @@
+"""Axis lengths with a prime factor above 5 (Bluestein transforms, member-operation steps).
+
+The reference transforms any n through FFTW (wf/grid.h:251-274); the fused kernels of
+this library are built for 2^a 3^b 5^c.  Other lengths take one chirp-z convolution per
+axis through the built M-point transforms (M >= 2n - 1) and qsf_step runs the reference's
+own member sequence evolve<X>(dt/2), fourier<P>, evolve<P>(dt), fourier<X>,
+evolve<X>(dt/2) (propagator.h:311-346).  Checked here: transforms against numpy's FFT
+(and the inverse round trip), real-time runs with a field, absorber, fluxes and
+imaginary-time runs against the oracle (which transforms prime lengths by direct DFT),
+and the rejection of such grids by batches."""
+import numpy as np
+import pytest
+
+from tests import cases as C
+
+pytestmark = pytest.mark.gpu
+
+TOL_FFT = 4e-14
+FLUX_RES = {1: 1e-19, 2: 1e-18, 3: 1e-18}
+
+
+@pytest.mark.parametrize("n", [7, 11, 97, 100, 127, 1021, 1031, 3001, 4099, 8191, 8209, 9973, 12289, 16383])
+def test_bluestein_1d_matches_numpy(n):
+    """Up to 8191 points one M-point transform (M <= 16384); above, M = M1 * M2 as a
+    four-step transform."""
+    import qsf_gb300 as Q
+    rng = np.random.default_rng(n)
+    psi = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    g = Q.Grid(1, n, 0.1)
+    g.upload(psi)
+    g.fourier(Q.REP_P)
+    assert C.rel_l2(g.download(), np.fft.fft(psi)) < TOL_FFT
+    g.fourier(Q.REP_X)
+    assert C.rel_l2(g.download(), psi) < TOL_FFT
+    g.close()
+
+
+@pytest.mark.parametrize("dim,n", [(2, 7), (2, 63), (2, 127), (2, 1021), (3, 14), (3, 35), (3, 97)])
+def test_bluestein_nd_matches_numpy(dim, n):
+    import qsf_gb300 as Q
+    rng = np.random.default_rng(11 * n + dim)
+    shape = (n,) * dim
+    psi = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    g = Q.Grid(dim, n, 0.1)
+    g.upload(psi)
+    g.fourier(Q.REP_P)
+    assert C.rel_l2(g.download(), np.fft.fftn(psi)) < TOL_FFT
+    g.fourier(Q.REP_X)
+    assert C.rel_l2(g.download(), psi) < TOL_FFT
+    g.close()
+
+
+def _params(n, dx, lg):
+    # flux border nodes in the proportions of the golden 2D / 3D cases (48: 6, 4, 3, 15)
+    return dict(n=n, dx=dx, nCAP=max(2, n // 10), Ncharge=1.0, Echarge=-1.0, Nsoft=1.0, Esoft=1.0, F0=0.08,
+                omega=1.5, ncycles=1.0, phase=0.0, re_dt=0.05, box=n // 3, lg=lg, im_dt=0.05, im_steps=40,
+                p_NS=max(3, n // 8), p_SD=max(2, n // 12), p_DT=max(2, n // 16), p_CAP=max(6, (5 * n) // 16))
+
+
+@pytest.mark.parametrize("dim,n,lg", [(1, 1021, 0), (1, 509, 1), (1, 9009, 1), (2, 77, 0), (2, 63, 1), (3, 21, 0)])
+def test_bluestein_real_time_run_matches_oracle(dim, n, lg):
+    """A full pulse (sin^2 envelope) with absorber and fluxes: rows and final psi."""
+    dx = {1: 0.1, 2: 0.3, 3: 0.4}[dim]
+    p = _params(n, dx, lg)
+    C.set_borders(p)
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    r2 = sum(np.meshgrid(*([x * x] * dim), indexing="ij"))
+    psi0 = np.exp(-0.5 * r2).astype(np.complex128) * (1.0 + 0.3j * np.tanh(sum(np.meshgrid(*([x] * dim),
+                                                                                        indexing="ij"))))
+    psi0 /= np.sqrt(np.sum(np.abs(psi0) ** 2) * dx ** dim)
+    og, orows = C.oracle_re(p, dim, psi0)
+    g, rows = C.gpu_re(p, dim, psi0)
+    nb = len(C.re_borders(dim))
+    got = np.array([C.re_dat_row(r, nb) for r in rows])
+    ref = np.array([C.re_dat_row(r, nb) for r in orows])
+    assert got.shape == ref.shape and len(got) > 10
+    np.testing.assert_allclose(got[:, :2], ref[:, :2], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(got[:, 2:5], ref[:, 2:5], rtol=1e-10, atol=0)
+    # fluxes to 1e-9 relative above a fixed resolution (values far below it are floating-
+    # point noise of psi's tails in both the oracle and the GPU transforms)
+    np.testing.assert_allclose(got[:, 5:], ref[:, 5:], rtol=1e-9, atol=FLUX_RES[dim])
+    assert C.rel_l2(g.download(), og.psi) < 1e-11
+    g.close()
+
+
+@pytest.mark.parametrize("dim,n", [(1, 719), (2, 91)])
+def test_bluestein_imaginary_time_matches_oracle(dim, n):
+    """Ground state search with Normalize and the energy convergence rule."""
+    p = _params(n, 0.3 if dim == 2 else 0.1, 0)
+    og, orows = C.oracle_im(p, dim)
+    g, rows = C.gpu_im(p, dim)
+    got = np.array([C.im_dat_row(r) for r in rows])
+    ref = np.array([C.im_dat_row(r) for r in orows])
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got[:, 0], ref[:, 0], rtol=0, atol=0)
+    np.testing.assert_allclose(got[:, 2:], ref[:, 2:], rtol=1e-10, atol=1e-13)
+    np.testing.assert_allclose(got[1:, 1], ref[1:, 1], rtol=0, atol=1e-11)  # E_n - E_(n-1)
+    assert C.rel_l2(g.download(), og.psi) < 1e-11
+    g.close()
+
+
+def test_bluestein_step_with_ekin_interval_and_substeps():
+    """qsf_step's descriptor on a member-operation grid: E_kin every 4th step, and the
+    multi-product chain (substeps) against the same sub-steps taken one by one."""
+    import qsf_gb300 as Q
+    n, steps = 77, 12
+    g = Q.Grid(2, n, 0.3, nCAP=7, Ncharge=2.0, gauge=Q.GAUGE_VELOCITY, n_fields=0)
+    rng = np.random.default_rng(5)
+    psi0 = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    outs = {}
+    for k in (1, 4):
+        g.upload(psi0)
+        rows, done = g.step(Q.MODE_IM, 0.05, steps, None, obs=Q.OBS_NORM | Q.OBS_EPOT | Q.OBS_EKIN,
+                            normalize=True, ekin_interval=k)
+        assert done == steps
+        outs[k] = (rows.copy(), g.download())
+    (r1, p1), (r4, p4) = outs[1], outs[4]
+    # E_kin takes psi through an extra transform pair (propagator.h:284-291), so the
+    # runs agree to rounding, not bit for bit
+    np.testing.assert_allclose(r4[:, :2], r1[:, :2], rtol=1e-12, atol=0)
+    assert C.rel_l2(p4, p1) < 1e-13
+    have = np.array([(s + 1) % 4 == 0 or s == steps - 1 for s in range(steps)])
+    np.testing.assert_allclose(r4[have, 2], r1[have, 2], rtol=1e-12, atol=0)
+    assert np.all(r4[~have, 2] == 0.0) and np.all(r1[:, 2] > 0.0)
+    # K = 3 sub-steps of dt / 3 equal three plain steps of dt / 3 observed at the end
+    g.upload(psi0)
+    rk, _ = g.step(Q.MODE_IM, 0.06, 2, None, obs=Q.OBS_NORM | Q.OBS_EPOT, substeps=3)
+    g2 = Q.Grid(2, n, 0.3, nCAP=7, Ncharge=2.0, gauge=Q.GAUGE_VELOCITY, n_fields=0)
+    g2.upload(psi0)
+    rp, _ = g2.step(Q.MODE_IM, 0.02, 6, None, obs=Q.OBS_NORM | Q.OBS_EPOT)
+    np.testing.assert_allclose(rk[:, :2], rp[[2, 5], :2], rtol=1e-12)
+    assert C.rel_l2(g.download(), g2.download()) < 1e-12
+    g.close()
+    g2.close()
+
+
+def test_bluestein_grids_stay_out_of_batches():
+    import qsf_gb300 as Q
+    g = Q.Grid(2, 63, 0.3, nCAP=6)
+    g.add_gaussian(0.0, 1.0)
+    b = Q.Batch()
+    with pytest.raises(Q.QsfError) as e:
+        b.add(g, Q.MODE_IM, 0.05, 4, None, obs=Q.OBS_NORM)
+    assert e.value.code == 1
+    b.close()
+    g.close()
+
+
+def test_server_rejects_lengths_without_fused_kernels():
+    import qsf_gb300 as Q
+    from qsf_gb300 import serve as S
+    srv = S.Server(max_slots=2, steps_per_round=4)
+    try:
+        with pytest.raises(Q.QsfError) as e:
+            srv.submit(S.grid_desc(2, 63, 0.3, nCAP=6), Q.MODE_IM, 0.05, 4, None, obs=Q.OBS_NORM)
+        assert e.value.code == 1
+    finally:
+        srv.stop()

@@ -159,9 +159,12 @@ def test_fused_step_is_deterministic(Q):
 
 
 def test_bad_sizes_are_rejected(Q):
-    with pytest.raises(Q.QsfError) as e:
-        Q.Grid(1, 7, 0.1)
-    assert e.value.code == 1
+    # lengths without fused kernels run through Bluestein transforms of a length
+    # M >= 2n - 1: any 1D line up to 16384 points, up to 2048 on the axes of a 2D/3D grid
+    for dim, n in ((1, 16385), (2, 2051), (3, 2051)):
+        with pytest.raises(Q.QsfError) as e:
+            Q.Grid(dim, n, 0.1)
+        assert e.value.code == 1
     with pytest.raises(Q.QsfError):
         Q.Grid(2, [64, 32], 0.1)
     with pytest.raises(Q.QsfError):
