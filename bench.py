@@ -232,8 +232,8 @@ def cpu_baseline(all_cores: bool, budget_s: float = 20.0):
 
 # ------------------------------------------------------------------ batched / served
 BATCH_EDGES = [256, 384, 512, 768, 1024]
-SERVE_1D = [1024, 1280, 1536, 2048, 2560, 3072, 4096, 5120, 6144, 8192, 10240, 12288, 16384]
-SERVE_2D = [256, 320, 384, 512, 640, 768, 1024]
+SERVE_1D = (1024, 16384)  # 1D N uniform over the integers of this range (Bluestein lengths included)
+SERVE_2D = [256, 320, 384, 512, 640, 768, 1024]  # 2D edges with fused kernels in 256..1024
 
 
 def _gauss_state(dim, n, dx):
@@ -345,8 +345,8 @@ def run_batched(steps, warmup, nsolves=256, seed=0, plain_arm=True, ws=1, rank=0
 
 
 def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, steps_per_round=16, ws=1, rank=0):
-    """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N in 1024..16384) and 2D
-    (edge in 256..1024) solves with seeded pulses; each solve runs its first
+    """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N uniform over 1024..16384)
+    and 2D (edge in 256..1024 with fused kernels) solves with seeded pulses; each solve runs its first
     `steps_per_solve` steps.  Returns throughput and p50/p99 submit->completion.  With
     several ranks every rank follows the same seeded stream and serves the requests
     shard.StreamAssigner gives it (serve.ShardedServer)."""
@@ -367,7 +367,7 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, ste
             continue
         t_next += rng.exponential(1.0 / rate)
         dim = 1 if rng.random() < 0.5 else 2
-        n = int(rng.choice(SERVE_1D if dim == 1 else SERVE_2D))
+        n = int(rng.integers(SERVE_1D[0], SERVE_1D[1] + 1)) if dim == 1 else int(rng.choice(SERVE_2D))
         dx = 0.2 if dim == 1 else DX
         inten = 10.0 ** rng.uniform(14.0, 15.0)
         lam = rng.uniform(400.0, 1600.0)
@@ -401,8 +401,9 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, ste
     return {"rate_per_s": rate, "submitted": _sum_over_ranks(ws, len(tickets)), "completed": len(lat),
             "value": pts / wall, "unit": UNIT,
             "p50_s": pct(0.50), "p99_s": pct(0.99), "wall_s": wall,
-            "workload": f"served: Poisson {rate}/s for {duration_s}s, 50/50 1D N in [1024,16384] / 2D edge in "
-                        f"[256,1024] (2^a 3^b 5^c sizes), I log-U[1e14,1e15], lambda U[400,1600] nm, "
+            "workload": f"served: Poisson {rate}/s for {duration_s}s, 50/50 1D N uniform over the integers "
+                        f"1024..16384 (lengths outside the fused-kernel list through Bluestein transforms and "
+                        f"member operations) / 2D edge in {SERVE_2D}, I log-U[1e14,1e15], lambda U[400,1600] nm, "
                         f"{steps_per_solve} steps per solve, seed {seed}"}
 
 

@@ -6,6 +6,7 @@
 // qsf_kernels.cuh -- per step through a captured CUDA graph that a device-side step
 // counter makes reusable for every step of a call.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -225,6 +226,27 @@ int qsf::make_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf) {
   QSF_CU(cudaMemcpy(*tw, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
   QSF_CU(cudaMemcpy(*twx, hx.data(), hx.size() * sizeof(longlong2), cudaMemcpyHostToDevice));
   QSF_CU(cudaMemcpy(*twf, hf.data(), hf.size() * sizeof(longlong2), cudaMemcpyHostToDevice));
+  return QSF_OK;
+}
+
+// Twiddle tables of a length, made once per process and device and shared by every
+// grid (never freed: one set per built length, at most a few MB in all).
+int qsf::shared_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, std::array<void*, 3>> cache;
+  int dev = 0;
+  QSF_CU(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({dev, n});
+  if (it == cache.end()) {
+    double2* a = nullptr;
+    longlong2 *b = nullptr, *c = nullptr;
+    if (int rc = make_twiddles(n, &a, &b, &c)) return rc;
+    it = cache.emplace(std::make_pair(dev, n), std::array<void*, 3>{a, b, c}).first;
+  }
+  *tw = (double2*)it->second[0];
+  *twx = (longlong2*)it->second[1];
+  *twf = (longlong2*)it->second[2];
   return QSF_OK;
 }
 
@@ -904,16 +926,18 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     a.inv_2dx = (1.0 / d->dx[k]) / 2.0;
     a.dp = 2.0 * M_PI / (double)d->n[k] / d->dx[k];
     auto it = tws.find(a.n);
-    if (it == tws.end()) {
+    if (!ks) {
+      // Bluestein lengths run no n-point transform kernel: no n-point twiddles
+      a.tw = nullptr;
+      a.twx = nullptr;
+      a.twf = nullptr;
+    } else if (it == tws.end()) {
       double2* dptr = nullptr;
       longlong2 *xptr = nullptr, *fptr = nullptr;
-      if (int rc = make_twiddles(a.n, &dptr, &xptr, &fptr)) {
+      if (int rc = shared_twiddles(a.n, &dptr, &xptr, &fptr)) {
         qsf_grid_destroy(g);
         return rc;
       }
-      g->tw_owned.push_back(dptr);
-      g->twx_owned.push_back(xptr);
-      g->twx_owned.push_back(fptr);
       tws[a.n] = dptr;
       twxs[a.n] = xptr;
       twfs[a.n] = fptr;
@@ -1011,8 +1035,6 @@ int qsf_grid_destroy(qsf_grid* g) {
     if (p) cudaFree(p);
   };
   fr(g->G.psi);
-  for (double2* t : g->tw_owned) fr(t);
-  for (longlong2* t : g->twx_owned) fr(t);
   fr(g->xs);
   fr(g->Vx);
   fr(g->ibuf);
@@ -1039,6 +1061,7 @@ int qsf_grid_destroy(qsf_grid* g) {
   fr(g->vtab);
   fr(g->mtab);
   for (const qsf_grid::StepGraph& sg : g->step_graphs) cudaGraphExecDestroy(sg.exec);
+  if (g->gen_exec) cudaGraphExecDestroy(g->gen_exec);
   fr(g->tmaps);
   bs_release(g);
   if (g->mg_event) cudaEventDestroy(g->mg_event);
@@ -1140,7 +1163,7 @@ int qsf_fourier(qsf_grid* g, int to_rep) {
     const double post = ax == last && !fwd ? back : 1.0;
     if (g->ks) {
       axis_fft(g, G, ax, fwd, post);
-    } else if (int rc = bs_axis(g, ax, fwd, post)) {
+    } else if (int rc = bs_axis(g, g->G.psi, ax, fwd, post)) {
       return rc;
     }
   }
@@ -1177,7 +1200,8 @@ int qsf_region_transfer(qsf_grid* dst, const qsf_grid* src, int axis, int group)
                                                         dst->nmax);
   GridDev Gs = G;
   Gs.psi = dst->mg_slice;
-  axis_fft(dst, Gs, axis, true, 1.0);
+  if (dst->ks) axis_fft(dst, Gs, axis, true, 1.0);
+  else if (int rc = bs_axis(dst, dst->mg_slice, axis, true, 1.0)) return rc;
   k_add_slice<<<grid_blocks(G.m), 256, 0, dst->stream>>>(G.psi, dst->mg_slice, G.m);
   QSF_CU(cudaGetLastError());
   QSF_CU(cudaEventRecord(dst->mg_event, dst->stream));
@@ -1185,8 +1209,16 @@ int qsf_region_transfer(qsf_grid* dst, const qsf_grid* src, int axis, int group)
   return QSF_OK;
 }
 
+static int evolve_impl(qsf_grid* g, int mode, int rep, double delta, const double* c3, CoupDev cd);
+
 int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* c3) {
   if (!g || (mode != 1 && mode != 2) || (rep != 1 && rep != 2)) return fail(QSF_EINVAL, "bad argument");
+  return evolve_impl(g, mode, rep, delta, c3, CoupDev{nullptr, nullptr, 0, 0});
+}
+
+// evolve<mode, rep>(delta) with the coupling values from c3 (host) or, when cd.c is
+// set, from the device rows of a step program
+static int evolve_impl(qsf_grid* g, int mode, int rep, double delta, const double* c3, CoupDev cd) {
   const double c0 = c3 ? c3[0] : 0.0, c1 = c3 ? c3[1] : 0.0, c2 = c3 ? c3[2] : 0.0;
   const GridDev& G = g->G;
   if (rep == QSF_REP_X && !(G.gauge == QSF_GAUGE_LENGTH && G.n_fields)) {
@@ -1204,10 +1236,10 @@ int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* c3) {
     if (!g->eptab)
       if (int rc = dev_alloc(g->eptab, (size_t)3 * g->nmax)) return rc;
     k_evolve_ptab<<<(G.dim * g->nmax + 255) / 256, 256, 0, g->stream>>>(G, mode, delta, c0, c1, c2, g->nmax,
-                                                                        g->eptab);
+                                                                        g->eptab, cd);
     k_apply_ptab<<<grid_blocks(G.m), 256, 0, g->stream>>>(G, g->eptab, g->nmax);
   } else {
-    k_evolve<<<grid_blocks(G.m), 256, 0, g->stream>>>(G, mode, rep, delta, c0, c1, c2);
+    k_evolve<<<grid_blocks(G.m), 256, 0, g->stream>>>(G, mode, rep, delta, c0, c1, c2, cd);
   }
   QSF_CU(cudaGetLastError());
   return QSF_OK;
@@ -1295,7 +1327,8 @@ int qsf_flux(qsf_grid* g, const double* A3, int nb, const int* types, int64_t bo
     k_gather<<<std::max(1, std::min(1024, (g->nsnap + 255) / 256)), 256, 0, g->stream>>>(g->G.psi, g->snap_idx,
                                                                                          g->nsnap, g->snap);
     k_flux<<<g->nfblk, 256, 0, g->stream>>>(g->G, g->fpts, g->fterms, g->nfterms, g->snap, A3 ? A3[0] : 0.0,
-                                            A3 ? A3[1] : 0.0, A3 ? A3[2] : 0.0, A3 ? 1 : 0, nb, g->fpartials);
+                                            A3 ? A3[1] : 0.0, A3 ? A3[2] : 0.0, A3 ? 1 : 0, nb, g->fpartials,
+                                            CoupDev{nullptr, nullptr, 0, 0});
     QSF_CU(cudaGetLastError());
     std::vector<double> part((size_t)g->nfblk * kMaxFluxBorders);
     QSF_CU(cudaMemcpyAsync(part.data(), g->fpartials, part.size() * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1399,20 +1432,24 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
 }
 
 // End of one member-operation step: the flux partials summed per border in block order
-// (the order qsf_flux sums them in), the NaN / non-positive norm flag and the Normalize
-// factor, all on the device so that the steps of a call need no host synchronisation.
+// (the order qsf_flux sums them in) into row *step, the NaN / non-positive norm flag,
+// the Normalize factor, and the step counter advanced, all on the device so that the
+// steps of a program need no host synchronisation and replay from a graph.
 __global__ void k_generic_row(const double* __restrict__ fpart, int nfblk, int nb, double dV, double dx,
-                              double* __restrict__ row, long long* __restrict__ flag, double* __restrict__ scale,
-                              int normalize) {
+                              double* __restrict__ rows, long long* __restrict__ step, int ncol,
+                              long long* __restrict__ flag, double* __restrict__ scale, int normalize) {
+  double* row = rows + (*step) * ncol;
   if ((int)threadIdx.x < nb) {
     double v = 0.0;
     for (int k = 0; k < nfblk; ++k) v += fpart[k * kMaxFluxBorders + threadIdx.x];
     row[3 + threadIdx.x] = v * dV / dx;
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
     const double norm = row[0];
     if (!(norm > 0.0) || isnan(row[1]) || isnan(row[2])) *flag = 1;
     *scale = normalize && norm > 0.0 ? sqrt(1.0 / norm) : 1.0;
+    *step += 1;
   }
 }
 
@@ -1422,7 +1459,7 @@ __global__ void k_generic_row(const double* __restrict__ fpart, int nfblk, int n
 // Normalize, E_kin interval and convergence rule as the fused path.  Observables
 // reduce into device rows; the host waits once per call (and once per step that runs
 // the imaginary-time convergence test).
-static int generic_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done) {
+static int generic_check(const qsf_grid* g, const qsf_step_desc* d) {
   if (d->mode != QSF_MODE_IM && d->mode != QSF_MODE_RE) return fail(QSF_EINVAL, "mode must be IM or RE");
   if (d->nsteps < 1) return fail(QSF_EINVAL, "nsteps < 1");
   if (d->nborders < 0 || d->nborders > QSF_MAX_BORDERS) return fail(QSF_EINVAL, "too many borders");
@@ -1430,65 +1467,185 @@ static int generic_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64
   if (d->ekin_interval < 0) return fail(QSF_EINVAL, "ekin_interval must be >= 0");
   if (g->G.free_mask)
     return fail(QSF_EINVAL, "a region with free axes keeps them in momentum space: step it with the member operations");
+  return QSF_OK;
+}
+
+static int generic_ncol(const qsf_step_desc* d) {
+  return 3 + ((d->obs & QSF_OBS_FLUX) && d->nborders > 0 ? d->nborders : 0);
+}
+
+}  // extern "C"
+
+bool qsf::grid_fused(const qsf_grid* g) { return g->ks != nullptr; }
+
+// the launch-shape key of a step program: what its captured kernels bake in
+static std::vector<long long> generic_key(const qsf_grid* g, const qsf_step_desc* d) {
+  long long dtb, bits[2];
+  std::memcpy(&dtb, &d->dt, sizeof(dtb));
+  std::memcpy(&bits[0], &d->state_accuracy, sizeof(double));
+  bits[1] = 0;
+  return {d->mode, dtb, std::max(1, d->substeps), (long long)d->obs, generic_ncol(d), d->normalize,
+          d->coupling != nullptr, (long long)(uintptr_t)g->rows_dev, (long long)(uintptr_t)g->coup_dev,
+          (long long)(uintptr_t)g->snap, (long long)(uintptr_t)g->fpts, (long long)(uintptr_t)g->fterms, g->nfterms,
+          g->nsnap, g->nfblk, (long long)(uintptr_t)g->etab, (long long)(uintptr_t)g->eptab,
+          (long long)(uintptr_t)g->vtab};
+}
+
+int qsf::generic_begin(qsf_grid* g, const qsf_step_desc* d) {
+  int rc;
+  if ((rc = generic_check(g, d))) return rc;
+  const int ncol = generic_ncol(d);
+  const int K = std::max(1, d->substeps), cs = g->G.gauge == QSF_GAUGE_LENGTH ? 6 : 3;
+  if (ncol > 3 && (rc = ensure_flux(g, d->nborders, d->border_types, d->box_size))) return rc;
+  if ((rc = dev_reserve(g->rows_dev, g->rows_cap, (size_t)d->nsteps * ncol))) return rc;
+  if (d->coupling) {
+    const size_t nc = (size_t)d->nsteps * K * cs;
+    if ((rc = dev_reserve(g->coup_dev, g->coup_cap, nc))) return rc;
+    QSF_CU(cudaMemcpyAsync(g->coup_dev, d->coupling, nc * sizeof(double), cudaMemcpyHostToDevice, g->stream));
+  }
+  QSF_CU(cudaMemsetAsync(g->rows_dev, 0, (size_t)d->nsteps * ncol * sizeof(double), g->stream));
+  QSF_CU(cudaMemsetAsync(g->ctl, 0, 8 * sizeof(long long), g->stream));  // [0] step, [4] NaN flag
+  g->gen_warm = false;
+  return QSF_OK;
+}
+
+// one step of the program d at the device step index ctl[0] (its sub-steps, then the
+// observables row, then ctl[0] + 1), queued on the grid's stream; E_kin when ek.  The
+// launches do not depend on the step index, so a run of them replays from a graph.
+static int generic_one(qsf_grid* g, const qsf_step_desc* d, bool ek) {
   const GridDev& G = g->G;
   const bool lg = G.gauge == QSF_GAUGE_LENGTH;
   const int K = std::max(1, d->substeps), cs = lg ? 6 : 3;
   const double dts = d->dt / K;
-  const bool want_flux = (d->obs & QSF_OBS_FLUX) && d->nborders > 0;
-  const int nb = want_flux ? d->nborders : 0, ncol = 3 + nb;
-  const int every = d->ekin_interval > 1 ? d->ekin_interval : 1;
-  const bool conv = d->mode == QSF_MODE_IM && d->state_accuracy > 0.0;
-  const double zero[3] = {0.0, 0.0, 0.0};
+  const int ncol = generic_ncol(d), nb = ncol - 3;
+  const CoupDev none{nullptr, nullptr, 0, 0};
+  const bool has_c = d->coupling != nullptr;
+  const long long sstride = (long long)K * cs;
   int rc;
-  if (nb && (rc = ensure_flux(g, nb, d->border_types, d->box_size))) return rc;
-  if ((rc = dev_reserve(g->rows_dev, g->rows_cap, (size_t)d->nsteps * ncol))) return rc;
-  QSF_CU(cudaMemsetAsync(g->rows_dev, 0, (size_t)d->nsteps * ncol * sizeof(double), g->stream));
-  QSF_CU(cudaMemsetAsync(g->ctl + 4, 0, sizeof(long long), g->stream));
+  for (int k = 0; k < K; ++k) {
+    // sub-step k of the step: E at its opening / closing X half (length gauge), A at
+    // its P sub-step (velocity gauge)
+    const CoupDev c1 = has_c ? CoupDev{g->coup_dev, g->ctl, sstride, k * cs} : none;
+    const CoupDev c2 = has_c && lg ? CoupDev{g->coup_dev, g->ctl, sstride, k * cs + 3} : none;
+    if ((rc = evolve_impl(g, d->mode, QSF_REP_X, 0.5 * dts, nullptr, lg ? c1 : none)) ||
+        (rc = qsf_fourier(g, QSF_REP_P)) || (rc = evolve_impl(g, d->mode, QSF_REP_P, dts, nullptr, lg ? none : c1)) ||
+        (rc = qsf_fourier(g, QSF_REP_X)) || (rc = evolve_impl(g, d->mode, QSF_REP_X, 0.5 * dts, nullptr, c2)))
+      return rc;
+  }
+  int nbk = 0;
+  if ((rc = launch_average(g, QSF_REP_X, QSF_OP_IDENTITY, &nbk))) return rc;
+  k_reduce_row<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dV, g->rows_dev, g->ctl, ncol, 0);
+  if (d->obs & QSF_OBS_EPOT) {
+    if ((rc = launch_average(g, QSF_REP_X, QSF_OP_POTENTIAL, &nbk))) return rc;
+    k_reduce_row<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dV, g->rows_dev, g->ctl, ncol, 1);
+  }
+  if (ek) {
+    if ((rc = qsf_fourier(g, QSF_REP_P)) || (rc = launch_average(g, QSF_REP_P, QSF_OP_KINETIC, &nbk))) return rc;
+    k_reduce_row<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dVm, g->rows_dev, g->ctl, ncol, 2);
+    if ((rc = qsf_fourier(g, QSF_REP_X))) return rc;
+  }
+  if (nb && g->nfterms > 0) {
+    // fluxes of psi_n with the A of the step's last P sub-step (velocity gauge)
+    const bool useA = !lg && has_c && G.n_fields;
+    const CoupDev ca = useA ? CoupDev{g->coup_dev, g->ctl, sstride, (K - 1) * cs} : none;
+    k_gather<<<std::max(1, std::min(1024, (g->nsnap + 255) / 256)), 256, 0, g->stream>>>(G.psi, g->snap_idx,
+                                                                                         g->nsnap, g->snap);
+    k_flux<<<g->nfblk, 256, 0, g->stream>>>(G, g->fpts, g->fterms, g->nfterms, g->snap, 0.0, 0.0, 0.0, useA ? 1 : 0,
+                                            nb, g->fpartials, ca);
+  }
+  k_generic_row<<<1, 32, 0, g->stream>>>(g->fpartials, g->nfterms > 0 ? g->nfblk : 0, nb, G.dV, G.ax[0].dx,
+                                         g->rows_dev, g->ctl, ncol, g->ctl + 4, g->scale + 1, d->normalize);
+  if (d->normalize) k_scale<<<grid_blocks(G.m), 256, 0, g->stream>>>(G.psi, G.m, g->scale + 1);
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+static bool generic_ekin_at(const qsf_step_desc* d, int64_t s, int64_t stop_after) {
+  const int every = d->ekin_interval > 1 ? d->ekin_interval : 1;
+  return (d->obs & QSF_OBS_EKIN) && ((s + 1) % every == 0 || s + 1 == d->nsteps || s == stop_after);
+}
+
+// Steps [first, first + count) of the program (the device step index must be `first`):
+// without E_kin, runs of kGenGraphSteps steps replay one captured graph per grid (its
+// launches bake in the program's shape, so it is recaptured when that changes); the
+// first step of a program and the remainder run as plain launches.
+int qsf::generic_enqueue(qsf_grid* g, const qsf_step_desc* d, int64_t first, int64_t count) {
+  constexpr int kGenGraphSteps = 16;
+  if (first < 0 || count < 0 || first + count > d->nsteps) return fail(QSF_EINVAL, "steps outside the program");
+  int rc;
+  int64_t s = first;
+  const int64_t end = first + count;
+  const bool graphs = !(d->obs & QSF_OBS_EKIN);
+  if (!g->gen_warm && s < end) {  // allocates the member operations' tables outside any capture
+    if ((rc = generic_one(g, d, generic_ekin_at(d, s, d->nsteps)))) return rc;
+    ++s;
+    g->gen_warm = true;
+  }
+  if (graphs && end - s >= kGenGraphSteps) {
+    const std::vector<long long> key = generic_key(g, d);
+    if (!g->gen_exec || g->gen_key != key) {
+      if (g->gen_exec) cudaGraphExecDestroy(g->gen_exec);
+      g->gen_exec = nullptr;
+      if ((rc = capture_graph(
+               g->stream,
+               [&]() {
+                 for (int k = 0; k < kGenGraphSteps; ++k)
+                   if (int r = generic_one(g, d, false)) return r;
+                 return QSF_OK;
+               },
+               &g->gen_exec)))
+        return rc;
+      g->gen_key = key;
+      g->gen_steps = kGenGraphSteps;
+    }
+    for (; end - s >= g->gen_steps; s += g->gen_steps) {
+      const cudaError_t ce = cudaGraphLaunch(g->gen_exec, g->stream);
+      if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
+    }
+  }
+  for (; s < end; ++s)
+    if ((rc = generic_one(g, d, generic_ekin_at(d, s, d->nsteps)))) return rc;
+  return QSF_OK;
+}
+
+int qsf::generic_wait(qsf_grid* g, bool* bad) {
+  long long flag = 0;
+  QSF_CU(cudaMemcpyAsync(&flag, g->ctl + 4, sizeof(flag), cudaMemcpyDeviceToHost, g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  *bad = flag != 0;
+  return QSF_OK;
+}
+
+int qsf::generic_rows(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t nsteps) {
+  if (nsteps > d->nsteps) return fail(QSF_EINVAL, "more rows than steps");
+  if (rows && nsteps > 0)
+    QSF_CU(cudaMemcpyAsync(rows, g->rows_dev, (size_t)nsteps * generic_ncol(d) * sizeof(double),
+                           cudaMemcpyDeviceToHost, g->stream));
+  QSF_CU(cudaStreamSynchronize(g->stream));
+  return QSF_OK;
+}
+
+extern "C" {
+
+static int generic_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_done) {
+  int rc;
+  if ((rc = qsf::generic_begin(g, d))) return rc;
+  const bool conv = d->mode == QSF_MODE_IM && d->state_accuracy > 0.0;
+  const int ncol = generic_ncol(d);
   double last_e = d->last_energy;
   int64_t stop_after = d->nsteps;  // set by the convergence rule
   int64_t s = 0;
-  for (; s < d->nsteps && s <= stop_after; ++s) {
-    const double* row_c = nullptr;
-    for (int k = 0; k < K; ++k) {
-      const double* cp = d->coupling ? d->coupling + (size_t)(s * K + k) * cs : nullptr;
-      row_c = cp;
-      const double* ex1 = lg && cp ? cp : zero;
-      const double* ex2 = lg && cp ? cp + 3 : zero;
-      const double* ap = !lg && cp ? cp : zero;
-      if ((rc = qsf_evolve(g, d->mode, QSF_REP_X, 0.5 * dts, ex1)) || (rc = qsf_fourier(g, QSF_REP_P)) ||
-          (rc = qsf_evolve(g, d->mode, QSF_REP_P, dts, ap)) || (rc = qsf_fourier(g, QSF_REP_X)) ||
-          (rc = qsf_evolve(g, d->mode, QSF_REP_X, 0.5 * dts, ex2)))
-        return rc;
-    }
-    double* row = g->rows_dev + (size_t)s * ncol;
-    int nbk = 0;
-    if ((rc = launch_average(g, QSF_REP_X, QSF_OP_IDENTITY, &nbk))) return rc;
-    k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dV, row + 0);
-    if (d->obs & QSF_OBS_EPOT) {
-      if ((rc = launch_average(g, QSF_REP_X, QSF_OP_POTENTIAL, &nbk))) return rc;
-      k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dV, row + 1);
-    }
-    const bool ek = (d->obs & QSF_OBS_EKIN) && ((s + 1) % every == 0 || s + 1 == d->nsteps || s == stop_after);
-    if (ek) {
-      if ((rc = qsf_fourier(g, QSF_REP_P)) || (rc = launch_average(g, QSF_REP_P, QSF_OP_KINETIC, &nbk))) return rc;
-      k_reduce_partials<<<1, 256, 0, g->stream>>>(g->partials, nbk, G.dVm, row + 2);
-      if ((rc = qsf_fourier(g, QSF_REP_X))) return rc;
-    }
-    if (nb && g->nfterms > 0) {
-      // fluxes of psi_n with the A of the step's last P sub-step (velocity gauge)
-      const double* A = !lg && row_c && G.n_fields ? row_c : nullptr;
-      k_gather<<<std::max(1, std::min(1024, (g->nsnap + 255) / 256)), 256, 0, g->stream>>>(G.psi, g->snap_idx,
-                                                                                           g->nsnap, g->snap);
-      k_flux<<<g->nfblk, 256, 0, g->stream>>>(G, g->fpts, g->fterms, g->nfterms, g->snap, A ? A[0] : 0.0,
-                                              A ? A[1] : 0.0, A ? A[2] : 0.0, A ? 1 : 0, nb, g->fpartials);
-    }
-    k_generic_row<<<1, 32, 0, g->stream>>>(g->fpartials, g->nfterms > 0 ? g->nfblk : 0, nb, G.dV, G.ax[0].dx, row,
-                                           g->ctl + 4, g->scale + 1, d->normalize);
-    if (d->normalize) k_scale<<<grid_blocks(G.m), 256, 0, g->stream>>>(G.psi, G.m, g->scale + 1);
-    QSF_CU(cudaGetLastError());
-    if (conv && (ek || !(d->obs & QSF_OBS_EKIN))) {
+  if (!conv) {
+    if ((rc = qsf::generic_enqueue(g, d, 0, d->nsteps))) return rc;
+    s = d->nsteps;
+  }
+  for (; conv && s < d->nsteps && s <= stop_after; ++s) {
+    const bool ek = generic_ekin_at(d, s, stop_after);
+    if ((rc = generic_one(g, d, ek))) return rc;
+    g->gen_warm = true;
+    if (ek || !(d->obs & QSF_OBS_EKIN)) {
       double r[3];
-      QSF_CU(cudaMemcpyAsync(r, row, sizeof(r), cudaMemcpyDeviceToHost, g->stream));
+      QSF_CU(cudaMemcpyAsync(r, g->rows_dev + (size_t)s * ncol, sizeof(r), cudaMemcpyDeviceToHost, g->stream));
       QSF_CU(cudaStreamSynchronize(g->stream));
       const double se = (d->energy_after_normalize & 1) ? 1.0 / r[0] : 1.0;
       const double sk = (d->energy_after_normalize & 2) ? 1.0 / r[0] : 1.0;
@@ -1497,14 +1654,10 @@ static int generic_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64
       last_e = e;
     }
   }
-  long long flag = 0;
-  QSF_CU(cudaMemcpyAsync(&flag, g->ctl + 4, sizeof(flag), cudaMemcpyDeviceToHost, g->stream));
-  if (rows)
-    QSF_CU(cudaMemcpyAsync(rows, g->rows_dev, (size_t)d->nsteps * ncol * sizeof(double), cudaMemcpyDeviceToHost,
-                           g->stream));
-  QSF_CU(cudaStreamSynchronize(g->stream));
+  bool bad = false;
+  if ((rc = qsf::generic_wait(g, &bad)) || (rc = qsf::generic_rows(g, d, rows, d->nsteps))) return rc;
   if (steps_done) *steps_done = s;
-  if (flag) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a step's reductions");
+  if (bad) return fail(QSF_ENUMERIC, "non-positive norm or NaN in a step's reductions");
   return QSF_OK;
 }
 

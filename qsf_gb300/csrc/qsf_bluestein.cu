@@ -17,7 +17,10 @@
 // from exact integer angle reduction (j^2 mod 2n) in long double; B is transformed once
 // per grid.  Grids of such lengths step through the member operations (qsf_step's
 // generic path); batches and the server take built lengths only.
+#include <array>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -77,6 +80,35 @@ __global__ void k_bs_twiddle(double2* __restrict__ scr, const double2* __restric
     double2 t = w[p % M];
     if (conj_w) t.y = -t.y;
     scr[p] = cmul(scr[p], t);
+  }
+}
+
+// chirp[j] = exp(-i pi (j^2 mod 2n) / n) (exact integer angle reduction) and the
+// convolution kernel w = conj(chirp) wrapped onto M points (w[j] = w[M - j]), zero
+// between
+__global__ void k_bs_chirp(double2* __restrict__ chirp, double2* __restrict__ w, int n, int M) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+    const int k = j < n ? j : M - j;  // the chirp index w[j] holds, or >= n (zero)
+    double2 v = make_double2(0.0, 0.0);
+    if (k < n) {
+      const long long r = ((long long)k * k) % (2LL * n);
+      double sn, cs;
+      sincospi((double)r / (double)n, &sn, &cs);
+      v = make_double2(cs, sn);  // conj(chirp[k])
+      if (j < n) chirp[j] = make_double2(cs, -sn);
+    }
+    w[j] = v;
+  }
+}
+
+// four-step twiddles w4[k1 * M2 + n2] = exp(-2 pi i (k1 n2 mod M) / M)
+__global__ void k_bs_w4(double2* __restrict__ w4, int M1, int M2) {
+  const int M = M1 * M2;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < M; p += gridDim.x * blockDim.x) {
+    const long long r = ((long long)(p / M2) * (p % M2)) % M;
+    double sn, cs;
+    sincospi(2.0 * (double)r / (double)M, &sn, &cs);
+    w4[p] = make_double2(cs, -sn);
   }
 }
 
@@ -238,6 +270,26 @@ int bs_size(int n, int dim) {
   return bs_plan(n, dim, &M, &M1, &M2) ? M : 0;
 }
 
+// four-step twiddles of (M1, M2), made once per process and device and shared
+int shared_w4(int M1, int M2, double2** w4) {
+  static std::mutex mu;
+  static std::map<std::array<int, 3>, double2*> cache;
+  int dev = 0;
+  QSF_CU(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({dev, M1, M2});
+  if (it == cache.end()) {
+    double2* p = nullptr;
+    if (int rc = dev_alloc(p, (size_t)M1 * M2)) return rc;
+    k_bs_w4<<<blocks_for((long long)M1 * M2), 256>>>(p, M1, M2);
+    QSF_CU(cudaGetLastError());
+    QSF_CU(cudaDeviceSynchronize());
+    it = cache.emplace(std::array<int, 3>{dev, M1, M2}, p).first;
+  }
+  *w4 = it->second;
+  return QSF_OK;
+}
+
 int bs_setup(qsf_grid* g) {
   const GridDev& G = g->G;
   const int n = G.ax[0].n;
@@ -253,36 +305,14 @@ int bs_setup(qsf_grid* g) {
   b.ks = kernels_for(M1 ? M2 : M);
   b.ks1 = M1 ? kernels_for(M1) : nullptr;
   int rc;
-  if ((rc = make_twiddles(M1 ? M2 : M, &b.tw, &b.twx, &b.twf))) return rc;
-  if (M1) {
-    if ((rc = make_twiddles(M1, &b.tw1, &b.twx1, &b.twf1))) return rc;
-    std::vector<double2> w4((size_t)M);
-    const long double twopi = 6.283185307179586476925286766559005768L;
-    for (long long k1 = 0; k1 < M1; ++k1)
-      for (long long n2 = 0; n2 < M2; ++n2) {
-        const long long r = (k1 * n2) % M;  // exact angle reduction
-        const long double a = twopi * (long double)r / (long double)M;
-        w4[(size_t)(k1 * M2 + n2)] = make_double2((double)cosl(a), -(double)sinl(a));
-      }
-    if ((rc = dev_alloc(b.tw4, (size_t)M))) return rc;
-    QSF_CU(cudaMemcpy(b.tw4, w4.data(), (size_t)M * sizeof(double2), cudaMemcpyHostToDevice));
-  }
-  std::vector<double2> c((size_t)n), w((size_t)M, make_double2(0.0, 0.0));
-  const long double pi = 3.141592653589793238462643383279502884L;
-  for (long long j = 0; j < n; ++j) {
-    const long long r = (j * j) % (2LL * n);  // exp(-i pi j^2 / n) depends on j^2 mod 2n
-    const long double a = pi * (long double)r / (long double)n;
-    c[(size_t)j] = make_double2((double)cosl(a), -(double)sinl(a));
-    const double2 cc = make_double2(c[(size_t)j].x, -c[(size_t)j].y);
-    w[(size_t)j] = cc;
-    if (j) w[(size_t)(M - j)] = cc;
-  }
+  if ((rc = shared_twiddles(M1 ? M2 : M, &b.tw, &b.twx, &b.twf))) return rc;
+  if (M1 && ((rc = shared_twiddles(M1, &b.tw1, &b.twx1, &b.twf1)) || (rc = shared_w4(M1, M2, &b.tw4)))) return rc;
   const size_t scr = (size_t)(G.m / n) * (size_t)M;
   if ((rc = dev_alloc(b.chirp, (size_t)n)) || (rc = dev_alloc(b.bhat, (size_t)M)) ||
       (rc = dev_alloc(b.scratch, std::max(scr, (size_t)M))))
     return rc;
-  QSF_CU(cudaMemcpy(b.chirp, c.data(), (size_t)n * sizeof(double2), cudaMemcpyHostToDevice));
-  QSF_CU(cudaMemcpy(b.bhat, w.data(), (size_t)M * sizeof(double2), cudaMemcpyHostToDevice));
+  k_bs_chirp<<<blocks_for(M), 256, 0, g->stream>>>(b.chirp, b.bhat, n, M);
+  QSF_CU(cudaGetLastError());
   // B = FFT_M(w): the kernel array as a one-line grid of M points
   GridDev L = G;
   L.dim = 1;
@@ -296,20 +326,17 @@ int bs_setup(qsf_grid* g) {
   L.ax[0].twf = reinterpret_cast<decltype(L.ax[0].twf)>(b.twf);
   L.m = M;
   for (int k = 0; k < kMaxDim; ++k) L.tmap[k] = nullptr;
-  if ((rc = fft_M(g, L, 0, true, 1.0, g->stream))) return rc;
-  QSF_CU(cudaStreamSynchronize(g->stream));
-  return QSF_OK;
+  return fft_M(g, L, 0, true, 1.0, g->stream);
 }
 
 void bs_release(qsf_grid* g) {
   qsf_grid::Bluestein& b = g->bs;
-  for (void* p : {(void*)b.chirp, (void*)b.bhat, (void*)b.scratch, (void*)b.tw, (void*)b.twx, (void*)b.twf,
-                  (void*)b.tw1, (void*)b.twx1, (void*)b.twf1, (void*)b.tw4})
+  for (void* p : {(void*)b.chirp, (void*)b.bhat, (void*)b.scratch})  // the twiddles are shared
     if (p) cudaFree(p);
   b = qsf_grid::Bluestein();
 }
 
-int bs_axis(qsf_grid* g, int ax, bool fwd, double post) {
+int bs_axis(qsf_grid* g, double2* arr, int ax, bool fwd, double post) {
   const GridDev& G = g->G;
   const qsf_grid::Bluestein& b = g->bs;
   const int n = b.n, M = b.M;
@@ -317,14 +344,14 @@ int bs_axis(qsf_grid* g, int ax, bool fwd, double post) {
   const GridDev S = scratch_view(g, ax);
   cudaStream_t st = g->stream;
   const int inv = fwd ? 0 : 1;
-  k_bs_pre<<<blocks_for(outer * M * inner), 256, 0, st>>>(G.psi, b.scratch, b.chirp, outer, n, M, inner, inv);
+  k_bs_pre<<<blocks_for(outer * M * inner), 256, 0, st>>>(arr, b.scratch, b.chirp, outer, n, M, inner, inv);
   QSF_CU(cudaGetLastError());
   int rc;
   if ((rc = fft_M(g, S, ax, true, 1.0, st))) return rc;
   k_bs_mul<<<blocks_for(outer * M * inner), 256, 0, st>>>(b.scratch, b.bhat, outer, M, inner);
   QSF_CU(cudaGetLastError());
   if ((rc = fft_M(g, S, ax, false, 1.0 / (double)M, st))) return rc;
-  k_bs_post<<<blocks_for(outer * n * inner), 256, 0, st>>>(G.psi, b.scratch, b.chirp, outer, n, M, inner, inv, post);
+  k_bs_post<<<blocks_for(outer * n * inner), 256, 0, st>>>(arr, b.scratch, b.chirp, outer, n, M, inner, inv, post);
   QSF_CU(cudaGetLastError());
   return QSF_OK;
 }

@@ -64,8 +64,6 @@ struct qsf_grid {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   BorderNodes bn;
-  std::vector<double2*> tw_owned;
-  std::vector<longlong2*> twx_owned;
   const KernelSet* ks = nullptr;  // kernels for this grid's line length
   GridDev* dG = nullptr;          // device copy of G (step kernels read descriptors from device arrays)
   StepDev* dS = nullptr;          // device copy of the current step descriptor
@@ -141,6 +139,13 @@ struct qsf_grid {
     cudaGraphExec_t exec;
   };
   std::vector<StepGraph> step_graphs;
+  // member-operation step programs (grids without fused kernels): the executable graph
+  // of gen_steps steps, the program it was captured for, and whether a step has run
+  // since the program began (the first one allocates the member operations' tables)
+  cudaGraphExec_t gen_exec = nullptr;
+  int gen_steps = 0;
+  std::vector<long long> gen_key;
+  bool gen_warm = false;
   // TMA tensor maps of psi for the strided-axis passes (GridDev::tmap), 128 bytes each
   unsigned char* tmaps = nullptr;
   // Bluestein transforms of a grid whose axis length has a prime factor above 5 (no
@@ -159,6 +164,7 @@ struct qsf_grid {
     double2* chirp = nullptr;
     double2* bhat = nullptr;
     double2* scratch = nullptr;
+    // shared per-process tables (not owned by the grid)
     double2* tw = nullptr;  // twiddles of M (or M2)
     longlong2* twx = nullptr;
     longlong2* twf = nullptr;
@@ -172,13 +178,27 @@ struct qsf_grid {
 namespace qsf {
 // whether n is a line length with fused step kernels in this build
 bool fused_length(int n);
+bool grid_fused(const qsf_grid* g);
+// Member-operation steps of a grid without fused kernels (qsf_step's path for them),
+// in parts for the server: begin checks the program and zeroes its device rows and
+// NaN flag; enqueue queues steps [first, first + count) on the grid's stream without
+// waiting (no convergence test); wait waits for the stream and reads the NaN flag;
+// rows copies the first nsteps rows to the host.
+int generic_begin(qsf_grid* g, const qsf_step_desc* d);
+int generic_enqueue(qsf_grid* g, const qsf_step_desc* d, int64_t first, int64_t count);
+int generic_wait(qsf_grid* g, bool* bad);
+int generic_rows(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t nsteps);
+// twiddle tables of an n-point transform shared by all grids of the process (not to
+// be freed by the caller)
+int shared_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf);
 // twiddle tables of an n-point transform (FP64, 2^62 fixed point, split form)
 int make_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf);
 // Bluestein plan of a grid without fused kernels (qsf_bluestein.cu)
 int bs_setup(qsf_grid* g);
 void bs_release(qsf_grid* g);
-// one axis of fourier<R>() by Bluestein's chirp-z convolution, scaled by post
-int bs_axis(qsf_grid* g, int ax, bool fwd, double post);
-// the smallest built size M >= 2n - 1 that a Bluestein plan of n can use (0: none)
+// one axis of fourier<R>() by Bluestein's chirp-z convolution, in place on the array
+// arr (psi's geometry: psi itself, or a region-transfer slice), scaled by post
+int bs_axis(qsf_grid* g, double2* arr, int ax, bool fwd, double post);
+// the convolution length M >= 2n - 1 of an n-point axis of a dim-D grid (0: none)
 int bs_size(int n, int dim);
 }  // namespace qsf

@@ -117,6 +117,23 @@ struct FluxTerm {
   double w[kMaxDim];
 };
 
+// Where a member-operation kernel finds its coupling values when they live on the
+// device (a step program replayed from a graph): the row at c + (*step) * stride + off
+// for the current step index *step; c == nullptr: the kernel's by-value arguments.
+struct CoupDev {
+  const double* c;
+  const long long* step;
+  long long stride;
+  int off;
+};
+__device__ __forceinline__ void coup_load(const CoupDev& cd, double* cv) {
+  if (!cd.c) return;
+  const double* p = cd.c + (*cd.step) * cd.stride + cd.off;
+  cv[0] = p[0];
+  cv[1] = p[1];
+  cv[2] = p[2];
+}
+
 struct StepDev {
   int mode;  // 1 IM, 2 RE
   double dt;
@@ -1539,9 +1556,10 @@ __global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis_fft
 // gauge), dotted with the normalised border vector.  out[b] written by thread b.
 __global__ void __launch_bounds__(256) k_flux(GridDev g, const FluxPoint* fpts, const FluxTerm* fterms, int nfterms,
                                               const double2* snap, double A0, double A1, double A2, int useA, int nb,
-                                              double* out_partials) {
+                                              double* out_partials, CoupDev cd) {
   __shared__ double red[32 * kMaxFluxBorders];
-  const double Av[3] = {A0, A1, A2};
+  double Av[3] = {A0, A1, A2};
+  coup_load(cd, Av);
   const int chunk = (nfterms + gridDim.x - 1) / gridDim.x;
   const int t0 = blockIdx.x * chunk, t1 = min(nfterms, t0 + chunk);
   flux_block(g, fpts, fterms, t0, t1, snap, useA ? Av : nullptr, nb, red, out_partials + blockIdx.x * kMaxFluxBorders);
@@ -1606,11 +1624,13 @@ __global__ void k_evolve_xtab(GridDev g, int mode, double delta, double2* __rest
 // per-axis factors of evolve<M, P>(delta): expOp(delta (k^2 / 2 + A_d k)) for axis d
 // (the P Hamiltonian is a sum over axes, so its exponential is their product)
 __global__ void k_evolve_ptab(GridDev g, int mode, double delta, double c0, double c1, double c2, int nmax,
-                              double2* __restrict__ tab) {
+                              double2* __restrict__ tab, CoupDev cd) {
   double cv[3] = {c0, c1, c2};
+  coup_load(cd, cv);
   if (g.p_swap && g.dim >= 2) {
-    cv[0] = c1;
-    cv[1] = c0;
+    const double t = cv[0];
+    cv[0] = cv[1];
+    cv[1] = t;
   }
   const bool coupled = g.gauge == 0 && g.n_fields;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < g.dim * nmax; e += gridDim.x * blockDim.x) {
@@ -1643,11 +1663,13 @@ __global__ void k_apply_ptab(GridDev g, const double2* __restrict__ tab, int nma
   }
 }
 
-__global__ void k_evolve(GridDev g, int mode, int rep, double delta, double c0, double c1, double c2) {
+__global__ void k_evolve(GridDev g, int mode, int rep, double delta, double c0, double c1, double c2, CoupDev cd) {
   double cv[3] = {c0, c1, c2};
+  coup_load(cd, cv);
   if (rep == 2 && g.p_swap && g.dim >= 2) {
-    cv[0] = c1;
-    cv[1] = c0;
+    const double t = cv[0];
+    cv[0] = cv[1];
+    cv[1] = t;
   }
   const int couples = g.gauge == 0 ? 2 : 1;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -1743,6 +1765,16 @@ __global__ void k_reduce_partials(const double* part, int n, double scale, doubl
   for (int i = threadIdx.x; i < n; i += blockDim.x) acc += part[i];
   block_sum<1>(&acc, red);
   if (threadIdx.x == 0) *out = acc * scale;
+}
+
+// the same into column col of row *step of rows (ncol columns): a step program's row
+__global__ void k_reduce_row(const double* part, int n, double scale, double* rows, const long long* step, int ncol,
+                             int col) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += part[i];
+  block_sum<1>(&acc, red);
+  if (threadIdx.x == 0) rows[(*step) * ncol + col] = acc * scale;
 }
 
 // gather psi at the snapshot indices (granular flux)

@@ -21,8 +21,14 @@
 
 #include "qsf_gpu.h"
 
-namespace qsf {
-bool fused_length(int n);  // qsf_api.cu
+namespace qsf {  // qsf_api.cu, qsf_bluestein.cu
+bool fused_length(int n);
+int bs_size(int n, int dim);
+bool grid_fused(const qsf_grid* g);
+int generic_begin(qsf_grid* g, const qsf_step_desc* d);
+int generic_enqueue(qsf_grid* g, const qsf_step_desc* d, int64_t first, int64_t count);
+int generic_wait(qsf_grid* g, bool* bad);
+int generic_rows(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t nsteps);
 }
 
 namespace {
@@ -50,6 +56,12 @@ struct Running {
   std::vector<double> coupling;  // kept alive while in the batch
   clk::time_point submitted, admitted;
   bool cancel = false;           // qsf_server_cancel: leave after this round
+  // a grid without fused kernels (Bluestein lengths): its steps run as member
+  // operations on the grid's own stream, beside the batch, with this step program
+  bool generic = false;
+  qsf_step_desc d{};
+  bool bad = false;  // NaN / non-positive norm seen
+  int rc = 0;        // error of a queued round
 };
 
 int64_t grid_points(const qsf_grid_desc& d) {
@@ -63,7 +75,11 @@ int64_t grid_points(const qsf_grid_desc& d) {
 size_t solve_bytes(const qsf_request& r) {
   const int64_t m = grid_points(r.grid);
   const int stride = r.grid.gauge == QSF_GAUGE_LENGTH ? 6 : 3;
-  return (size_t)m * (16 + 16 + 8) + (size_t)r.nsteps * (size_t)(3 + r.nborders + stride) * 8 + (1u << 20);
+  size_t b = (size_t)m * (16 + 16 + 8) + (size_t)r.nsteps * (size_t)(3 + r.nborders + stride) * 8 + (1u << 20);
+  // Bluestein lengths: the convolution scratch (up to 4 m points) and the member
+  // operations' X / P phase tables
+  if (!qsf::fused_length((int)r.grid.n[0])) b += (size_t)m * 16 * 6;
+  return b;
 }
 
 }  // namespace
@@ -214,7 +230,13 @@ int admit(qsf_server* s, Pending& p, Running& r) {
   d.nborders = p.req.nborders;
   for (int b = 0; b < QSF_MAX_BORDERS; ++b) d.border_types[b] = p.req.border_types[b];
   d.box_size = p.req.box_size;
-  rc = qsf_batch_add(s->batch, g, &d, &r.slot);
+  if (!qsf::grid_fused(g)) {
+    r.generic = true;
+    r.d = d;
+    rc = qsf::generic_begin(g, &r.d);
+  } else {
+    rc = qsf_batch_add(s->batch, g, &d, &r.slot);
+  }
   if (rc) {
     qsf_grid_destroy(g);
     r.grid = nullptr;
@@ -288,30 +310,61 @@ void worker_loop(qsf_server* s) {
       s->running.emplace(r.ticket, std::move(r));
     }
     if (s->running.empty()) continue;
-    // one round of steps for every resident solve
+    // one round of steps for every resident solve: the member-operation solves' steps
+    // queued first on their own streams (they overlap with one another and with the
+    // batch), then the batch's round, then a wait for each member-operation solve
+    bool any_fused = false;
+    for (auto& kv : s->running) {
+      Running& r = kv.second;
+      if (!r.generic) {
+        any_fused = true;
+        continue;
+      }
+      const int64_t first = r.nsteps - r.remaining;
+      const int64_t count = std::min<int64_t>(s->cfg.steps_per_round, r.remaining);
+      r.d.coupling = r.coupling.empty() ? nullptr : r.coupling.data();
+      if (!r.cancel && !r.rc && count > 0) r.rc = qsf::generic_enqueue(r.grid, &r.d, first, count);
+    }
     int64_t active = 0;
-    const int rc_run = qsf_batch_run(s->batch, s->cfg.steps_per_round, &active);
+    const int rc_run = any_fused ? qsf_batch_run(s->batch, s->cfg.steps_per_round, &active) : QSF_OK;
+    for (auto& kv : s->running) {
+      Running& r = kv.second;
+      if (!r.generic) continue;
+      const int rw = qsf::generic_wait(r.grid, &r.bad);
+      if (rw && !r.rc) r.rc = rw;
+    }
     // retire finished, cancelled and failed solves.  A numeric failure (QSF_ENUMERIC)
     // belongs to single members, which qsf_batch_result names; any other error of the
     // round ends every resident solve.
     const bool fatal = rc_run && rc_run != QSF_ENUMERIC;
     std::vector<int64_t> done;
     for (auto& kv : s->running) {
-      kv.second.remaining -= s->cfg.steps_per_round;
-      bool bad = false;
-      if (rc_run == QSF_ENUMERIC) {
+      Running& r = kv.second;
+      const int64_t ran = r.cancel && r.generic ? 0 : std::min<int64_t>(s->cfg.steps_per_round, r.remaining);
+      r.remaining -= r.generic ? ran : s->cfg.steps_per_round;
+      bool bad = r.generic && (r.bad || r.rc);
+      if (!r.generic && rc_run == QSF_ENUMERIC) {
         int64_t st = 0;
-        bad = qsf_batch_result(s->batch, kv.second.slot, nullptr, &st) == QSF_ENUMERIC;
+        bad = qsf_batch_result(s->batch, r.slot, nullptr, &st) == QSF_ENUMERIC;
       }
-      if (kv.second.remaining <= 0 || fatal || bad || kv.second.cancel) done.push_back(kv.first);
+      if (r.remaining <= 0 || fatal || bad || r.cancel) done.push_back(kv.first);
     }
     for (int64_t t : done) {
       Running& r = s->running[t];
       rows.assign((size_t)r.nsteps * (3 + r.nb), 0.0);
       int64_t steps = 0;
-      int rc = fatal ? rc_run : qsf_batch_result(s->batch, r.slot, rows.data(), &steps);
+      int rc;
+      if (fatal) {
+        rc = rc_run;
+      } else if (r.generic) {
+        steps = r.nsteps - std::max<int64_t>(r.remaining, 0);
+        rc = r.rc ? r.rc : qsf::generic_rows(r.grid, &r.d, rows.data(), steps);
+        if (rc == QSF_OK && r.bad) rc = QSF_ENUMERIC;
+      } else {
+        rc = qsf_batch_result(s->batch, r.slot, rows.data(), &steps);
+      }
       if (rc == QSF_OK && r.cancel && r.remaining > 0) rc = QSF_ECANCELED;
-      qsf_batch_remove(s->batch, r.slot);
+      if (!r.generic) qsf_batch_remove(s->batch, r.slot);
       if (rc && rc != QSF_ECANCELED) qsf_grid_destroy(r.grid);
       else release_grid(s, r.desc, r.grid);
       finish(s, r, rc, rows.data(), steps);
@@ -341,8 +394,9 @@ int qsf_server_start(const qsf_server_config* cfg, qsf_server** out) {
 
 int qsf_server_submit(qsf_server* s, const qsf_request* r, int64_t* ticket) {
   if (!s || !r || !ticket || r->nsteps < 1 || r->nborders < 0 || r->nborders > QSF_MAX_BORDERS) return QSF_EINVAL;
-  // solves advance in the batch, whose launches need fused kernels of the line length
-  if (r->grid.dim < 1 || r->grid.dim > 3 || !qsf::fused_length((int)r->grid.n[0])) return QSF_EINVAL;
+  // lengths with fused kernels join the batch; the others need a Bluestein length
+  if (r->grid.dim < 1 || r->grid.dim > 3) return QSF_EINVAL;
+  if (!qsf::fused_length((int)r->grid.n[0]) && !qsf::bs_size((int)r->grid.n[0], r->grid.dim)) return QSF_EINVAL;
   Pending p;
   p.req = *r;
   const int stride = r->grid.gauge == QSF_GAUGE_LENGTH ? 6 : 3;

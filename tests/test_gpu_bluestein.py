@@ -146,13 +146,42 @@ def test_bluestein_grids_stay_out_of_batches():
     g.close()
 
 
-def test_server_rejects_lengths_without_fused_kernels():
+def test_server_serves_bluestein_lengths_beside_the_batch():
+    """Solves of lengths without fused kernels run in the server beside the batch (their
+    own streams, member operations): each result equals the same solve run alone through
+    qsf_step, bit for bit, in a mix with fused-length solves."""
     import qsf_gb300 as Q
     from qsf_gb300 import serve as S
-    srv = S.Server(max_slots=2, steps_per_round=4)
+    from qsf_gb300.propagator import coupling_schedule
+    nsteps, dt = 40, 0.05
+    cases = [(1, 1021, 0.2, ["BOX"], 400), (2, 63, 0.3, Q.ZOA_FLUX_2D, 0), (2, 64, 0.3, Q.ZOA_FLUX_2D, 0),
+             (1, 9009, 0.2, ["BOX"], 3000)]
+    reqs, alone = [], []
+    for dim, n, dx, borders, box in cases:
+        c = Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field({1: 1, 2: 3}[dim], [Q.Pulse(field=0.1, omega=1.0, ncycles=1.0)])])
+        sched = coupling_schedule(c, dt, nsteps)[0]
+        x = (np.arange(n) - (n - 1) / 2.0) * dx
+        psi0 = np.exp(-0.5 * sum(np.meshgrid(*([x * x] * dim), indexing="ij"))).astype(np.complex128)
+        psi0 /= np.sqrt(np.sum(np.abs(psi0) ** 2) * dx ** dim)
+        g = Q.Grid(dim, n, dx, nCAP=n // 10, Ncharge=float(dim), gauge=Q.GAUGE_VELOCITY, n_fields=1)
+        g.upload(psi0)
+        rows, done = g.step(Q.MODE_RE, dt, nsteps, sched, obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders,
+                            box_size=box)
+        assert done == nsteps
+        alone.append(rows.copy())
+        g.close()
+        reqs.append(dict(gdesc=S.grid_desc(dim, n, dx, nCAP=n // 10, Ncharge=float(dim), gauge=Q.GAUGE_VELOCITY,
+                                           n_fields=1),
+                         mode=Q.MODE_RE, dt=dt, nsteps=nsteps, coupling=sched, psi0=psi0,
+                         obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box))
+    srv = S.Server(max_slots=8, steps_per_round=16)
     try:
-        with pytest.raises(Q.QsfError) as e:
-            srv.submit(S.grid_desc(2, 63, 0.3, nCAP=6), Q.MODE_IM, 0.05, 4, None, obs=Q.OBS_NORM)
-        assert e.value.code == 1
+        tickets = [srv.submit(**r) for r in reqs]
+        for t, rows, (dim, n, _, borders, _) in zip(tickets, alone, cases):
+            r = srv.wait(t, 300)
+            assert r["status"] == 0 and r["steps"] == nsteps, (dim, n)
+            assert r["final_norm"] == rows[-1, 0] and r["final_epot"] == rows[-1, 1], (dim, n)
+            for b in range(len(borders)):
+                assert r["flux_integral"][b] == pytest.approx(np.sum(rows[:, 3 + b]) * dt, rel=1e-13, abs=0)
     finally:
         srv.stop()
