@@ -429,18 +429,24 @@ def _mg_oracle_rate(n: int, nsteps: int) -> float:
     return len(regs) * n * n * nsteps / (time.perf_counter() - t0)
 
 
-def run_multigrid(steps, warmup, cpu=True):
-    """Multi-region 2D grid (regions NO, X, Y, XY of 1024^2 each): one step = the Strang
-    step of every region, norm and E_pot of the main region, the region transfer and the
-    region masks.  Timed on the host around `steps` steps with every region's stream
-    synchronised at both ends (the regions run on four streams)."""
+def run_multigrid(steps, warmup, cpu=True, dim=2):
+    """Multi-region grid: 2D regions NO, X, Y, XY of 1024^2 each (the C2 pulse), or 3D
+    regions NO ... XYZ of 256^3 each (three electrons, e-n charge 3, 2-cycle 800 nm 1e15
+    W/cm^2; velocity gauge, the gauge the reference's multi-region grids support): one
+    step = the Strang step of every region, norm and E_pot of the main region, the region
+    transfers and the region masks.  Timed on the host around `steps` steps with every
+    region's stream synchronised at both ends (each region runs on its own stream)."""
     import qsf_gb300 as Q
     from qsf_gb300.multigrid import MultiGrid, MultiRegionPropagator
-    pa = _pulse_args()
-    mg = MultiGrid(2, MG_EDGE, DX, MG_NCAP, potential=Q.POT_EBERLY, Ncharge=NCHARGE, Echarge=ECHARGE, Nsoft=NSOFT,
+    if dim == 2:
+        edge, ncap, dx, charge, axis, pa = MG_EDGE, MG_NCAP, DX, NCHARGE, 3, _pulse_args()
+    else:
+        edge, ncap, dx, charge, axis = 256, 26, 0.4, 3.0, 7
+        pa = dict(field=Q.field_from_intensity(1e15), omega=Q.omega_from_wavelength(800.0), ncycles=2.0)
+    mg = MultiGrid(dim, edge, dx, ncap, potential=Q.POT_EBERLY, Ncharge=charge, Echarge=ECHARGE, Nsoft=NSOFT,
                    Esoft=ESOFT, gauge=Q.GAUGE_VELOCITY, n_fields=1)
-    mg.main.upload(_gauss_state(2, MG_EDGE, DX))
-    prop = MultiRegionPropagator(DT, mg, Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(3, [Q.Pulse(**pa)])]),
+    mg.main.upload(_gauss_state(dim, edge, dx))
+    prop = MultiRegionPropagator(DT, mg, Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(axis, [Q.Pulse(**pa)])]),
                                  ["norm", "epot"])
 
     def one():
@@ -456,11 +462,12 @@ def run_multigrid(steps, warmup, cpu=True):
         one()
     mg.synchronize()
     wall = time.perf_counter() - t0
-    pts = 4.0 * MG_EDGE * MG_EDGE * steps
+    nreg = 2 ** dim
+    pts = float(nreg) * edge ** dim * steps
     out = {"value": pts / wall, "unit": UNIT, "ms_per_step": wall * 1e3 / steps, "steps": steps,
-           "config": f"2D multi-region grid, 4 regions x {MG_EDGE}^2, nCAP {MG_NCAP}, VG sin^2 pulse, "
-                     f"norm + E_pot of the main region every step, transfer + masks every step"}
-    if cpu:
+           "config": f"{dim}D multi-region grid, {nreg} regions x {edge}^{dim}, nCAP {ncap}, VG sin^2 pulse, "
+                     f"norm + E_pot of the main region every step, transfers + masks every step"}
+    if cpu and dim == 2:
         n_cpu = 256
         out["cpu_baseline"] = {"value": _mg_oracle_rate(n_cpu, 4), "unit": UNIT, "cores": 1, "kind": "port",
                                "sample": f"4 steps of the same multi-region propagator on 4 x {n_cpu}^2 regions "
@@ -695,6 +702,7 @@ def run_gpu(args):
     batched = run_batched(steps=20, warmup=3, ws=ws, rank=rank)
     served = [run_served(rate=r, duration_s=2.0, ws=ws, rank=rank) for r in (10.0, 100.0, 1000.0)]
     multigrid = run_multigrid(steps=20, warmup=3, cpu=rank == 0)
+    multigrid_3d = run_multigrid(steps=5, warmup=2, cpu=False, dim=3)
     c1 = run_c1(steps=max(args.steps, 200), warmup=args.warmup, flush=flush)
     c4 = run_c4(steps=max(args.steps, 10), warmup=args.warmup, flush=flush)
     ekin = run_ekin(steps=max(args.steps, 40), flush=flush)
@@ -725,6 +733,7 @@ def run_gpu(args):
             "batched": batched,
             "served": served,
             "multigrid": multigrid,
+            "c4_multi_region": multigrid_3d,
             "c1": c1,
             "c4": c4,
             "ekin": ekin,
@@ -772,6 +781,7 @@ def main():
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served", "multigrid"])
     ap.add_argument("--rates", default="10,30,100,300,1000")
     ap.add_argument("--duration", type=float, default=5.0)
+    ap.add_argument("--mg-dim", type=int, default=2, choices=[2, 3], help="multigrid workload: 2D 1024^2 or 3D 256^3")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -787,7 +797,7 @@ def main():
     elif args.workload == "multigrid":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"metric": METRIC, **run_multigrid(args.steps, args.warmup)}), flush=True)
+        print(json.dumps({"metric": METRIC, **run_multigrid(args.steps, args.warmup, dim=args.mg_dim)}), flush=True)
     else:
         run_gpu(args)
 

@@ -66,6 +66,27 @@ def test_multigrid_2d_matches_oracle_larger():
         assert C.rel_l2(psis[r], gs[r].psi) < TOL_PSI, r
 
 
+def test_multigrid_3d_128_matches_oracle():
+    """The 3D multi-region grid at 128^3 (regions NO ... XYZ, three electrons, velocity
+    gauge, transfers and masks every step) against the oracle over a short pulse."""
+    n = 128
+    p = dict(n=n, dx=0.4, nCAP=13, Ncharge=3.0, Echarge=-1.0, Nsoft=1.0, Esoft=1.0, F0=0.3, omega=20.0,
+             ncycles=1, re_dt=0.05)
+    rng = np.random.default_rng(13)
+    x = (np.arange(n) - (n - 1) / 2.0) * p["dx"]
+    r2 = x[:, None, None] ** 2 + x[None, :, None] ** 2 + x[None, None, :] ** 2
+    env = np.exp(-r2 / (2 * (0.3 * n * p["dx"]) ** 2))
+    psi0 = env * (rng.standard_normal((n,) * 3) + 1j * rng.standard_normal((n,) * 3))
+    gs, orows = C.oracle_mg(p, 3, psi0)
+    psis, rows = _gpu_run(p, 3, psi0)
+    assert len(rows) == len(orows) > 5
+    np.testing.assert_allclose(np.array([C.mg_dat_row(r) for r in rows]),
+                               np.array([C.mg_dat_row(r) for r in orows]), rtol=TOL_ROWS, atol=1e-12)
+    for r in range(8):
+        assert np.linalg.norm(gs[r].psi) > 0, r
+        assert C.rel_l2(psis[r], gs[r].psi) < TOL_PSI, r
+
+
 def test_region_rules():
     import qsf_gb300 as Q
     from qsf_gb300.multigrid import MultiGrid
