@@ -1,4 +1,4 @@
-// qsf_bluestein.cu -- fourier<R>() for axis lengths with a prime factor above 5.
+// qsf_bluestein.cu -- fourier<R>() for axis lengths outside the built kernel list.
 //
 // The reference's FFTW plans take any n (wf/grid.h:251-274); the fused step kernels of
 // this library are compiled for a list of lengths 2^a 3^b 5^c (8 ... 16384, the
@@ -14,9 +14,10 @@
 // whose output order is transposed, the same for the kernel B and the data, so the
 // pointwise product and the inverse four-step give the cyclic convolution unchanged.
 // The inverse transform is the forward one between two conjugations.  The chirp comes
-// from exact integer angle reduction (j^2 mod 2n) in long double; B is transformed once
-// per grid.  Grids of such lengths step through the member operations (qsf_step's
-// generic path); batches and the server take built lengths only.
+// from exact integer angle reduction (j^2 mod 2n) and sincospi on the device; B is
+// transformed once per grid.  Grids of such lengths step through the member operations
+// (qsf_step's step programs, replayed from graphs); batches take built lengths only,
+// the server runs such solves beside its batch.
 #include <array>
 #include <cmath>
 #include <map>
@@ -183,26 +184,8 @@ int fft_M(const qsf_grid* g, const GridDev& S, int ax, bool fwd, double post, cu
     QSF_CU(cudaGetLastError());
     return QSF_OK;
   }
-  if (ax == S.dim - 1) {
-    const long long nrows = S.m / M;
-    const int L = (int)std::max<long long>(1, std::min<long long>(nrows, (16LL * kLineThreads) / M));
-    int blocks = (int)((nrows + L - 1) / L);
-    size_t smem = (size_t)L * M * sizeof(double2);
-    if (K.fft_ctas > 1) {
-      blocks = K.fft_ctas;
-      smem = (size_t)(M / K.fft_ctas) * sizeof(double2);
-    }
-    if (fwd) K.row_fft_f<<<blocks, kLineThreads, smem, st>>>(S, L, post);
-    else K.row_fft_b<<<blocks, kLineThreads, smem, st>>>(S, L, post);
-  } else {
-    const long long inner = S.ax[ax].stride;
-    const int C = (int)std::max<long long>(1, std::min<long long>({64, 4096 / M, inner}));
-    const long long outer = S.m / ((long long)M * inner);
-    const int blocks = (int)(outer * ((inner + C - 1) / C));
-    const size_t smem = (size_t)M * C * sizeof(double2);
-    if (fwd) K.axis_fft_f<<<blocks, K.row_threads, smem, st>>>(S, ax, C, post);
-    else K.axis_fft_b<<<blocks, K.row_threads, smem, st>>>(S, ax, C, post);
-  }
+  if (ax == S.dim - 1) row_pass(K, S, fwd, post, st);
+  else axis_pass(K, S, ax, fwd, post, st);
   QSF_CU(cudaGetLastError());
   return QSF_OK;
 }

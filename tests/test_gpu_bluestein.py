@@ -185,3 +185,31 @@ def test_server_serves_bluestein_lengths_beside_the_batch():
                 assert r["flux_integral"][b] == pytest.approx(np.sum(rows[:, 3 + b]) * dt, rel=1e-13, abs=0)
     finally:
         srv.stop()
+
+
+def test_bluestein_multi_region_grid_matches_oracle():
+    """A 2D multi-region grid of a length outside the built list (66 = 2 * 3 * 11):
+    partial transforms and region transfers through the Bluestein transforms."""
+    from qsf_gb300.multigrid import MultiGrid, MultiRegionPropagator
+    import qsf_gb300 as Q
+    n = 66
+    p = dict(n=n, dx=0.4, nCAP=7, Ncharge=2.0, Echarge=-1.0, Nsoft=1.0, Esoft=1.0, F0=0.2, omega=1.2,
+             ncycles=1, re_dt=0.05)
+    rng = np.random.default_rng(17)
+    x = (np.arange(n) - (n - 1) / 2.0) * p["dx"]
+    env = np.exp(-(x[:, None] ** 2 + x[None, :] ** 2) / 60.0)
+    psi0 = env * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    gs, orows = C.oracle_mg(p, 2, psi0)
+    mg = MultiGrid(2, n, p["dx"], p["nCAP"], potential=Q.POT_EBERLY, Ncharge=p["Ncharge"], Echarge=p["Echarge"],
+                   Nsoft=p["Nsoft"], Esoft=p["Esoft"], gauge=Q.GAUGE_VELOCITY, n_fields=1)
+    mg.main.upload(psi0)
+    pulse = Q.Pulse(field=p["F0"], omega=p["omega"], ncycles=p["ncycles"])
+    prop = MultiRegionPropagator(p["re_dt"], mg, Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(3, [pulse])]), C.MG_OUTPUTS)
+    rows = prop.run()
+    psis = [g.download() for g in mg.regions]
+    mg.close()
+    np.testing.assert_allclose(np.array([C.mg_dat_row(r) for r in rows]),
+                               np.array([C.mg_dat_row(r) for r in orows]), rtol=1e-9, atol=1e-12)
+    for r in range(4):
+        assert np.linalg.norm(gs[r].psi) > 0, r
+        assert C.rel_l2(psis[r], gs[r].psi) < 1e-10, r
