@@ -84,8 +84,22 @@ size_t solve_bytes(const qsf_request& r) {
 
 }  // namespace
 
+// Build-time worker trace (-DQSF_SERVER_TRACE): host seconds per phase of the worker
+// loop, printed to stderr when the server stops.
+#ifdef QSF_SERVER_TRACE
+#include <cstdio>
+#define QSF_TRACE_T(v) const auto v = clk::now()
+#define QSF_TRACE_ADD(s, k, t0) ((s)->trace[k] += std::chrono::duration<double>(clk::now() - (t0)).count())
+#else
+#define QSF_TRACE_T(v)
+#define QSF_TRACE_ADD(s, k, t0)
+#endif
+
 struct qsf_server {
   qsf_server_config cfg{};
+#ifdef QSF_SERVER_TRACE
+  double trace[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // decide, admit, enqueue, batch, wait, retire, rounds, admits
+#endif
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Pending> queue;
@@ -249,6 +263,7 @@ void worker_loop(qsf_server* s) {
   for (;;) {
     // admission
     std::vector<Pending> take;
+    QSF_TRACE_T(t_decide);
     {
       std::unique_lock<std::mutex> lk(s->mu);
       if (s->running.empty() && s->queue.empty()) {
@@ -297,6 +312,8 @@ void worker_loop(qsf_server* s) {
       }
       s->cancel_running.clear();
     }
+    QSF_TRACE_ADD(s, 0, t_decide);
+    QSF_TRACE_T(t_admit);
     for (Pending& p : take) {
       Running r;
       r.ticket = p.ticket;
@@ -309,7 +326,12 @@ void worker_loop(qsf_server* s) {
       }
       s->running.emplace(r.ticket, std::move(r));
     }
+    QSF_TRACE_ADD(s, 1, t_admit);
+#ifdef QSF_SERVER_TRACE
+    s->trace[7] += (double)take.size();
+#endif
     if (s->running.empty()) continue;
+    QSF_TRACE_T(t_enqueue);
     // one round of steps for every resident solve: the member-operation solves' steps
     // queued first on their own streams (they overlap with one another and with the
     // batch), then the batch's round, then a wait for each member-operation solve
@@ -325,14 +347,23 @@ void worker_loop(qsf_server* s) {
       r.d.coupling = r.coupling.empty() ? nullptr : r.coupling.data();
       if (!r.cancel && !r.rc && count > 0) r.rc = qsf::generic_enqueue(r.grid, &r.d, first, count);
     }
+    QSF_TRACE_ADD(s, 2, t_enqueue);
+    QSF_TRACE_T(t_batch);
     int64_t active = 0;
     const int rc_run = any_fused ? qsf_batch_run(s->batch, s->cfg.steps_per_round, &active) : QSF_OK;
+    QSF_TRACE_ADD(s, 3, t_batch);
+    QSF_TRACE_T(t_wait);
     for (auto& kv : s->running) {
       Running& r = kv.second;
       if (!r.generic) continue;
       const int rw = qsf::generic_wait(r.grid, &r.bad);
       if (rw && !r.rc) r.rc = rw;
     }
+    QSF_TRACE_ADD(s, 4, t_wait);
+    QSF_TRACE_T(t_retire);
+#ifdef QSF_SERVER_TRACE
+    s->trace[6] += 1.0;
+#endif
     // retire finished, cancelled and failed solves.  A numeric failure (QSF_ENUMERIC)
     // belongs to single members, which qsf_batch_result names; any other error of the
     // round ends every resident solve.
@@ -370,6 +401,7 @@ void worker_loop(qsf_server* s) {
       finish(s, r, rc, rows.data(), steps);
       s->running.erase(t);
     }
+    QSF_TRACE_ADD(s, 5, t_retire);
   }
 }
 
@@ -489,6 +521,13 @@ int qsf_server_stop(qsf_server* s) {
     s->cv_done.notify_all();
   }
   if (s->worker.joinable()) s->worker.join();
+#ifdef QSF_SERVER_TRACE
+  std::fprintf(stderr,
+               "qsf_server trace: decide %.3f s, admit %.3f s (%.0f), enqueue %.3f s, batch %.3f s, wait %.3f s, "
+               "retire %.3f s, rounds %.0f\n",
+               s->trace[0], s->trace[1], s->trace[7], s->trace[2], s->trace[3], s->trace[4], s->trace[5],
+               s->trace[6]);
+#endif
   drain_pool(s);
   qsf_batch_destroy(s->batch);
   delete s;
