@@ -381,13 +381,14 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, ste
                                                                               steps_per_solve),
                        psi0=states[key], obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box)
         if t is not None:
-            tickets.append(t)
-            pts += float(n ** dim) * steps_per_solve
-    lat = []
-    for t in tickets:
+            tickets.append((t, float(n ** dim) * steps_per_solve))
+    lat, statuses = [], {}
+    for t, tp in tickets:  # grid-point-steps of the solves that completed
         r = srv.wait(t, 3600)
+        statuses[r["status"]] = statuses.get(r["status"], 0) + 1
         if r["status"] == 0:
             lat.append(r["latency_s"])
+            pts += tp
     wall = _max_over_ranks(ws, time.perf_counter() - t0)
     srv.stop()
     pts = _sum_over_ranks(ws, pts)
@@ -399,6 +400,7 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, ste
     lat.sort()
     pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
     return {"rate_per_s": rate, "submitted": _sum_over_ranks(ws, len(tickets)), "completed": len(lat),
+            "statuses": {str(k): v for k, v in sorted(statuses.items())},
             "value": pts / wall, "unit": UNIT,
             "p50_s": pct(0.50), "p99_s": pct(0.99), "wall_s": wall,
             "workload": f"served: Poisson {rate}/s for {duration_s}s, 50/50 1D N uniform over the integers "

@@ -190,7 +190,10 @@ int make_tensor_maps(qsf_grid* g) {
            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
         CUDA_SUCCESS)
       continue;  // this axis keeps cp.async loads
-    QSF_CU(cudaMemcpy(g->tmaps + 128 * ax, &map, sizeof(map), cudaMemcpyHostToDevice));
+    // on the grid's stream and waited for: a pageable copy on another stream may still
+    // be in flight when it returns, unordered with the grid's later work
+    QSF_CU(cudaMemcpyAsync(g->tmaps + 128 * ax, &map, sizeof(map), cudaMemcpyHostToDevice, g->stream));
+    QSF_CU(cudaStreamSynchronize(g->stream));
     G.tmap[ax] = g->tmaps + 128 * ax;
   }
   return QSF_OK;
@@ -226,6 +229,9 @@ int qsf::make_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf) {
   QSF_CU(cudaMemcpy(*tw, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
   QSF_CU(cudaMemcpy(*twx, hx.data(), hx.size() * sizeof(longlong2), cudaMemcpyHostToDevice));
   QSF_CU(cudaMemcpy(*twf, hf.data(), hf.size() * sizeof(longlong2), cudaMemcpyHostToDevice));
+  // a pageable copy may return before its transfer lands; the tables are shared by
+  // every stream, so wait for the device
+  QSF_CU(cudaDeviceSynchronize());
   return QSF_OK;
 }
 
@@ -407,11 +413,16 @@ int ensure_flux(qsf_grid* g, int nb, const int* types, int64_t box) {
   if ((rc = dev_alloc(g->row_ptr, rp.size()))) return rc;
   if ((rc = dev_alloc(g->fpts, std::max<size_t>(fps.size(), 1)))) return rc;
   if ((rc = dev_alloc(g->fterms, std::max<size_t>(fts.size(), 1)))) return rc;
+  // on the grid's stream (ordered before its later work) and waited for
+  cudaStream_t st = g->stream;
   if (!need.empty())
-    QSF_CU(cudaMemcpy(g->snap_idx, need.data(), need.size() * sizeof(long long), cudaMemcpyHostToDevice));
-  QSF_CU(cudaMemcpy(g->row_ptr, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice));
-  if (!fps.empty()) QSF_CU(cudaMemcpy(g->fpts, fps.data(), fps.size() * sizeof(FluxPoint), cudaMemcpyHostToDevice));
-  if (!fts.empty()) QSF_CU(cudaMemcpy(g->fterms, fts.data(), fts.size() * sizeof(FluxTerm), cudaMemcpyHostToDevice));
+    QSF_CU(cudaMemcpyAsync(g->snap_idx, need.data(), need.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
+  QSF_CU(cudaMemcpyAsync(g->row_ptr, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  if (!fps.empty())
+    QSF_CU(cudaMemcpyAsync(g->fpts, fps.data(), fps.size() * sizeof(FluxPoint), cudaMemcpyHostToDevice, st));
+  if (!fts.empty())
+    QSF_CU(cudaMemcpyAsync(g->fterms, fts.data(), fts.size() * sizeof(FluxTerm), cudaMemcpyHostToDevice, st));
+  QSF_CU(cudaStreamSynchronize(st));
   g->nsnap = (int)need.size();
   g->nfpts = (int)fps.size();
   g->nfterms = (int)fts.size();
@@ -1478,6 +1489,13 @@ static int generic_ncol(const qsf_step_desc* d) {
 
 bool qsf::grid_fused(const qsf_grid* g) { return g->ks != nullptr; }
 
+// psi = 0, ordered on the grid's stream (a memset on another stream would not be
+// ordered before the grid's later work)
+int qsf::grid_clear(qsf_grid* g) {
+  QSF_CU(cudaMemsetAsync(g->G.psi, 0, (size_t)g->G.m * sizeof(double2), g->stream));
+  return QSF_OK;
+}
+
 // the launch-shape key of a step program: what its captured kernels bake in
 static std::vector<long long> generic_key(const qsf_grid* g, const qsf_step_desc* d) {
   long long dtb, bits[2];
@@ -1694,12 +1712,19 @@ int qsf_batch_destroy(qsf_batch* b) {
 }
 
 int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot) {
+  if (!b) return fail(QSF_EINVAL, "null argument");
+  QSF_CU(cudaStreamSynchronize(b->stream));
+  return qsf::batch_add_nowait(b, g, d, slot);
+}
+
+}  // extern "C"
+
+int qsf::batch_add_nowait(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot) {
   if (!b || !g || !d || !slot) return fail(QSF_EINVAL, "null argument");
   if (d->substeps > 1) return fail(QSF_EINVAL, "batched solves run plain Strang steps (substeps <= 1)");
   if (!g->ks) return fail(QSF_EINVAL, "batched grids need a line length with fused kernels in this build");
   for (auto& kv : b->members)
     if (kv.second.g == g) return fail(QSF_ESTATE, "grid is already in the batch");
-  QSF_CU(cudaStreamSynchronize(b->stream));
   BatchMember mb;
   mb.g = g;
   qsf_step_desc dd = *d;
@@ -1715,6 +1740,8 @@ int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* sl
   b->dirty = true;
   return QSF_OK;
 }
+
+extern "C" {
 
 int qsf_batch_remove(qsf_batch* b, int64_t slot) {
   if (!b) return fail(QSF_EINVAL, "null argument");
@@ -1732,6 +1759,14 @@ int qsf_batch_remove(qsf_batch* b, int64_t slot) {
 }
 
 int qsf_batch_run(qsf_batch* b, int64_t steps, int64_t* active) {
+  int rc;
+  if ((rc = qsf::batch_launch(b, steps))) return rc;
+  return qsf::batch_finish(b, active);
+}
+
+}  // extern "C"
+
+int qsf::batch_launch(qsf_batch* b, int64_t steps) {
   if (!b || steps < 0) return fail(QSF_EINVAL, "bad argument");
   int rc;
   if (b->dirty && (rc = rebuild_batch(b))) return rc;
@@ -1740,6 +1775,11 @@ int qsf_batch_run(qsf_batch* b, int64_t steps, int64_t* active) {
       const cudaError_t ce = cudaGraphLaunch(b->exec, b->stream);
       if (ce != cudaSuccess) return fail(QSF_ECUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
     }
+  return QSF_OK;
+}
+
+int qsf::batch_finish(qsf_batch* b, int64_t* active) {
+  if (!b) return fail(QSF_EINVAL, "null argument");
   const size_t nm = b->members.size();
   if (nm * 8 > b->ctl_cap) {
     if (b->ctl_host) cudaFreeHost(b->ctl_host);
@@ -1768,6 +1808,8 @@ int qsf_batch_run(qsf_batch* b, int64_t steps, int64_t* active) {
   return QSF_OK;
 }
 
+extern "C" {
+
 int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_done) {
   if (!b) return fail(QSF_EINVAL, "null argument");
   auto it = b->members.find(slot);
@@ -1786,6 +1828,7 @@ int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_do
   if (rows)
     QSF_CU(cudaMemcpy(rows, mb.g->rows_dev, (size_t)mb.nsteps * mb.ncol * sizeof(double), cudaMemcpyDeviceToHost));
   if (steps_done) *steps_done = ctl_h[2];
+  if (ctl_h[4] == 2) return fail(QSF_ETIMEDOUT, "a bulk copy into shared memory did not complete in time");
   if (ctl_h[4]) return fail(QSF_ENUMERIC, "non-finite psi, NaN or non-positive norm in this member's reductions");
   return QSF_OK;
 }

@@ -179,6 +179,8 @@ namespace qsf {
 // whether n is a line length with fused step kernels in this build
 bool fused_length(int n);
 bool grid_fused(const qsf_grid* g);
+// psi = 0 on the grid's stream
+int grid_clear(qsf_grid* g);
 // Member-operation steps of a grid without fused kernels (qsf_step's path for them),
 // in parts for the server: begin checks the program and zeroes its device rows and
 // NaN flag; enqueue queues steps [first, first + count) on the grid's stream without
@@ -188,6 +190,14 @@ int generic_begin(qsf_grid* g, const qsf_step_desc* d);
 int generic_enqueue(qsf_grid* g, const qsf_step_desc* d, int64_t first, int64_t count);
 int generic_wait(qsf_grid* g, bool* bad);
 int generic_rows(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t nsteps);
+// qsf_batch_add without waiting for the batch's stream, for a grid that no queued work
+// of the batch touches (a solve the server prepares while a round runs); it joins at
+// the next batch_launch
+int batch_add_nowait(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot);
+// qsf_batch_run in two halves: launch (rebuild after membership changes, queue the
+// steps' graph launches) and finish (wait, read every member's counters)
+int batch_launch(qsf_batch* b, int64_t steps);
+int batch_finish(qsf_batch* b, int64_t* active);
 // twiddle tables of an n-point transform shared by all grids of the process (not to
 // be freed by the caller)
 int shared_twiddles(int n, double2** tw, longlong2** twx, longlong2** twf);

@@ -22,6 +22,10 @@
 #include "qsf_gpu.h"
 
 namespace qsf {  // qsf_api.cu, qsf_bluestein.cu
+int grid_clear(qsf_grid* g);
+int batch_add_nowait(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot);
+int batch_launch(qsf_batch* b, int64_t steps);
+int batch_finish(qsf_batch* b, int64_t* active);
 bool fused_length(int n);
 int bs_size(int n, int dim);
 bool grid_fused(const qsf_grid* g);
@@ -62,6 +66,7 @@ struct Running {
   qsf_step_desc d{};
   bool bad = false;  // NaN / non-positive norm seen
   int rc = 0;        // error of a queued round
+  bool in_round = false;  // has steps in the current round (joined before it was queued)
 };
 
 int64_t grid_points(const qsf_grid_desc& d) {
@@ -154,17 +159,7 @@ int take_grid(qsf_server* s, const qsf_grid_desc& d, qsf_grid** out) {
     if (!same_grid(s->pool[i].first, d)) continue;
     qsf_grid* g = s->pool[i].second;
     s->pool.erase(s->pool.begin() + (long)i);
-    void* psi = nullptr;
-    int64_t m = 0;
-    int rc = qsf_psi_device_ptr(g, &psi);
-    if (!rc) rc = qsf_grid_size(g, &m);
-    if (!rc) rc = qsf_synchronize(g);
-    if (!rc && cudaMemset(psi, 0, (size_t)m * 16) != cudaSuccess) rc = QSF_ECUDA;
-    if (rc) {
-      qsf_grid_destroy(g);
-      return rc;
-    }
-    *out = g;
+    *out = g;  // psi is overwritten (upload) or cleared on the grid's stream by admit
     return QSF_OK;
   }
   int rc = qsf_grid_create(&d, nullptr, out);
@@ -181,6 +176,12 @@ void release_grid(qsf_server* s, const qsf_grid_desc& d, qsf_grid* g) {
 }
 
 void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t steps) {
+#ifdef QSF_SERVER_TRACE
+  if (status && status != QSF_ECANCELED)
+    std::fprintf(stderr, "qsf_server trace: ticket %lld status %d generic %d in_round %d remaining %lld n %lld: %s\n",
+                 (long long)r.ticket, status, (int)r.generic, (int)r.in_round, (long long)r.remaining,
+                 (long long)r.desc.n[0], qsf_last_error());
+#endif
   qsf_result res{};
   res.status = status;
   res.steps = steps;
@@ -208,16 +209,18 @@ void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t s
   s->cv_done.notify_all();
 }
 
-// admit one request: grid, start state, batch membership
-int admit(qsf_server* s, Pending& p, Running& r) {
+// admit one request: grid, start state, batch membership (nowait: while a round of the
+// batch runs; the new member joins the next round)
+int admit(qsf_server* s, Pending& p, Running& r, bool nowait) {
   qsf_grid* g = nullptr;
   int rc = take_grid(s, p.req.grid, &g);
   if (rc) return rc;
   const int64_t m = grid_points(p.req.grid);
   if (!p.psi0.empty()) {
     rc = qsf_upload(g, p.psi0.data(), m);
-  } else {
-    rc = qsf_add_gaussian(g, 0.0, 1.0);
+  } else {  // gaussian(0, 1) added to a cleared psi, on the grid's own stream
+    rc = qsf::grid_clear(g);
+    if (!rc) rc = qsf_add_gaussian(g, 0.0, 1.0);
     if (!rc) rc = qsf_normalize(g, nullptr);
   }
   if (rc) {
@@ -249,7 +252,7 @@ int admit(qsf_server* s, Pending& p, Running& r) {
     r.d = d;
     rc = qsf::generic_begin(g, &r.d);
   } else {
-    rc = qsf_batch_add(s->batch, g, &d, &r.slot);
+    rc = nowait ? qsf::batch_add_nowait(s->batch, g, &d, &r.slot) : qsf_batch_add(s->batch, g, &d, &r.slot);
   }
   if (rc) {
     qsf_grid_destroy(g);
@@ -313,31 +316,48 @@ void worker_loop(qsf_server* s) {
       s->cancel_running.clear();
     }
     QSF_TRACE_ADD(s, 0, t_decide);
-    QSF_TRACE_T(t_admit);
-    for (Pending& p : take) {
-      Running r;
-      r.ticket = p.ticket;
-      r.submitted = p.submitted;
-      r.admitted = clk::now();
-      const int rc = admit(s, p, r);
-      if (rc) {
-        finish(s, r, rc, nullptr, 0);
-        continue;
+    // Admissions cost host time (grid creation or reuse, psi upload, tables).  While
+    // solves are resident, the new ones are prepared after this round's work is queued,
+    // so that this host work overlaps the GPU's round: a member-operation solve starts
+    // its first steps at once on its own stream, a batched one joins the next round.
+    const bool overlap = !s->running.empty();
+    auto admit_all = [&]() {
+      QSF_TRACE_T(t_admit);
+      for (Pending& p : take) {
+        Running r;
+        r.ticket = p.ticket;
+        r.submitted = p.submitted;
+        r.admitted = clk::now();
+        const int rc = admit(s, p, r, overlap);
+        if (rc) {
+          finish(s, r, rc, nullptr, 0);
+          continue;
+        }
+        if (r.generic && overlap) {
+          const int64_t count = std::min<int64_t>(s->cfg.steps_per_round, r.remaining);
+          r.d.coupling = r.coupling.empty() ? nullptr : r.coupling.data();
+          r.rc = qsf::generic_enqueue(r.grid, &r.d, 0, count);
+          r.in_round = true;
+        } else {
+          r.in_round = !overlap;
+        }
+        s->running.emplace(r.ticket, std::move(r));
       }
-      s->running.emplace(r.ticket, std::move(r));
-    }
-    QSF_TRACE_ADD(s, 1, t_admit);
+      QSF_TRACE_ADD(s, 1, t_admit);
 #ifdef QSF_SERVER_TRACE
-    s->trace[7] += (double)take.size();
+      s->trace[7] += (double)take.size();
 #endif
+    };
+    if (!overlap) admit_all();
     if (s->running.empty()) continue;
     QSF_TRACE_T(t_enqueue);
     // one round of steps for every resident solve: the member-operation solves' steps
-    // queued first on their own streams (they overlap with one another and with the
-    // batch), then the batch's round, then a wait for each member-operation solve
+    // queued on their own streams (they overlap with one another and with the batch),
+    // then the batch's round; then the admissions; then the waits
     bool any_fused = false;
     for (auto& kv : s->running) {
       Running& r = kv.second;
+      r.in_round = true;
       if (!r.generic) {
         any_fused = true;
         continue;
@@ -350,12 +370,14 @@ void worker_loop(qsf_server* s) {
     QSF_TRACE_ADD(s, 2, t_enqueue);
     QSF_TRACE_T(t_batch);
     int64_t active = 0;
-    const int rc_run = any_fused ? qsf_batch_run(s->batch, s->cfg.steps_per_round, &active) : QSF_OK;
+    int rc_run = any_fused ? qsf::batch_launch(s->batch, s->cfg.steps_per_round) : QSF_OK;
+    if (overlap) admit_all();
+    if (any_fused && rc_run == QSF_OK) rc_run = qsf::batch_finish(s->batch, &active);
     QSF_TRACE_ADD(s, 3, t_batch);
     QSF_TRACE_T(t_wait);
     for (auto& kv : s->running) {
       Running& r = kv.second;
-      if (!r.generic) continue;
+      if (!r.generic || !r.in_round) continue;
       const int rw = qsf::generic_wait(r.grid, &r.bad);
       if (rw && !r.rc) r.rc = rw;
     }
@@ -371,12 +393,13 @@ void worker_loop(qsf_server* s) {
     std::vector<int64_t> done;
     for (auto& kv : s->running) {
       Running& r = kv.second;
+      if (!r.in_round && !fatal) continue;  // joined the batch during this round: runs from the next
       const int64_t ran = r.cancel && r.generic ? 0 : std::min<int64_t>(s->cfg.steps_per_round, r.remaining);
-      r.remaining -= r.generic ? ran : s->cfg.steps_per_round;
+      if (r.in_round) r.remaining -= r.generic ? ran : s->cfg.steps_per_round;
       bool bad = r.generic && (r.bad || r.rc);
-      if (!r.generic && rc_run == QSF_ENUMERIC) {
+      if (!r.generic && r.in_round && rc_run == QSF_ENUMERIC) {
         int64_t st = 0;
-        bad = qsf_batch_result(s->batch, r.slot, nullptr, &st) == QSF_ENUMERIC;
+        bad = qsf_batch_result(s->batch, r.slot, nullptr, &st) != QSF_OK;
       }
       if (r.remaining <= 0 || fatal || bad || r.cancel) done.push_back(kv.first);
     }
