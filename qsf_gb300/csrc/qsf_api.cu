@@ -1229,19 +1229,33 @@ int qsf_evolve(qsf_grid* g, int mode, int rep, double delta, const double* c3) {
 
 // evolve<mode, rep>(delta) with the coupling values from c3 (host) or, when cd.c is
 // set, from the device rows of a step program
+// the X factor table of evolve<mode, X>(delta) without X-space coupling, per point:
+// evaluated once and reused while (mode, delta) stay the same
+static int ensure_xtab(qsf_grid* g, int mode, double delta) {
+  if (g->etab && g->etab_mode == mode && g->etab_delta == delta) return QSF_OK;
+  if (!g->etab)
+    if (int rc = dev_alloc(g->etab, (size_t)g->G.m)) return rc;
+  k_evolve_xtab<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, mode, delta, g->etab);
+  g->etab_mode = mode;
+  g->etab_delta = delta;
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
+// the potential per point for E_pot averages (built on first use)
+static int ensure_vtab(qsf_grid* g) {
+  if (g->vtab) return QSF_OK;
+  if (int rc = dev_alloc(g->vtab, (size_t)g->G.m)) return rc;
+  k_build_vtab<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, g->vtab);
+  QSF_CU(cudaGetLastError());
+  return QSF_OK;
+}
+
 static int evolve_impl(qsf_grid* g, int mode, int rep, double delta, const double* c3, CoupDev cd) {
   const double c0 = c3 ? c3[0] : 0.0, c1 = c3 ? c3[1] : 0.0, c2 = c3 ? c3[2] : 0.0;
   const GridDev& G = g->G;
   if (rep == QSF_REP_X && !(G.gauge == QSF_GAUGE_LENGTH && G.n_fields)) {
-    // no X-space coupling: the factor per point depends on (mode, delta) only; it is
-    // evaluated once and reused while they stay the same
-    if (!g->etab || g->etab_mode != mode || g->etab_delta != delta) {
-      if (!g->etab)
-        if (int rc = dev_alloc(g->etab, (size_t)G.m)) return rc;
-      k_evolve_xtab<<<grid_blocks(G.m), 256, 0, g->stream>>>(G, mode, delta, g->etab);
-      g->etab_mode = mode;
-      g->etab_delta = delta;
-    }
+    if (int rc = ensure_xtab(g, mode, delta)) return rc;
     k_apply_xtab<<<grid_blocks(G.m), 256, 0, g->stream>>>(G.psi, g->etab, G.m);
   } else if (rep == QSF_REP_P) {
     if (!g->eptab)
@@ -1260,10 +1274,7 @@ static int evolve_impl(qsf_grid* g, int mode, int rep, double delta, const doubl
 static int launch_average(qsf_grid* g, int rep, int op, int* nblocks) {
   const int nb = std::min(256, grid_blocks(g->G.m));
   if (rep == QSF_REP_X && op == QSF_OP_POTENTIAL) {
-    if (!g->vtab) {
-      if (int rc = dev_alloc(g->vtab, (size_t)g->G.m)) return rc;
-      k_build_vtab<<<grid_blocks(g->G.m), 256, 0, g->stream>>>(g->G, g->vtab);
-    }
+    if (int rc = ensure_vtab(g)) return rc;
     k_average_tab<<<nb, 256, 0, g->stream>>>(g->G, g->vtab, g->partials);
   } else {
     k_average<<<nb, 256, 0, g->stream>>>(g->G, rep, op, g->partials);
@@ -1523,7 +1534,7 @@ int qsf::generic_begin(qsf_grid* g, const qsf_step_desc* d) {
   }
   QSF_CU(cudaMemsetAsync(g->rows_dev, 0, (size_t)d->nsteps * ncol * sizeof(double), g->stream));
   QSF_CU(cudaMemsetAsync(g->ctl, 0, 8 * sizeof(long long), g->stream));  // [0] step, [4] NaN flag
-  g->gen_warm = false;
+  g->gen_primed = false;
   return QSF_OK;
 }
 
@@ -1583,22 +1594,37 @@ static bool generic_ekin_at(const qsf_step_desc* d, int64_t s, int64_t stop_afte
   return (d->obs & QSF_OBS_EKIN) && ((s + 1) % every == 0 || s + 1 == d->nsteps || s == stop_after);
 }
 
+// steps per captured graph of a member-operation step program
+#ifndef QSF_GEN_GRAPH_STEPS
+#define QSF_GEN_GRAPH_STEPS 16
+#endif
+
+// The member operations' tables a step program uses, made before any capture (a
+// capture may not allocate): the X factor for (mode, dt/2K) where no coupling acts in X,
+// the P factor table, the potential table for E_pot.
+static int generic_prime(qsf_grid* g, const qsf_step_desc* d) {
+  const GridDev& G = g->G;
+  const int K = std::max(1, d->substeps);
+  int rc;
+  if (!(G.gauge == QSF_GAUGE_LENGTH && G.n_fields) && (rc = ensure_xtab(g, d->mode, 0.5 * (d->dt / K)))) return rc;
+  if (!g->eptab && (rc = dev_alloc(g->eptab, (size_t)3 * g->nmax))) return rc;
+  if ((d->obs & QSF_OBS_EPOT) && (rc = ensure_vtab(g))) return rc;
+  g->gen_primed = true;
+  return QSF_OK;
+}
+
 // Steps [first, first + count) of the program (the device step index must be `first`):
 // without E_kin, runs of kGenGraphSteps steps replay one captured graph per grid (its
 // launches bake in the program's shape, so it is recaptured when that changes); the
-// first step of a program and the remainder run as plain launches.
+// remainder runs as plain launches.
 int qsf::generic_enqueue(qsf_grid* g, const qsf_step_desc* d, int64_t first, int64_t count) {
-  constexpr int kGenGraphSteps = 16;
+  constexpr int kGenGraphSteps = QSF_GEN_GRAPH_STEPS;
   if (first < 0 || count < 0 || first + count > d->nsteps) return fail(QSF_EINVAL, "steps outside the program");
   int rc;
   int64_t s = first;
   const int64_t end = first + count;
   const bool graphs = !(d->obs & QSF_OBS_EKIN);
-  if (!g->gen_warm && s < end) {  // allocates the member operations' tables outside any capture
-    if ((rc = generic_one(g, d, generic_ekin_at(d, s, d->nsteps)))) return rc;
-    ++s;
-    g->gen_warm = true;
-  }
+  if (!g->gen_primed && (rc = generic_prime(g, d))) return rc;
   if (graphs && end - s >= kGenGraphSteps) {
     const std::vector<long long> key = generic_key(g, d);
     if (!g->gen_exec || g->gen_key != key) {
@@ -1660,7 +1686,6 @@ static int generic_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64
   for (; conv && s < d->nsteps && s <= stop_after; ++s) {
     const bool ek = generic_ekin_at(d, s, stop_after);
     if ((rc = generic_one(g, d, ek))) return rc;
-    g->gen_warm = true;
     if (ek || !(d->obs & QSF_OBS_EKIN)) {
       double r[3];
       QSF_CU(cudaMemcpyAsync(r, g->rows_dev + (size_t)s * ncol, sizeof(r), cudaMemcpyDeviceToHost, g->stream));

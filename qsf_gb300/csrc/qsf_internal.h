@@ -140,12 +140,12 @@ struct qsf_grid {
   };
   std::vector<StepGraph> step_graphs;
   // member-operation step programs (grids without fused kernels): the executable graph
-  // of gen_steps steps, the program it was captured for, and whether a step has run
-  // since the program began (the first one allocates the member operations' tables)
+  // of gen_steps steps, the program it was captured for, and whether the member
+  // operations' tables of the current program are made (before any capture)
   cudaGraphExec_t gen_exec = nullptr;
   int gen_steps = 0;
   std::vector<long long> gen_key;
-  bool gen_warm = false;
+  bool gen_primed = false;
   // TMA tensor maps of psi for the strided-axis passes (GridDev::tmap), 128 bytes each
   unsigned char* tmaps = nullptr;
   // Bluestein transforms of a grid whose axis length has a prime factor above 5 (no

@@ -103,7 +103,9 @@ size_t solve_bytes(const qsf_request& r) {
 struct qsf_server {
   qsf_server_config cfg{};
 #ifdef QSF_SERVER_TRACE
-  double trace[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // decide, admit, enqueue, batch, wait, retire, rounds, admits
+  // decide, admit, enqueue, batch, wait, retire, rounds, admits, batch launch (rebuilds)
+  // admits of member-operation / batched solves (incl. their first queued steps)
+  double trace[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 #endif
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -153,9 +155,9 @@ void drain_pool(qsf_server* s) {
   s->pool.clear();
 }
 
-// a grid for this descriptor: a pooled one (psi cleared) or a new one
+// a grid for this descriptor: a pooled one (the most recently returned) or a new one
 int take_grid(qsf_server* s, const qsf_grid_desc& d, qsf_grid** out) {
-  for (size_t i = 0; i < s->pool.size(); ++i) {
+  for (size_t i = s->pool.size(); i-- > 0;) {
     if (!same_grid(s->pool[i].first, d)) continue;
     qsf_grid* g = s->pool[i].second;
     s->pool.erase(s->pool.begin() + (long)i);
@@ -170,9 +172,15 @@ int take_grid(qsf_server* s, const qsf_grid_desc& d, qsf_grid** out) {
   return rc;
 }
 
+// a finished solve's grid goes to the back of the pool; a full pool gives up its least
+// recently returned grid (so that a stream of one-off sizes does not crowd out the
+// sizes that come back)
 void release_grid(qsf_server* s, const qsf_grid_desc& d, qsf_grid* g) {
-  if ((int)s->pool.size() < s->cfg.max_slots) s->pool.emplace_back(d, g);
-  else qsf_grid_destroy(g);
+  s->pool.emplace_back(d, g);
+  if ((int)s->pool.size() > s->cfg.max_slots) {
+    qsf_grid_destroy(s->pool.front().second);
+    s->pool.erase(s->pool.begin());
+  }
 }
 
 void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t steps) {
@@ -328,6 +336,7 @@ void worker_loop(qsf_server* s) {
         r.ticket = p.ticket;
         r.submitted = p.submitted;
         r.admitted = clk::now();
+        QSF_TRACE_T(t_one);
         const int rc = admit(s, p, r, overlap);
         if (rc) {
           finish(s, r, rc, nullptr, 0);
@@ -341,6 +350,9 @@ void worker_loop(qsf_server* s) {
         } else {
           r.in_round = !overlap;
         }
+#ifdef QSF_SERVER_TRACE
+        QSF_TRACE_ADD(s, r.generic ? 9 : 10, t_one);
+#endif
         s->running.emplace(r.ticket, std::move(r));
       }
       QSF_TRACE_ADD(s, 1, t_admit);
@@ -370,7 +382,9 @@ void worker_loop(qsf_server* s) {
     QSF_TRACE_ADD(s, 2, t_enqueue);
     QSF_TRACE_T(t_batch);
     int64_t active = 0;
+    QSF_TRACE_T(t_launch);
     int rc_run = any_fused ? qsf::batch_launch(s->batch, s->cfg.steps_per_round) : QSF_OK;
+    QSF_TRACE_ADD(s, 8, t_launch);
     if (overlap) admit_all();
     if (any_fused && rc_run == QSF_OK) rc_run = qsf::batch_finish(s->batch, &active);
     QSF_TRACE_ADD(s, 3, t_batch);
@@ -546,10 +560,10 @@ int qsf_server_stop(qsf_server* s) {
   if (s->worker.joinable()) s->worker.join();
 #ifdef QSF_SERVER_TRACE
   std::fprintf(stderr,
-               "qsf_server trace: decide %.3f s, admit %.3f s (%.0f), enqueue %.3f s, batch %.3f s, wait %.3f s, "
-               "retire %.3f s, rounds %.0f\n",
-               s->trace[0], s->trace[1], s->trace[7], s->trace[2], s->trace[3], s->trace[4], s->trace[5],
-               s->trace[6]);
+               "qsf_server trace: decide %.3f s, admit %.3f s (%.0f; member programs %.3f s, batched %.3f s), "
+               "enqueue %.3f s, batch %.3f s (launch %.3f s), wait %.3f s, retire %.3f s, rounds %.0f\n",
+               s->trace[0], s->trace[1], s->trace[7], s->trace[9], s->trace[10], s->trace[2], s->trace[3],
+               s->trace[8], s->trace[4], s->trace[5], s->trace[6]);
 #endif
   drain_pool(s);
   qsf_batch_destroy(s->batch);
