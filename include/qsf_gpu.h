@@ -291,7 +291,10 @@ int qsf_batch_result(qsf_batch* b, int64_t slot, double* rows, int64_t* steps_do
  * admitted while a slot is free and enough HBM stays free, join the running batch
  * between rounds of steps (their wavefunctions stay resident on the device for the
  * whole solve), and leave it when their last step is done, returning yields, flux
- * integrals and latencies.  No counterpart in the reference. */
+ * integrals and latencies.  Admissions are prepared while a round runs.  Solves of
+ * axis lengths outside the built kernel list run beside the batch, each on its own
+ * stream, as graph-replayed member-operation programs.  No counterpart in the
+ * reference. */
 typedef struct qsf_request {
   qsf_grid_desc grid;
   int mode;                 /* QSF_MODE_RE or QSF_MODE_IM                               */

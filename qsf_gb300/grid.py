@@ -36,6 +36,11 @@ def _dp(a: np.ndarray):
 
 
 class Grid:
+    """One wavefunction on the GPU (qsf_grid_create).  Axis lengths: any n >= 2 up to
+    16384 on a 1D line and 4096 per axis in 2D / 3D; lengths of the built kernel list
+    (2^a 3^b 5^c) take the fused step kernels, the others (up to 2048 per axis in 2D / 3D)
+    Bluestein transforms and graph-replayed member-operation step programs."""
+
     def __init__(self, dim: int, n, dx, nCAP: int = 0, potential: int = POT_EBERLY, Ncharge: float = 1.0,
                  Echarge: float = -1.0, Nsoft: float = 1.0, Esoft: float = 1.0, gauge: int = 0,
                  n_fields: int = 0, p_axis_swap: Optional[bool] = None, border_nodes=(25, 14, 10, 40),
