@@ -105,7 +105,9 @@ struct qsf_server {
 #ifdef QSF_SERVER_TRACE
   // decide, admit, enqueue, batch, wait, retire, rounds, admits, batch launch (rebuilds)
   // admits of member-operation / batched solves (incl. their first queued steps)
-  double trace[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  // admission parts: grid (pool or new), psi upload, batch add / member program begin,
+  // grids created new
+  double trace[15] = {0};
 #endif
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -221,8 +223,17 @@ void finish(qsf_server* s, Running& r, int status, const double* rows, int64_t s
 // batch runs; the new member joins the next round)
 int admit(qsf_server* s, Pending& p, Running& r, bool nowait) {
   qsf_grid* g = nullptr;
+  QSF_TRACE_T(t_grid);
+#ifdef QSF_SERVER_TRACE
+  const size_t pooled = s->pool.size();
+#endif
   int rc = take_grid(s, p.req.grid, &g);
+  QSF_TRACE_ADD(s, 11, t_grid);
+#ifdef QSF_SERVER_TRACE
+  if (s->pool.size() == pooled) s->trace[14] += 1.0;
+#endif
   if (rc) return rc;
+  QSF_TRACE_T(t_upload);
   const int64_t m = grid_points(p.req.grid);
   if (!p.psi0.empty()) {
     rc = qsf_upload(g, p.psi0.data(), m);
@@ -231,6 +242,7 @@ int admit(qsf_server* s, Pending& p, Running& r, bool nowait) {
     if (!rc) rc = qsf_add_gaussian(g, 0.0, 1.0);
     if (!rc) rc = qsf_normalize(g, nullptr);
   }
+  QSF_TRACE_ADD(s, 12, t_upload);
   if (rc) {
     qsf_grid_destroy(g);
     return rc;
@@ -255,6 +267,7 @@ int admit(qsf_server* s, Pending& p, Running& r, bool nowait) {
   d.nborders = p.req.nborders;
   for (int b = 0; b < QSF_MAX_BORDERS; ++b) d.border_types[b] = p.req.border_types[b];
   d.box_size = p.req.box_size;
+  QSF_TRACE_T(t_add);
   if (!qsf::grid_fused(g)) {
     r.generic = true;
     r.d = d;
@@ -262,6 +275,7 @@ int admit(qsf_server* s, Pending& p, Running& r, bool nowait) {
   } else {
     rc = nowait ? qsf::batch_add_nowait(s->batch, g, &d, &r.slot) : qsf_batch_add(s->batch, g, &d, &r.slot);
   }
+  QSF_TRACE_ADD(s, 13, t_add);
   if (rc) {
     qsf_grid_destroy(g);
     r.grid = nullptr;
@@ -564,6 +578,8 @@ int qsf_server_stop(qsf_server* s) {
                "enqueue %.3f s, batch %.3f s (launch %.3f s), wait %.3f s, retire %.3f s, rounds %.0f\n",
                s->trace[0], s->trace[1], s->trace[7], s->trace[9], s->trace[10], s->trace[2], s->trace[3],
                s->trace[8], s->trace[4], s->trace[5], s->trace[6]);
+  std::fprintf(stderr, "qsf_server trace: admission parts: grid %.3f s (%.0f new), upload %.3f s, add %.3f s\n",
+               s->trace[11], s->trace[14], s->trace[12], s->trace[13]);
 #endif
   drain_pool(s);
   qsf_batch_destroy(s->batch);
