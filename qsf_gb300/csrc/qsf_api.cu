@@ -1015,12 +1015,17 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   g->l2m = 0;
   while ((1LL << (g->l2m + 1)) <= G.m) ++g->l2m;
   g->m_mant = std::ldexp(1.0, g->l2m) / (double)G.m;
-  if ((rc = dev_alloc(g->ibuf, (size_t)kTexp + kGmin + 4 * (size_t)g->scmax)) ||
-      (rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) || (rc = dev_alloc(g->xdyn, (size_t)3 * D * g->nmax)) ||
-      (rc = dev_alloc(g->partials, (size_t)5 * g->pmax)) || (rc = dev_alloc(g->ctl, 8)) ||
+  if ((rc = dev_alloc(g->partials, (size_t)5 * g->pmax)) || (rc = dev_alloc(g->ctl, 8)) ||
       (rc = dev_alloc(g->energy, 2)) || (rc = dev_alloc(g->scale, 2)) ||
-      (rc = dev_alloc(g->fpartials, (size_t)kMaxFluxBlocks * kMaxFluxBorders)) || (rc = dev_alloc(g->dG, 1)) ||
-      (rc = dev_alloc(g->dS, 1))) {
+      (rc = dev_alloc(g->fpartials, (size_t)kMaxFluxBlocks * kMaxFluxBorders))) {
+    qsf_grid_destroy(g);
+    return rc;
+  }
+  // the fused kernels' exponent slots, per-step tables and device descriptors
+  if (ks && ((rc = dev_alloc(g->ibuf, (size_t)kTexp + kGmin + 4 * (size_t)g->scmax)) ||
+             (rc = dev_alloc(g->ptab, (size_t)D * g->nmax)) ||
+             (rc = dev_alloc(g->xdyn, (size_t)3 * D * g->nmax)) || (rc = dev_alloc(g->dG, 1)) ||
+             (rc = dev_alloc(g->dS, 1)))) {
     qsf_grid_destroy(g);
     return rc;
   }
@@ -1029,7 +1034,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
     qsf_grid_destroy(g);
     return rc;
   }
-  cudaMemcpyAsync(g->dG, &g->G, sizeof(GridDev), cudaMemcpyHostToDevice, g->stream);
+  if (ks) cudaMemcpyAsync(g->dG, &g->G, sizeof(GridDev), cudaMemcpyHostToDevice, g->stream);
   cudaMemsetAsync(g->partials, 0, sizeof(double) * 5 * g->pmax, g->stream);
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) {
     qsf_grid_destroy(g);

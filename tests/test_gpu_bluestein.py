@@ -19,7 +19,8 @@ TOL_FFT = 4e-14
 FLUX_RES = {1: 1e-19, 2: 1e-18, 3: 1e-18}
 
 
-@pytest.mark.parametrize("n", [7, 11, 97, 100, 127, 1021, 1031, 3001, 4099, 8191, 8209, 9973, 12289, 16383])
+@pytest.mark.parametrize("n", [2, 3, 4, 5, 6, 7, 11, 97, 100, 127, 1021, 1031, 3001, 4099, 8191, 8209, 9973, 12289,
+                               16383])
 def test_bluestein_1d_matches_numpy(n):
     """Up to 8191 points one M-point transform (M <= 16384); above, M = M1 * M2 as a
     four-step transform."""
@@ -35,7 +36,8 @@ def test_bluestein_1d_matches_numpy(n):
     g.close()
 
 
-@pytest.mark.parametrize("dim,n", [(2, 7), (2, 63), (2, 127), (2, 1021), (3, 14), (3, 35), (3, 97)])
+@pytest.mark.parametrize("dim,n", [(2, 2), (2, 5), (2, 7), (2, 63), (2, 127), (2, 1021), (3, 3), (3, 14), (3, 35),
+                                   (3, 97)])
 def test_bluestein_nd_matches_numpy(dim, n):
     import qsf_gb300 as Q
     rng = np.random.default_rng(11 * n + dim)
@@ -213,3 +215,35 @@ def test_bluestein_multi_region_grid_matches_oracle():
     for r in range(4):
         assert np.linalg.norm(gs[r].psi) > 0, r
         assert C.rel_l2(psis[r], gs[r].psi) < 1e-10, r
+
+
+@pytest.mark.parametrize("dim,n", [(1, 2), (1, 5), (2, 3), (3, 4)])
+def test_tiny_grids_step_like_the_oracle(dim, n):
+    """The smallest grids (no fused kernels: lengths below 8 run as Bluestein lengths)
+    step through the member-operation program like the oracle: norm and E_pot rows and
+    the final psi."""
+    import qsf_gb300 as Q
+    from oracle import oracle as O
+    from qsf_gb300.propagator import coupling_schedule
+    dx, dt, steps = 0.7, 0.05, 12
+    rng = np.random.default_rng(n + 10 * dim)
+    psi0 = rng.standard_normal((n,) * dim) + 1j * rng.standard_normal((n,) * dim)
+    pulse = dict(field=0.1, omega=1.0, ncycles=1.0)
+    axis = {1: 1, 2: 3, 3: 7}[dim]
+    oc = O.Coupling(O.GAUGE_VELOCITY, [O.Field(axis, [O.Pulse(**pulse)])])
+    og = O.Grid(dim, n, dx, nCAP=0, Ncharge=float(dim), coupling=oc)
+    og.psi[...] = psi0
+    prop = O.Propagator(O.MODE_RE, dt, 0, og, ["norm", "epot"])
+    orows = []
+    for _ in range(steps):
+        prop.make_step()
+        prop.compute_each()
+        orows.append([prop.rows[-1]["norm"], prop.rows[-1]["epot"]])
+    g = Q.Grid(dim, n, dx, nCAP=0, Ncharge=float(dim), gauge=Q.GAUGE_VELOCITY, n_fields=1)
+    g.upload(psi0)
+    c = Q.Coupling(Q.GAUGE_VELOCITY, [Q.Field(axis, [Q.Pulse(**pulse)])])
+    rows, done = g.step(Q.MODE_RE, dt, steps, coupling_schedule(c, dt, steps)[0], obs=Q.OBS_NORM | Q.OBS_EPOT)
+    assert done == steps
+    np.testing.assert_allclose(rows[:, :2], np.array(orows), rtol=1e-11, atol=1e-14)
+    assert C.rel_l2(g.download(), og.psi) < 1e-12
+    g.close()
