@@ -11,6 +11,7 @@ and the rejection of such grids by batches."""
 import numpy as np
 import pytest
 
+from oracle import oracle as O
 from tests import cases as C
 
 pytestmark = pytest.mark.gpu
@@ -246,4 +247,34 @@ def test_tiny_grids_step_like_the_oracle(dim, n):
     assert done == steps
     np.testing.assert_allclose(rows[:, :2], np.array(orows), rtol=1e-11, atol=1e-14)
     assert C.rel_l2(g.download(), og.psi) < 1e-12
+    g.close()
+
+
+@pytest.mark.parametrize("K,lg", [(2, 0), (3, 1)])
+def test_bluestein_multiproduct_matches_oracle(K, lg):
+    """MultiProductSplit<Split3Base, K> on a Bluestein length (1D, 733 points) against the
+    oracle's literal chains (propagator.h:331-413): the step program's sub-steps."""
+    import qsf_gb300 as Q
+    n, dx = 733, 0.2
+    p = _params(n, dx, lg)
+    p["F0"], p["omega"], p["ncycles"] = 0.06, 1.0, 1.0
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    psi0 = (np.exp(-0.5 * x * x) * (1 + 0.2j * x)).astype(np.complex128)
+    psi0 /= np.sqrt(np.sum(np.abs(psi0) ** 2) * dx)
+    outs = ["step", "time", "norm", "epot"]
+    oc = O.Coupling(O.GAUGE_LENGTH if lg else O.GAUGE_VELOCITY, [O.Field(1, [C.pulse(p)])])
+    og = C.oracle_grid(p, 1, oc)
+    og.psi[...] = psi0
+    orows = O.Propagator(O.MODE_RE, p["re_dt"], 0, og, outs, order=K).run()
+    gauge = Q.GAUGE_LENGTH if lg else Q.GAUGE_VELOCITY
+    g = C.gpu_grid(p, 1, gauge, 1)
+    g.upload(psi0)
+    rows = Q.SplitPropagator(Q.MODE_RE, p["re_dt"], 0, g, Q.Coupling(gauge, [Q.Field(1, [C.gpu_pulse(p)])]), outs,
+                             order=K).run()
+    got = np.array([[r[k] for k in outs] for r in rows])
+    ref = np.array([[r[k] for k in outs] for r in orows])
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got[:, :2], ref[:, :2], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(got[:, 2:], ref[:, 2:], rtol=1e-10, atol=0)
+    assert C.rel_l2(g.download(), og.psi) < 1e-11
     g.close()
