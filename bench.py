@@ -344,15 +344,45 @@ def run_batched(steps, warmup, nsolves=256, seed=0, plain_arm=True, ws=1, rank=0
     return out
 
 
-def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, steps_per_round=16, ws=1, rank=0):
+def _plain_sample_rate(Q, reqs):
+    """The plain path on a sample of the served requests: each solve alone through
+    qsf_step (grids made beforehand, one step call per solve, one after another on one
+    stream), grid-point-steps over the summed device time."""
+    import torch
+    stream = torch.cuda.Stream()
+    grids = []
+    for dim, n, dx, coupling, psi0, borders, box, nsteps in reqs:
+        g = Q.Grid(dim, n, dx, nCAP=n // 10, Ncharge=float(dim), gauge=Q.GAUGE_VELOCITY, n_fields=1,
+                   stream=stream.cuda_stream)
+        g.upload(psi0)
+        grids.append(g)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pts = 0.0
+    a.record(stream)
+    for g, (dim, n, dx, coupling, psi0, borders, box, nsteps) in zip(grids, reqs):
+        g.step(Q.MODE_RE, DT, nsteps, coupling, obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box)
+        pts += float(n ** dim) * nsteps
+    b.record(stream)
+    torch.cuda.synchronize()
+    for g in grids:
+        g.close()
+    return pts / (a.elapsed_time(b) / 1e3)
+
+
+def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, steps_per_round=16, ws=1, rank=0,
+               plain_sample=0):
     """Poisson arrivals at `rate`/s for `duration_s`: 50/50 1D (N uniform over 1024..16384)
     and 2D (edge in 256..1024 with fused kernels) solves with seeded pulses; each solve runs its first
     `steps_per_solve` steps.  Returns throughput and p50/p99 submit->completion.  With
     several ranks every rank follows the same seeded stream and serves the requests
-    shard.StreamAssigner gives it (serve.ShardedServer)."""
+    shard.StreamAssigner gives it (serve.ShardedServer).  With plain_sample = k the first k
+    requests also run one by one through qsf_step after the served run, and the line
+    reports that plain rate and the served value over it."""
     import qsf_gb300 as Q
     from qsf_gb300 import serve as S
     rng = np.random.default_rng(seed)
+    sample = []
     srv = S.ShardedServer(rank, ws, max_slots=max_slots, hbm_reserve_gb=16.0, steps_per_round=steps_per_round)
     tickets, pts = [], 0.0
     t0 = time.perf_counter()
@@ -377,9 +407,11 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, ste
             states[key] = _gauss_state(dim, n, dx)
         borders = ["BOX"] if dim == 1 else Q.ZOA_FLUX_2D
         box = int(0.4 * n) if dim == 1 else 0
-        t = srv.submit(gd, Q.MODE_RE, DT, steps_per_solve, coupling=_schedule(Q, dim, inten, lam, NCYCLES,
-                                                                              steps_per_solve),
-                       psi0=states[key], obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box)
+        sched = _schedule(Q, dim, inten, lam, NCYCLES, steps_per_solve)
+        t = srv.submit(gd, Q.MODE_RE, DT, steps_per_solve, coupling=sched, psi0=states[key],
+                       obs=Q.OBS_NORM | Q.OBS_EPOT, borders=borders, box_size=box)
+        if len(sample) < plain_sample:
+            sample.append((dim, n, dx, sched, states[key], borders, box, steps_per_solve))
         if t is not None:
             tickets.append((t, float(n ** dim) * steps_per_solve))
     lat, statuses = [], {}
@@ -399,7 +431,14 @@ def run_served(rate, duration_s, steps_per_solve=256, seed=0, max_slots=128, ste
         lat = [v for part in allv for v in part]
     lat.sort()
     pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None
-    return {"rate_per_s": rate, "submitted": _sum_over_ranks(ws, len(tickets)), "completed": len(lat),
+    extra = {}
+    if sample and rank == 0:
+        plain = _plain_sample_rate(Q, sample)
+        extra = {"plain_same_solves_sample": {"value": plain, "unit": UNIT, "solves": len(sample),
+                                              "method": "the first requests of the stream, each alone through "
+                                                        "qsf_step, one after another on one stream"},
+                 "served_vs_plain_same_solves": pts / wall / plain}
+    return {"rate_per_s": rate, "submitted": _sum_over_ranks(ws, len(tickets)), "completed": len(lat), **extra,
             "statuses": {str(k): v for k, v in sorted(statuses.items())},
             "value": pts / wall, "unit": UNIT,
             "p50_s": pct(0.50), "p99_s": pct(0.99), "wall_s": wall,
@@ -702,7 +741,8 @@ def run_gpu(args):
     launches = sum(v[1] for v in kinds.values()) - max(0, kinds.get("row_open", (0.0, 1))[1] - 1)
 
     batched = run_batched(steps=20, warmup=3, ws=ws, rank=rank)
-    served = [run_served(rate=r, duration_s=2.0, ws=ws, rank=rank) for r in (10.0, 100.0, 1000.0)]
+    served = [run_served(rate=r, duration_s=2.0, ws=ws, rank=rank, plain_sample=100 if r >= 1000.0 else 0)
+              for r in (10.0, 100.0, 1000.0)]
     multigrid = run_multigrid(steps=20, warmup=3, cpu=rank == 0)
     multigrid_3d = run_multigrid(steps=5, warmup=2, cpu=False, dim=3)
     c1 = run_c1(steps=max(args.steps, 200), warmup=args.warmup, flush=flush)
@@ -784,6 +824,8 @@ def main():
     ap.add_argument("--rates", default="10,30,100,300,1000")
     ap.add_argument("--duration", type=float, default=5.0)
     ap.add_argument("--mg-dim", type=int, default=2, choices=[2, 3], help="multigrid workload: 2D 1024^2 or 3D 256^3")
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="served workload: also run the first K requests one by one through qsf_step")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -795,7 +837,8 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         for r in [float(v) for v in args.rates.split(",")]:
-            print(json.dumps({"metric": METRIC, **run_served(r, args.duration)}), flush=True)
+            print(json.dumps({"metric": METRIC, **run_served(r, args.duration, plain_sample=args.plain_sample)}),
+                  flush=True)
     elif args.workload == "multigrid":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
