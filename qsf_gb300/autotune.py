@@ -1,4 +1,5 @@
-"""Autotuner of the row / axis pass kernels: threads per block per line length.
+"""Autotuner of the pass kernels: threads per block of the row / axis passes per line
+length, and the radix plan (points per thread) of the one-CTA 1D line kernel per length.
 
 The count sets the radix plan with it: 256 threads carry 16 points of a 4096-point tile
 each (radix-16 passes, 128 registers), 512 threads 8 points (radix-8 passes, 64
@@ -9,15 +10,19 @@ one call of K graph-replayed steps after a warm-up call) in a subprocess that lo
 build; per line length the count with the least summed step time over the workloads of
 that edge wins (the 2D grid and the 3D cube of one edge share their kernels).  With
 --write the choice goes to qsf_gb300/csrc/qsf_tuning.h, which the default build
-compiles in.  Needs a GPU.
+compiles in.  The 1D line kernel's plan is tuned the same way: candidate builds force 4,
+8 or 16 points per thread (`QSF_LINE_PPT`, at least n / 512), the 1D workloads are
+timed, and each measured length keeps its fastest plan; a length between measured ones
+takes the plan of the next longer measured length.  Needs a GPU.
 
-    python -m qsf_gb300.autotune [--repeat 2] [--write]
+    python -m qsf_gb300.autotune [--repeat 2] [--write] [--only rows|lines]
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import re
 import subprocess
 import sys
 
@@ -25,6 +30,8 @@ from . import build as B
 from .profile_step import WORKLOADS
 
 CANDIDATES = (256, 512)
+LINE_CANDIDATES = (4, 8, 16)
+LINE_WORKLOADS = [("1d1024", 400), ("1d1536", 400), ("1d2048", 400), ("1d3072", 400), ("1d4096", 400)]
 # (workload of profile_step, steps per timed call)
 TUNE_WORKLOADS = [("2d256", 400), ("2d384", 400), ("2d512", 400), ("2d768", 300), ("2d1024", 300),
                   ("2d2048", 100), ("2d4096", 30), ("3d128", 100), ("3d256", 30)]
@@ -54,14 +61,46 @@ def choose(times: dict) -> dict:
     return {n: min(per, key=lambda t: per[t]) for n, per in edges.items()}
 
 
-def header_text(choice: dict, times: dict) -> str:
+def line_valid(n: int, p: int) -> bool:
+    """A plan of p points per thread fits a line of n points on the kernel's 512 threads."""
+    return p * 512 >= n
+
+
+def choose_lines(ltimes: dict) -> dict:
+    """ltimes[(workload, p)] -> ms per step; returns line length -> fastest valid p."""
+    per = {}
+    for (w, p), ms in ltimes.items():
+        n = WORKLOADS[w][1]
+        if line_valid(n, p):
+            per.setdefault(n, {})[p] = ms
+    return {n: min(c, key=lambda p: c[p]) for n, c in per.items()}
+
+
+def line_function(lchoice: dict) -> str:
+    """tuned_line_ppt(n): the plan of the smallest measured length >= n (16 above them);
+    a threshold whose plan equals the next longer one's is left out."""
+    expr, nxt = "16", 16
+    for n in sorted(lchoice, reverse=True):
+        if lchoice[n] != nxt:
+            expr, nxt = f"n <= {n} ? {lchoice[n]} : {expr}", lchoice[n]
+    return expr
+
+
+def header_text(choice: dict, times: dict, lchoice: dict = None, ltimes: dict = None) -> str:
+    lchoice = lchoice if lchoice is not None else {1024: 4, 2048: 8, 4096: 16}
     rows = []
     for w, _ in TUNE_WORKLOADS:
         cells = "  ".join(f"{t}: {times[(w, t)]:.4f}" for t in CANDIDATES if (w, t) in times)
         rows.append(f"//   {w:7s} ms/step  {cells}")
+    lrows = []
+    for w, _ in LINE_WORKLOADS:
+        cells = "  ".join(f"{p}: {ltimes[(w, p)]:.4f}" for p in LINE_CANDIDATES if ltimes and (w, p) in ltimes)
+        if cells:
+            lrows.append(f"//   {w:7s} ms/step  {cells}")
     big = sorted(n for n, t in choice.items() if t != 256)
     cond = " || ".join(f"n == {n}" for n in big) or "false"
-    return f"""// qsf_tuning.h -- threads per block of the row / axis pass kernels per line length.
+    return f"""// qsf_tuning.h -- pass kernel shapes per line length: threads per block of the row /
+// axis passes, and the radix plan of the one-CTA 1D line kernel.
 //
 // Written by the autotuner (qsf_gb300/autotune.py) from step times measured on a GB300:
 //   python -m qsf_gb300.autotune --write
@@ -78,26 +117,61 @@ __host__ __device__ constexpr int tuned_row_threads(int n) {{
   return ({cond}) ? 512 : 256;
 }}
 
+// Points per thread of the one-CTA 1D line kernel per line length (4: radix-4 plans,
+// 8: radix 8, 16: radix 16); a length between measured ones takes the plan of the next
+// longer measured length.  Measured (one call of graph-replayed steps, points per
+// thread: ms per step):
+{chr(10).join(lrows)}
+__host__ __device__ constexpr int tuned_line_ppt(int n) {{
+  return {line_function(lchoice)};
+}}
+
 }}  // namespace qsf
 """
+
+
+def committed_row_times() -> dict:
+    """The row / axis timings of the committed table (kept when only the lines are tuned)."""
+    if not os.path.exists(HEADER):
+        return {}
+    txt = open(HEADER).read()
+    times = {}
+    for w, a, b in re.findall(r"//\s+(\S+)\s+ms/step\s+256: ([0-9.]+)\s+512: ([0-9.]+)", txt):
+        times[(w, 256)] = float(a)
+        times[(w, 512)] = float(b)
+    return times
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--write", action="store_true", help="rewrite qsf_gb300/csrc/qsf_tuning.h")
+    ap.add_argument("--only", choices=["rows", "lines"], default=None)
     args = ap.parse_args()
-    times = {}
-    for t in CANDIDATES:
-        lib_path = B.build(defines=[f"QSF_ROW_THREADS={t}"], tag=f"tune_{t}")
-        for w, steps in TUNE_WORKLOADS:
-            times[(w, t)] = time_workload(lib_path, w, steps, args.repeat)
-            print(json.dumps({"workload": w, "threads": t, "ms_per_step": times[(w, t)]}), flush=True)
+    times, ltimes = {}, {}
+    if args.only != "lines":
+        for t in CANDIDATES:
+            lib_path = B.build(defines=[f"QSF_ROW_THREADS={t}"], tag=f"tune_{t}")
+            for w, steps in TUNE_WORKLOADS:
+                times[(w, t)] = time_workload(lib_path, w, steps, args.repeat)
+                print(json.dumps({"workload": w, "threads": t, "ms_per_step": times[(w, t)]}), flush=True)
+    if args.only != "rows":
+        for p in LINE_CANDIDATES:
+            lib_path = B.build(defines=[f"QSF_LINE_PPT={p}"], tag=f"tune_line{p}")
+            for w, steps in LINE_WORKLOADS:
+                if not line_valid(WORKLOADS[w][1], p):
+                    continue
+                ltimes[(w, p)] = time_workload(lib_path, w, steps, args.repeat)
+                print(json.dumps({"workload": w, "points_per_thread": p, "ms_per_step": ltimes[(w, p)]}), flush=True)
+    if not times:
+        times = committed_row_times()
     choice = choose(times)
-    print(json.dumps({"choice": {str(n): t for n, t in sorted(choice.items())}}), flush=True)
+    lchoice = choose_lines(ltimes) if ltimes else None
+    print(json.dumps({"choice": {str(n): t for n, t in sorted(choice.items())},
+                      "line_choice": {str(n): p for n, p in sorted((lchoice or {}).items())}}), flush=True)
     if args.write:
         with open(HEADER, "w") as f:
-            f.write(header_text(choice, times))
+            f.write(header_text(choice, times, lchoice, ltimes))
 
 
 if __name__ == "__main__":

@@ -49,13 +49,20 @@ __host__ __device__ constexpr int row_threads(int) { return QSF_ROW_THREADS; }
 __host__ __device__ constexpr int row_threads(int n) { return tuned_row_threads(n); }
 #endif
 __host__ __device__ constexpr int row_ppt(int n) { return 4096 / row_threads(n); }
+constexpr int kLinePptDiv = 512;  // threads of the one-CTA line kernel (kLineThreads)
 // Points per thread of the one-CTA line kernel (512 threads, one line of n points): a
 // line shorter than 8192 points leaves threads idle in radix-16 passes, and with one
 // CTA per line the per-thread work sets the step's latency, so shorter lines take
-// smaller radices (measured: 1024 points 0.041 -> 0.030 ms, 2048 0.052 -> 0.044 ms);
-// from 4096 points on the radix-16 plan's fewer passes win (4096: 0.0733 ms with
-// radix-8 passes, 0.0694 ms with radix-16 ones; 2048 stays faster with radix 8)
-__host__ __device__ constexpr int line_ppt(int n) { return n <= 1024 ? 4 : n < 4096 ? 8 : 16; }
+// smaller radices; the choice per length comes from the autotuner (tuned_line_ppt,
+// qsf_tuning.h).  At least n / 512 points per thread (the line must fit the threads);
+// the autotuner's candidate builds force one value with QSF_LINE_PPT.
+#ifdef QSF_LINE_PPT
+__host__ __device__ constexpr int line_ppt(int n) { return n / kLinePptDiv > QSF_LINE_PPT ? n / kLinePptDiv : QSF_LINE_PPT; }
+#else
+__host__ __device__ constexpr int line_ppt(int n) {
+  return n / kLinePptDiv > tuned_line_ppt(n) ? n / kLinePptDiv : tuned_line_ppt(n);
+}
+#endif
 constexpr int kLineThreads = 512;
 constexpr int kMaxFluxBorders = 16;
 // 1D lines of 1024 .. 8192 points (powers of two): one step spread over a cluster of

@@ -1,4 +1,5 @@
-// qsf_tuning.h -- threads per block of the row / axis pass kernels per line length.
+// qsf_tuning.h -- pass kernel shapes per line length: threads per block of the row /
+// axis passes, and the radix plan of the one-CTA 1D line kernel.
 //
 // Written by the autotuner (qsf_gb300/autotune.py) from step times measured on a GB300:
 //   python -m qsf_gb300.autotune --write
@@ -21,6 +22,19 @@ namespace qsf {
 
 __host__ __device__ constexpr int tuned_row_threads(int n) {
   return (n == 384 || n == 512) ? 512 : 256;
+}
+
+// Points per thread of the one-CTA 1D line kernel per line length (4: radix-4 plans,
+// 8: radix 8, 16: radix 16); a length between measured ones takes the plan of the next
+// longer measured length.  Measured (one call of graph-replayed steps, points per
+// thread: ms per step):
+//   1d1024  ms/step  4: 0.0392  8: 0.0416  16: 0.0452
+//   1d1536  ms/step  4: 0.0479  8: 0.0472  16: 0.0568
+//   1d2048  ms/step  4: 0.0537  8: 0.0522  16: 0.0543
+//   1d3072  ms/step  8: 0.0663  16: 0.0683
+//   1d4096  ms/step  8: 0.0733  16: 0.0711
+__host__ __device__ constexpr int tuned_line_ppt(int n) {
+  return n <= 1024 ? 4 : n <= 3072 ? 8 : 16;
 }
 
 }  // namespace qsf

@@ -32,6 +32,8 @@ WORKLOADS = {
     "1d1024": (1, 1024, 0.2, 102, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 400),
     "1d2048": (1, 2048, 0.2, 205, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 800),
     "1d8192": (1, 8192, 0.2, 819, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 1638),
+    "1d1536": (1, 1536, 0.2, 153, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 600),
+    "1d3072": (1, 3072, 0.2, 307, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 1200),
 }
 
 

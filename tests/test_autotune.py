@@ -36,3 +36,26 @@ def test_committed_table_is_the_autotuner_output():
     cond = re.search(r"return \((.*)\) \? 512 : 256;", txt).group(1)
     big = {int(v) for v in re.findall(r"n == (\d+)", cond)}
     assert big == {n for n, t in A.choose(times).items() if t == 512}
+
+
+def test_line_plans_choose_the_fastest_valid_plan_per_length():
+    lt = {("1d1024", 4): 0.030, ("1d1024", 8): 0.031, ("1d1024", 16): 0.039,
+          ("1d2048", 4): 0.055, ("1d2048", 8): 0.051, ("1d2048", 16): 0.053,
+          ("1d4096", 4): 0.010,  # a plan that does not fit (4 points x 512 threads < 4096): ignored
+          ("1d4096", 8): 0.073, ("1d4096", 16): 0.069}
+    ch = A.choose_lines(lt)
+    assert ch == {1024: 4, 2048: 8, 4096: 16}
+    assert not A.line_valid(4096, 4) and A.line_valid(4096, 8)
+    assert A.line_function({1024: 4, 2048: 8, 4096: 16}) == "n <= 1024 ? 4 : n <= 2048 ? 8 : 16"
+    assert A.line_function({1024: 16, 4096: 16}) == "16"
+
+
+def test_committed_line_plans_match_their_timings():
+    txt = open(os.path.join(ROOT, "qsf_gb300", "csrc", "qsf_tuning.h")).read()
+    lt = {}
+    for w, cells in re.findall(r"//\s+(1d\d+)\s+ms/step\s+(.*)", txt):
+        for p, ms in re.findall(r"(\d+): ([0-9.]+)", cells):
+            lt[(w, int(p))] = float(ms)
+    assert lt, "no line plan timings in the table"
+    expr = re.search(r"tuned_line_ppt\(int n\) \{\s*return (.*);", txt).group(1)
+    assert expr == A.line_function(A.choose_lines(lt))
