@@ -1,13 +1,16 @@
-"""Autotuner of the pass kernels: threads per block of the row / axis passes per line
-length, and the radix plan (points per thread) of the one-CTA 1D line kernel per length.
+"""Autotuner of the pass kernels: the shape of the row / axis passes per line length
+(points per block and threads per block), and the radix plan (points per thread) of the
+one-CTA 1D line kernel per length.
 
-The count sets the radix plan with it: 256 threads carry 16 points of a 4096-point tile
-each (radix-16 passes, 128 registers), 512 threads 8 points (radix-8 passes, 64
-registers, twice the resident warps).  For each candidate count the library is built
-with every line length forced to it (`QSF_ROW_THREADS`, in qsf_gb300/_build/tune_<T>/);
+A row / axis shape is a tile of whole lines (1024, 2048 or 4096 points per block, or
+one line when lines are longer) and a thread count; their ratio, the points each thread
+carries per pass, sets the radix plan (16: radix 16, 128 registers; 8: radix 8).
+Smaller tiles give small grids more blocks (a 256^2 grid is 16 blocks of 4096 points
+on 152 SMs).  For each candidate shape the library is built with every line length
+forced to it (`QSF_TILE`, `QSF_ROW_THREADS`, in qsf_gb300/_build/tune_<tile>_<threads>/);
 each tuning workload's fused step is timed as a user runs it (`profile_step --timed`:
 one call of K graph-replayed steps after a warm-up call) in a subprocess that loads that
-build; per line length the count with the least summed step time over the workloads of
+build; per line length the shape with the least summed step time over the workloads of
 that edge wins (the 2D grid and the 3D cube of one edge share their kernels).  With
 --write the choice goes to qsf_gb300/csrc/qsf_tuning.h, which the default build
 compiles in.  The 1D line kernel's plan is tuned the same way: candidate builds force 4,
@@ -29,12 +32,14 @@ import sys
 from . import build as B
 from .profile_step import WORKLOADS
 
-CANDIDATES = (256, 512)
+# (points per block, threads per block) of the row / axis passes
+CANDIDATES = ((4096, 256), (4096, 512), (2048, 128), (2048, 256), (1024, 128))
+DEFAULT_SHAPE = (4096, 256)
 LINE_CANDIDATES = (4, 8, 16)
 LINE_WORKLOADS = [("1d1024", 400), ("1d1536", 400), ("1d2048", 400), ("1d3072", 400), ("1d4096", 400)]
 # (workload of profile_step, steps per timed call)
-TUNE_WORKLOADS = [("2d256", 400), ("2d384", 400), ("2d512", 400), ("2d768", 300), ("2d1024", 300),
-                  ("2d2048", 100), ("2d4096", 30), ("3d128", 100), ("3d256", 30)]
+TUNE_WORKLOADS = [("2d256", 400), ("2d320", 400), ("2d384", 400), ("2d512", 400), ("2d640", 300), ("2d768", 300),
+                  ("2d1024", 300), ("2d2048", 100), ("2d4096", 30), ("3d128", 100), ("3d256", 30)]
 HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "qsf_tuning.h")
 
 
@@ -52,8 +57,8 @@ def time_workload(lib_path: str, workload: str, steps: int, repeat: int) -> floa
 
 
 def choose(times: dict) -> dict:
-    """times[(workload, T)] -> ms per step; returns edge -> chosen T (summed over the
-    workloads of each edge)."""
+    """times[(workload, shape)] -> ms per step; returns edge -> chosen shape (summed over
+    the workloads of each edge)."""
     edges = {}
     for (w, t), ms in times.items():
         edges.setdefault(WORKLOADS[w][1], {}).setdefault(t, 0.0)
@@ -86,35 +91,47 @@ def line_function(lchoice: dict) -> str:
     return expr
 
 
+def shape_function(choice: dict, k: int, default: int) -> str:
+    """An expression of n giving component k of the chosen shape (default elsewhere)."""
+    expr = str(default)
+    for n in sorted(choice, reverse=True):
+        v = choice[n][k]
+        if v != default:
+            expr = f"n == {n} ? {v} : {expr}"
+    return expr
+
+
 def header_text(choice: dict, times: dict, lchoice: dict = None, ltimes: dict = None) -> str:
     lchoice = lchoice if lchoice is not None else {1024: 4, 2048: 8, 4096: 16}
     rows = []
     for w, _ in TUNE_WORKLOADS:
-        cells = "  ".join(f"{t}: {times[(w, t)]:.4f}" for t in CANDIDATES if (w, t) in times)
-        rows.append(f"//   {w:7s} ms/step  {cells}")
+        cells = "  ".join(f"{c[0]}x{c[1]}: {times[(w, c)]:.4f}" for c in CANDIDATES if (w, c) in times)
+        if cells:
+            rows.append(f"//   {w:7s} ms/step  {cells}")
     lrows = []
     for w, _ in LINE_WORKLOADS:
         cells = "  ".join(f"{p}: {ltimes[(w, p)]:.4f}" for p in LINE_CANDIDATES if ltimes and (w, p) in ltimes)
         if cells:
             lrows.append(f"//   {w:7s} ms/step  {cells}")
-    big = sorted(n for n, t in choice.items() if t != 256)
-    cond = " || ".join(f"n == {n}" for n in big) or "false"
-    return f"""// qsf_tuning.h -- pass kernel shapes per line length: threads per block of the row /
-// axis passes, and the radix plan of the one-CTA 1D line kernel.
+    return f"""// qsf_tuning.h -- pass kernel shapes per line length: points and threads per block of
+// the row / axis passes, and the radix plan of the one-CTA 1D line kernel.
 //
 // Written by the autotuner (qsf_gb300/autotune.py) from step times measured on a GB300:
 //   python -m qsf_gb300.autotune --write
-// 256 threads carry 16 points of a 4096-point tile each (radix-16 plans, 128 registers),
-// 512 threads 8 points (radix-8 plans, 64 registers, twice the resident warps).  Line
-// lengths not listed take 256.  Measured (one call of graph-replayed steps per
-// workload, threads per block: ms per step):
+// Row / axis shapes: points per block x threads per block (16 points per thread:
+// radix-16 plans, 128 registers; 8: radix-8 plans); lengths not listed take
+// {DEFAULT_SHAPE[0]}x{DEFAULT_SHAPE[1]}.  Measured (one call of graph-replayed steps per workload, ms per step):
 {chr(10).join(rows)}
 #pragma once
 
 namespace qsf {{
 
 __host__ __device__ constexpr int tuned_row_threads(int n) {{
-  return ({cond}) ? 512 : 256;
+  return {shape_function(choice, 1, DEFAULT_SHAPE[1])};
+}}
+
+__host__ __device__ constexpr int tuned_tile(int n) {{
+  return {shape_function(choice, 0, DEFAULT_SHAPE[0])};
 }}
 
 // Points per thread of the one-CTA 1D line kernel per line length (4: radix-4 plans,
@@ -136,9 +153,9 @@ def committed_row_times() -> dict:
         return {}
     txt = open(HEADER).read()
     times = {}
-    for w, a, b in re.findall(r"//\s+(\S+)\s+ms/step\s+256: ([0-9.]+)\s+512: ([0-9.]+)", txt):
-        times[(w, 256)] = float(a)
-        times[(w, 512)] = float(b)
+    for w, cells in re.findall(r"//\s+([23]d\d+)\s+ms/step\s+(.*)", txt):
+        for tile, thr, ms in re.findall(r"(\d+)x(\d+): ([0-9.]+)", cells):
+            times[(w, (int(tile), int(thr)))] = float(ms)
     return times
 
 
@@ -150,11 +167,12 @@ def main():
     args = ap.parse_args()
     times, ltimes = {}, {}
     if args.only != "lines":
-        for t in CANDIDATES:
-            lib_path = B.build(defines=[f"QSF_ROW_THREADS={t}"], tag=f"tune_{t}")
+        for c in CANDIDATES:
+            lib_path = B.build(defines=[f"QSF_TILE={c[0]}", f"QSF_ROW_THREADS={c[1]}"], tag=f"tune_{c[0]}_{c[1]}")
             for w, steps in TUNE_WORKLOADS:
-                times[(w, t)] = time_workload(lib_path, w, steps, args.repeat)
-                print(json.dumps({"workload": w, "threads": t, "ms_per_step": times[(w, t)]}), flush=True)
+                times[(w, c)] = time_workload(lib_path, w, steps, args.repeat)
+                print(json.dumps({"workload": w, "tile": c[0], "threads": c[1], "ms_per_step": times[(w, c)]}),
+                      flush=True)
     if args.only != "rows":
         for p in LINE_CANDIDATES:
             lib_path = B.build(defines=[f"QSF_LINE_PPT={p}"], tag=f"tune_line{p}")
@@ -167,7 +185,7 @@ def main():
         times = committed_row_times()
     choice = choose(times)
     lchoice = choose_lines(ltimes) if ltimes else None
-    print(json.dumps({"choice": {str(n): t for n, t in sorted(choice.items())},
+    print(json.dumps({"choice": {str(n): list(t) for n, t in sorted(choice.items())},
                       "line_choice": {str(n): p for n, p in sorted((lchoice or {}).items())}}), flush=True)
     if args.write:
         with open(HEADER, "w") as f:

@@ -992,13 +992,13 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
   const int nlast = G.ax[D - 1].n;
   const long long nrows = G.m / nlast;
   if (D >= 2) {
-    g->row_L = (int)std::max<long long>(1, std::min<long long>(nrows, kMaxTile / nlast));
+    g->row_L = (int)std::max<long long>(1, std::min<long long>(nrows, tile_pts(nlast) / nlast));
     g->nrowblk = (int)((nrows + g->row_L - 1) / g->row_L);
     g->row_smem = (size_t)g->row_L * nlast * sizeof(double2);
     for (int ax = 0; ax < D - 1; ++ax) {
       const AxisDev& a = G.ax[ax];
       const long long inner = a.stride;
-      int C = (int)std::max<long long>(1, std::min<long long>({64, kMaxTile / a.n, inner}));
+      int C = (int)std::max<long long>(1, std::min<long long>({64, (long long)tile_pts(a.n) / a.n, inner}));
       g->ax_C[ax] = C;
       const long long outer = G.m / ((long long)a.n * inner);
       g->ax_blocks[ax] = (int)(outer * ((inner + C - 1) / C));

@@ -39,16 +39,24 @@
 namespace qsf {
 
 constexpr int kMaxDim = 3;
-// Threads per block of the row / axis passes (tiles of 4096 points): 512 threads with
-// radix-8 plans (8 points per thread, twice the resident warps) or 256 threads with
-// radix-16 plans, per line length as the autotuner measured (qsf_tuning.h).  The
-// autotuner's candidate builds define QSF_ROW_THREADS to force one count everywhere.
+// Shape of the row / axis pass kernels per line length, as the autotuner measured it
+// (qsf_tuning.h): points per block (a tile of whole lines, 1024-4096 points) and
+// threads per block, which together set the points per thread and with them the radix
+// plan (16 points: radix 16, 8: radix 8).  The autotuner's candidate builds define
+// QSF_TILE and QSF_ROW_THREADS to force one shape everywhere.
 #ifdef QSF_ROW_THREADS
 __host__ __device__ constexpr int row_threads(int) { return QSF_ROW_THREADS; }
 #else
 __host__ __device__ constexpr int row_threads(int n) { return tuned_row_threads(n); }
 #endif
-__host__ __device__ constexpr int row_ppt(int n) { return 4096 / row_threads(n); }
+#ifdef QSF_TILE
+__host__ __device__ constexpr int tile_size(int) { return QSF_TILE; }
+#else
+__host__ __device__ constexpr int tile_size(int n) { return tuned_tile(n); }
+#endif
+// points per block: the tile, or one whole line when lines are longer
+__host__ __device__ constexpr int tile_pts(int n) { return n > tile_size(n) ? n : tile_size(n); }
+__host__ __device__ constexpr int row_ppt(int n) { return tile_pts(n) / row_threads(n); }
 constexpr int kLinePptDiv = 512;  // threads of the one-CTA line kernel (kLineThreads)
 // Points per thread of the one-CTA line kernel (512 threads, one line of n points): a
 // line shorter than 8192 points leaves threads idle in radix-16 passes, and with one
@@ -77,6 +85,11 @@ constexpr int kMaxFluxBorders = 16;
 #ifndef QSF_FFT_MIN_BLOCKS
 #define QSF_FFT_MIN_BLOCKS 2
 #endif
+// resident blocks per SM the row / axis pass kernels are compiled for: twice as many
+// for blocks of 128 threads or fewer (the registers per thread stay the same)
+__host__ __device__ constexpr int row_min_blocks(int n) {
+  return row_threads(n) <= 128 ? 2 * QSF_FFT_MIN_BLOCKS : QSF_FFT_MIN_BLOCKS;
+}
 
 struct AxisDev {
   int n, n2;
@@ -417,7 +430,7 @@ struct TileWalk {
   }
 };
 
-__host__ __device__ constexpr int row_lines(int n) { return n >= 4096 ? 1 : 4096 / n; }
+__host__ __device__ constexpr int row_lines(int n) { return tile_pts(n) / n; }
 // rows of one TMA box of a strided-axis tile: the largest divisor of n up to 256 (the
 // box limit), so that the boxes cover the n rows exactly and none writes past the tile
 __host__ __device__ constexpr int tma_box_rows(int n) {
@@ -425,7 +438,7 @@ __host__ __device__ constexpr int tma_box_rows(int n) {
   while (n % b) --b;
   return b;
 }
-__host__ __device__ constexpr int tile_cols(int n) { return (4096 / n) < 64 ? (4096 / n) : 64; }
+__host__ __device__ constexpr int tile_cols(int n) { return (tile_pts(n) / n) < 64 ? (tile_pts(n) / n) : 64; }
 
 // Passes that leave the wavefunction in fixed point inside a step; each block of a
 // pass records its exponent in sc[pass][block] and the pass minimum in gmin[pass]:
@@ -1079,7 +1092,7 @@ __device__ __forceinline__ double ekin_rows(const AxisDev& a, longlong2* smx, co
 // Rows of the last axis: L rows of N points per block, contiguous in memory.
 // Open: psi (double) . [Normalize] . X half . forward FFT -> fixed point (pass 0).
 template <int N>
-__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_open(const GridDev* __restrict__ Gs,
+__global__ void __launch_bounds__(row_threads(N), row_min_blocks(N)) k_row_open(const GridDev* __restrict__ Gs,
                                                           const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -1195,7 +1208,7 @@ __device__ __forceinline__ void build_dtab(const StepDev& S, int in_pass, int* d
 // on into the next sub-step: its opening X half and the forward transform of the last
 // axis, leaving pass 0 of that sub-step in fixed point.
 template <int N>
-__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_row_close(const GridDev* __restrict__ Gs,
+__global__ void __launch_bounds__(row_threads(N), row_min_blocks(N)) k_row_close(const GridDev* __restrict__ Gs,
                                                            const StepDev* __restrict__ Ss, int L) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -1329,7 +1342,7 @@ __device__ __forceinline__ int p_phase(const GridDev& g, const StepDev& S, longl
 //   3 forward of psi_n (double) + E_kin partial
 // Inverse transforms run as forward ones on conjugated data.
 template <int MODE, int N>
-__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
+__global__ void __launch_bounds__(row_threads(N), row_min_blocks(N)) k_axis(const GridDev* __restrict__ Gs, const StepDev* __restrict__ Ss,
                                                       int ax, int C) {
   const GridDev& g = Gs[blockIdx.y];
   const StepDev& S = Ss[blockIdx.y];
@@ -1517,7 +1530,7 @@ __global__ void __launch_bounds__(kLineThreads, (QSF_FFT_MIN_BLOCKS + 1) / 2) k_
 }
 
 template <int N, bool FWD>
-__global__ void __launch_bounds__(row_threads(N), QSF_FFT_MIN_BLOCKS) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
+__global__ void __launch_bounds__(row_threads(N), row_min_blocks(N)) k_axis_fft(GridDev g, int ax, int C, double post_scale) {
   extern __shared__ __align__(128) longlong2 smx[];
   __shared__ int red[kRedInts];
   const AxisDev& a = g.ax[ax];

@@ -24,7 +24,9 @@ WORKLOADS = {
     "3d256": (3, 256, 0.4, 26, 3.0, 1, 1e15, 800.0, 2.0, "ZOA_FLUX_3D", 0),
     # further edges of the batched / served 2D mix and a smaller 3D cube
     "2d256": (2, 256, 0.3, 26, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
+    "2d320": (2, 320, 0.3, 32, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
     "2d384": (2, 384, 0.3, 38, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
+    "2d640": (2, 640, 0.3, 64, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
     "2d512": (2, 512, 0.3, 51, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
     "2d768": (2, 768, 0.3, 77, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
     "2d4096": (2, 4096, 0.3, 410, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),

@@ -10,32 +10,35 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_choice_sums_over_the_workloads_of_an_edge():
-    times = {("2d256", 256): 0.089, ("2d256", 512): 0.079, ("3d256", 256): 2.13, ("3d256", 512): 2.21,
-             ("2d2048", 256): 0.60, ("2d2048", 512): 0.51}
+    A4, A5, B2 = (4096, 256), (4096, 512), (2048, 256)
+    times = {("2d256", A4): 0.089, ("2d256", A5): 0.079, ("2d256", B2): 0.083,
+             ("3d256", A4): 2.13, ("3d256", A5): 2.21, ("3d256", B2): 2.40,
+             ("2d2048", A4): 0.60, ("2d2048", A5): 0.51, ("2d2048", B2): 0.70}
     ch = A.choose(times)
-    assert ch == {256: 256, 2048: 512}   # the cube outweighs the grid at 256
+    assert ch == {256: A4, 2048: A5}   # the cube outweighs the grid at 256
 
 
 def test_header_encodes_the_choice():
-    times = {(w, t): 1.0 for w, _ in A.TUNE_WORKLOADS for t in A.CANDIDATES}
-    txt = A.header_text({384: 512, 512: 512, 2048: 512, 256: 256}, times)
-    assert "return (n == 384 || n == 512 || n == 2048) ? 512 : 256;" in txt
-    assert "return (false) ? 512 : 256;" in A.header_text({256: 256}, times)
+    times = {(w, c): 1.0 for w, _ in A.TUNE_WORKLOADS for c in A.CANDIDATES}
+    txt = A.header_text({384: (4096, 512), 512: (2048, 256), 2048: (4096, 512), 256: (2048, 128),
+                         1024: (4096, 256)}, times)
+    assert "return n == 384 ? 512 : n == 2048 ? 512 : n == 256 ? 128 : 256;" not in txt  # ordered by n
+    assert "return n == 256 ? 128 : n == 384 ? 512 : n == 2048 ? 512 : 256;" in txt
+    assert "return n == 256 ? 2048 : n == 512 ? 2048 : 4096;" in txt
+    plain = A.header_text({256: A.DEFAULT_SHAPE}, times)
+    assert "tuned_row_threads(int n) {\n  return 256;" in plain and "tuned_tile(int n) {\n  return 4096;" in plain
 
 
 def test_committed_table_is_the_autotuner_output():
     txt = open(os.path.join(ROOT, "qsf_gb300", "csrc", "qsf_tuning.h")).read()
     assert "python -m qsf_gb300.autotune --write" in txt
-    rows = dict(re.findall(r"//\s+(\S+)\s+ms/step\s+256: ([0-9.]+)\s+512: [0-9.]+", txt))
-    assert set(rows) == {w for w, _ in A.TUNE_WORKLOADS}
-    times = {}
-    for line in re.findall(r"//\s+(\S+)\s+ms/step\s+256: ([0-9.]+)\s+512: ([0-9.]+)", txt):
-        w, a, b = line
-        times[(w, 256)] = float(a)
-        times[(w, 512)] = float(b)
-    cond = re.search(r"return \((.*)\) \? 512 : 256;", txt).group(1)
-    big = {int(v) for v in re.findall(r"n == (\d+)", cond)}
-    assert big == {n for n, t in A.choose(times).items() if t == 512}
+    times = A.committed_row_times()
+    assert times and {w for w, _ in times} <= {w for w, _ in A.TUNE_WORKLOADS}
+    ch = A.choose(times)
+    threads = re.search(r"tuned_row_threads\(int n\) \{\s*return (.*);", txt).group(1)
+    tile = re.search(r"tuned_tile\(int n\) \{\s*return (.*);", txt).group(1)
+    assert threads == A.shape_function(ch, 1, A.DEFAULT_SHAPE[1])
+    assert tile == A.shape_function(ch, 0, A.DEFAULT_SHAPE[0])
 
 
 def test_line_plans_choose_the_fastest_valid_plan_per_length():
