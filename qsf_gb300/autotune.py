@@ -159,6 +159,17 @@ def committed_row_times() -> dict:
     return times
 
 
+def committed_line_times() -> dict:
+    """The 1D line-plan timings of the committed table (kept when only the rows are tuned)."""
+    if not os.path.exists(HEADER):
+        return {}
+    lt = {}
+    for w, cells in re.findall(r"//\s+(1d\d+)\s+ms/step\s+(.*)", open(HEADER).read()):
+        for p, ms in re.findall(r"(\d+): ([0-9.]+)", cells):
+            lt[(w, int(p))] = float(ms)
+    return lt
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--repeat", type=int, default=2)
@@ -184,6 +195,8 @@ def main():
     if not times:
         times = committed_row_times()
     choice = choose(times)
+    if not ltimes:
+        ltimes = committed_line_times()
     lchoice = choose_lines(ltimes) if ltimes else None
     print(json.dumps({"choice": {str(n): list(t) for n, t in sorted(choice.items())},
                       "line_choice": {str(n): p for n, p in sorted((lchoice or {}).items())}}), flush=True)

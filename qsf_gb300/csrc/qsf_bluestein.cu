@@ -137,7 +137,8 @@ void row_pass(const KernelSet& K, const GridDev& S, bool fwd, double post, cudaS
 void axis_pass(const KernelSet& K, const GridDev& S, int ax, bool fwd, double post, cudaStream_t st) {
   const int n = S.ax[ax].n;
   const long long inner = S.ax[ax].stride;
-  const int C = (int)std::max<long long>(1, std::min<long long>({64, 4096 / n, inner}));
+  // the tile the kernels are compiled for (tile_pts(n) points: C columns of n)
+  const int C = (int)std::max<long long>(1, std::min<long long>({64, (long long)tile_pts(n) / n, inner}));
   const long long outer = S.m / ((long long)n * inner);
   const int blocks = (int)(outer * ((inner + C - 1) / C));
   const size_t smem = (size_t)n * C * sizeof(double2);

@@ -6,25 +6,27 @@
 // Row / axis shapes: points per block x threads per block (16 points per thread:
 // radix-16 plans, 128 registers; 8: radix-8 plans); lengths not listed take
 // 4096x256.  Measured (one call of graph-replayed steps per workload, ms per step):
-//   2d256   ms/step  4096x256: 0.0690  4096x512: 0.0684
-//   2d320   ms/step  4096x256: 0.0856  4096x512: 0.0793
-//   2d512   ms/step  4096x256: 0.0878  4096x512: 0.0719
-//   2d640   ms/step  4096x256: 0.1040  4096x512: 0.1200
-//   2d1024  ms/step  4096x256: 0.1072  4096x512: 0.1266
-//   2d2048  ms/step  4096x256: 0.4266  4096x512: 0.4351
-//   2d4096  ms/step  4096x256: 1.7265  4096x512: 1.9262
-//   3d128   ms/step  4096x256: 0.2970  4096x512: 0.3152
-//   3d256   ms/step  4096x256: 1.8341  4096x512: 1.9360
+//   2d256   ms/step  4096x256: 0.0693  4096x512: 0.0691  2048x128: 0.0577  2048x256: 0.0511  1024x128: 0.0449
+//   2d320   ms/step  4096x256: 0.0904  4096x512: 0.0744  2048x128: 0.0823  2048x256: 0.0552  1024x128: 0.0510
+//   2d384   ms/step  4096x256: 0.0860  4096x512: 0.0801  2048x128: 0.0777  2048x256: 0.0608  1024x128: 0.0522
+//   2d512   ms/step  4096x256: 0.0889  4096x512: 0.0725  2048x128: 0.0776  2048x256: 0.0513  1024x128: 0.0499
+//   2d640   ms/step  4096x256: 0.0921  4096x512: 0.0863  2048x128: 0.0869  2048x256: 0.0765  1024x128: 0.1035
+//   2d768   ms/step  4096x256: 0.1050  4096x512: 0.1213  2048x128: 0.0830  2048x256: 0.1095  1024x128: 0.1096
+//   2d1024  ms/step  4096x256: 0.1069  4096x512: 0.1276  2048x128: 0.1098  2048x256: 0.1376  1024x128: 0.1306
+//   2d2048  ms/step  4096x256: 0.4450  4096x512: 0.4330  2048x128: 0.4477  2048x256: 0.5127  1024x128: 0.4559
+//   2d4096  ms/step  4096x256: 1.6895  4096x512: 1.8929  2048x128: 2.6868  2048x256: 1.6912  1024x128: 2.7324
+//   3d128   ms/step  4096x256: 0.2978  4096x512: 0.3166  2048x128: 0.2872  2048x256: 0.3250  1024x128: 0.3178
+//   3d256   ms/step  4096x256: 1.8134  4096x512: 1.9213  2048x128: 1.8110  2048x256: 2.2277  1024x128: 2.2397
 #pragma once
 
 namespace qsf {
 
 __host__ __device__ constexpr int tuned_row_threads(int n) {
-  return n == 320 ? 512 : n == 512 ? 512 : 256;
+  return n == 128 ? 128 : n == 256 ? 128 : n == 320 ? 128 : n == 384 ? 128 : n == 512 ? 128 : n == 768 ? 128 : n == 2048 ? 512 : 256;
 }
 
 __host__ __device__ constexpr int tuned_tile(int n) {
-  return 4096;
+  return n == 128 ? 2048 : n == 256 ? 2048 : n == 320 ? 1024 : n == 384 ? 1024 : n == 512 ? 1024 : n == 640 ? 2048 : n == 768 ? 2048 : 4096;
 }
 
 // Points per thread of the one-CTA 1D line kernel per line length (4: radix-4 plans,
