@@ -32,8 +32,12 @@ import sys
 from . import build as B
 from .profile_step import WORKLOADS
 
-# (points per block, threads per block) of the row / axis passes
-CANDIDATES = ((4096, 256), (4096, 512), (2048, 128), (2048, 256), (1024, 128))
+# (points per block, threads per block) of the row / axis passes.  The committed table
+# comes from the 4096-point tiles: smaller tiles (--shapes all) make small grids faster
+# alone (2D 512^2 0.0725 -> 0.0499 ms per step with 1024 x 128) but the 256-solve batch
+# slower (1.25e10 -> 1.19e10 grid-pt-steps/s), where the solves already fill the GPU.
+CANDIDATES = ((4096, 256), (4096, 512))
+ALL_CANDIDATES = ((4096, 256), (4096, 512), (2048, 128), (2048, 256), (1024, 128))
 DEFAULT_SHAPE = (4096, 256)
 LINE_CANDIDATES = (4, 8, 16)
 LINE_WORKLOADS = [("1d1024", 400), ("1d1536", 400), ("1d2048", 400), ("1d3072", 400), ("1d4096", 400)]
@@ -105,7 +109,7 @@ def header_text(choice: dict, times: dict, lchoice: dict = None, ltimes: dict = 
     lchoice = lchoice if lchoice is not None else {1024: 4, 2048: 8, 4096: 16}
     rows = []
     for w, _ in TUNE_WORKLOADS:
-        cells = "  ".join(f"{c[0]}x{c[1]}: {times[(w, c)]:.4f}" for c in CANDIDATES if (w, c) in times)
+        cells = "  ".join(f"{c[0]}x{c[1]}: {times[(w, c)]:.4f}" for c in ALL_CANDIDATES if (w, c) in times)
         if cells:
             rows.append(f"//   {w:7s} ms/step  {cells}")
     lrows = []
@@ -120,7 +124,9 @@ def header_text(choice: dict, times: dict, lchoice: dict = None, ltimes: dict = 
 //   python -m qsf_gb300.autotune --write
 // Row / axis shapes: points per block x threads per block (16 points per thread:
 // radix-16 plans, 128 registers; 8: radix-8 plans); lengths not listed take
-// {DEFAULT_SHAPE[0]}x{DEFAULT_SHAPE[1]}.  Measured (one call of graph-replayed steps per workload, ms per step):
+// {DEFAULT_SHAPE[0]}x{DEFAULT_SHAPE[1]}.  Chosen among {", ".join(f"{c[0]}x{c[1]}" for c in CANDIDATES)}; smaller tiles, timed
+// beside them, speed up small grids run alone but slow the batched form down.
+// Measured (one call of graph-replayed steps per workload, ms per step):
 {chr(10).join(rows)}
 #pragma once
 
@@ -175,10 +181,13 @@ def main():
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--write", action="store_true", help="rewrite qsf_gb300/csrc/qsf_tuning.h")
     ap.add_argument("--only", choices=["rows", "lines"], default=None)
+    ap.add_argument("--shapes", choices=["tiles4096", "all"], default="tiles4096",
+                    help="row / axis candidates: 4096-point tiles (the committed table) or all shapes")
     args = ap.parse_args()
+    cands = CANDIDATES if args.shapes == "tiles4096" else ALL_CANDIDATES
     times, ltimes = {}, {}
     if args.only != "lines":
-        for c in CANDIDATES:
+        for c in cands:
             lib_path = B.build(defines=[f"QSF_TILE={c[0]}", f"QSF_ROW_THREADS={c[1]}"], tag=f"tune_{c[0]}_{c[1]}")
             for w, steps in TUNE_WORKLOADS:
                 times[(w, c)] = time_workload(lib_path, w, steps, args.repeat)
@@ -194,7 +203,7 @@ def main():
                 print(json.dumps({"workload": w, "points_per_thread": p, "ms_per_step": ltimes[(w, p)]}), flush=True)
     if not times:
         times = committed_row_times()
-    choice = choose(times)
+    choice = choose({k: v for k, v in times.items() if k[1] in cands})
     if not ltimes:
         ltimes = committed_line_times()
     lchoice = choose_lines(ltimes) if ltimes else None

@@ -5,7 +5,9 @@
 //   python -m qsf_gb300.autotune --write
 // Row / axis shapes: points per block x threads per block (16 points per thread:
 // radix-16 plans, 128 registers; 8: radix-8 plans); lengths not listed take
-// 4096x256.  Measured (one call of graph-replayed steps per workload, ms per step):
+// 4096x256.  Chosen among 4096x256, 4096x512; smaller tiles, timed
+// beside them, speed up small grids run alone but slow the batched form down.
+// Measured (one call of graph-replayed steps per workload, ms per step):
 //   2d256   ms/step  4096x256: 0.0693  4096x512: 0.0691  2048x128: 0.0577  2048x256: 0.0511  1024x128: 0.0449
 //   2d320   ms/step  4096x256: 0.0904  4096x512: 0.0744  2048x128: 0.0823  2048x256: 0.0552  1024x128: 0.0510
 //   2d384   ms/step  4096x256: 0.0860  4096x512: 0.0801  2048x128: 0.0777  2048x256: 0.0608  1024x128: 0.0522
@@ -22,11 +24,11 @@
 namespace qsf {
 
 __host__ __device__ constexpr int tuned_row_threads(int n) {
-  return n == 128 ? 128 : n == 256 ? 128 : n == 320 ? 128 : n == 384 ? 128 : n == 512 ? 128 : n == 768 ? 128 : n == 2048 ? 512 : 256;
+  return n == 320 ? 512 : n == 384 ? 512 : n == 512 ? 512 : n == 640 ? 512 : n == 2048 ? 512 : 256;
 }
 
 __host__ __device__ constexpr int tuned_tile(int n) {
-  return n == 128 ? 2048 : n == 256 ? 2048 : n == 320 ? 1024 : n == 384 ? 1024 : n == 512 ? 1024 : n == 640 ? 2048 : n == 768 ? 2048 : 4096;
+  return 4096;
 }
 
 // Points per thread of the one-CTA 1D line kernel per line length (4: radix-4 plans,

@@ -19,7 +19,7 @@ def test_choice_sums_over_the_workloads_of_an_edge():
 
 
 def test_header_encodes_the_choice():
-    times = {(w, c): 1.0 for w, _ in A.TUNE_WORKLOADS for c in A.CANDIDATES}
+    times = {(w, c): 1.0 for w, _ in A.TUNE_WORKLOADS for c in A.ALL_CANDIDATES}
     txt = A.header_text({384: (4096, 512), 512: (2048, 256), 2048: (4096, 512), 256: (2048, 128),
                          1024: (4096, 256)}, times)
     assert "return n == 384 ? 512 : n == 2048 ? 512 : n == 256 ? 128 : 256;" not in txt  # ordered by n
@@ -34,7 +34,7 @@ def test_committed_table_is_the_autotuner_output():
     assert "python -m qsf_gb300.autotune --write" in txt
     times = A.committed_row_times()
     assert times and {w for w, _ in times} <= {w for w, _ in A.TUNE_WORKLOADS}
-    ch = A.choose(times)
+    ch = A.choose({k: v for k, v in times.items() if k[1] in A.CANDIDATES})
     threads = re.search(r"tuned_row_threads\(int n\) \{\s*return (.*);", txt).group(1)
     tile = re.search(r"tuned_tile\(int n\) \{\s*return (.*);", txt).group(1)
     assert threads == A.shape_function(ch, 1, A.DEFAULT_SHAPE[1])
