@@ -35,6 +35,9 @@ WORKLOADS = {
     "1d2048": (1, 2048, 0.2, 205, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 800),
     "1d8192": (1, 8192, 0.2, 819, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 1638),
     "1d1536": (1, 1536, 0.2, 153, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 600),
+    # lengths outside the built list: Bluestein transforms, member-operation programs
+    "1d4099": (1, 4099, 0.2, 410, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 1638),
+    "2d1000": (2, 1000, 0.3, 100, 2.0, 0, 5e14, 800.0, 3.0, "ZOA_FLUX_2D", 0),
     "1d3072": (1, 3072, 0.2, 307, 1.0, 1, 1e14, 800.0, 2.0, ["BOX"], 1200),
 }
 
