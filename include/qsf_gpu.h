@@ -333,6 +333,8 @@ typedef struct qsf_server_stats {
 } qsf_server_stats;
 
 typedef struct qsf_server qsf_server;
+/* The server's worker thread runs on the calling thread's current device at start
+ * (one process per GPU selects its device first). */
 int qsf_server_start(const qsf_server_config* cfg, qsf_server** out);
 int qsf_server_submit(qsf_server* s, const qsf_request* r, int64_t* ticket);
 /* Admission: a request is admitted while a slot is free and its device bytes fit in

@@ -1514,10 +1514,8 @@ int qsf::grid_clear(qsf_grid* g) {
 
 // the launch-shape key of a step program: what its captured kernels bake in
 static std::vector<long long> generic_key(const qsf_grid* g, const qsf_step_desc* d) {
-  long long dtb, bits[2];
+  long long dtb;
   std::memcpy(&dtb, &d->dt, sizeof(dtb));
-  std::memcpy(&bits[0], &d->state_accuracy, sizeof(double));
-  bits[1] = 0;
   return {d->mode, dtb, std::max(1, d->substeps), (long long)d->obs, generic_ncol(d), d->normalize,
           d->coupling != nullptr, (long long)(uintptr_t)g->rows_dev, (long long)(uintptr_t)g->coup_dev,
           (long long)(uintptr_t)g->snap, (long long)(uintptr_t)g->fpts, (long long)(uintptr_t)g->fterms, g->nfterms,

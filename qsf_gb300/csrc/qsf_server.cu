@@ -102,6 +102,7 @@ size_t solve_bytes(const qsf_request& r) {
 
 struct qsf_server {
   qsf_server_config cfg{};
+  int device = 0;  // the caller's current device at qsf_server_start; the worker thread selects it
 #ifdef QSF_SERVER_TRACE
   // decide, admit, enqueue, batch, wait, retire, rounds, admits, batch launch (rebuilds)
   // admits of member-operation / batched solves (incl. their first queued steps)
@@ -284,6 +285,9 @@ int admit(qsf_server* s, Pending& p, Running& r, bool nowait) {
 }
 
 void worker_loop(qsf_server* s) {
+  // a new host thread starts on device 0: select the device the server was started on
+  // (one process per GPU selects its own before qsf_server_start)
+  cudaSetDevice(s->device);
   std::vector<double> rows;
   for (;;) {
     // admission
@@ -465,6 +469,10 @@ int qsf_server_start(const qsf_server_config* cfg, qsf_server** out) {
     return QSF_EINVAL;
   qsf_server* s = new qsf_server();
   s->cfg = *cfg;
+  if (cudaGetDevice(&s->device) != cudaSuccess) {
+    delete s;
+    return QSF_ECUDA;
+  }
   int rc = qsf_batch_create(nullptr, &s->batch);
   if (rc) {
     delete s;
