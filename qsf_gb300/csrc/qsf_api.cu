@@ -7,6 +7,7 @@
 // counter makes reusable for every step of a call.
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -30,13 +31,16 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 int device_sm_count() {
-  static int cache[64] = {0};
+  static std::atomic<int> cache[64];  // zero-initialised (static storage); read by any host thread
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 152;
-  if (dev < 64 && cache[dev] > 0) return cache[dev];
+  if (dev < 64) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
   int n = 0;
   if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
-  if (dev < 64) cache[dev] = n;
+  if (dev < 64) cache[dev].store(n, std::memory_order_relaxed);
   return n;
 }
 }  // namespace qsf
@@ -90,6 +94,7 @@ int init_kernel_table() {
   std::lock_guard<std::mutex> lk(mu);
   if (done) return QSF_OK;
   std::vector<KernelSet>& t = kernel_table();
+  t.clear();  // a failed earlier attempt starts over
   add_sizes_p2a(t);
   add_sizes_p2b(t);
   add_sizes_r3(t);
