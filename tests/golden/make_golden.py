@@ -38,6 +38,17 @@ CASES = {
     "c3_lg": ("c3", dict(n=16, dx=0.4, nCAP=2, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=20,
                          re_dt=0.05, F0=0.1688, omega=1.5, ncycles=1, phase=0.0, p_NS=4, p_SD=3, p_DT=2, p_CAP=6,
                          lg=1), 6, 13, 3),
+    # the same runs at axis lengths with a prime factor above 5 (514 = 2 * 257,
+    # 46 = 2 * 23, 14 = 2 * 7): the reference's FFTW plans take any n, the GPU path
+    # transforms them by Bluestein's convolution
+    "c1_bs": ("c1", dict(n=514, dx=0.2, nCAP=51, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=100,
+                         re_dt=0.05, F0=0.05338, omega=0.5, ncycles=2, phase=0.25, box=100, lg=1), 6, 6, 1),
+    "c2_bs": ("c2", dict(n=46, dx=0.3, nCAP=5, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=40,
+                         re_dt=0.05, F0=0.11936, omega=1.0, ncycles=2, phase=0.0, p_NS=6, p_SD=4, p_DT=3, p_CAP=15,
+                         lg=0), 6, 12, 2),
+    "c3_bs": ("c3", dict(n=14, dx=0.4, nCAP=2, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, im_dt=0.01, im_steps=20,
+                         re_dt=0.05, F0=0.1688, omega=1.5, ncycles=1, phase=0.0, p_NS=4, p_SD=3, p_DT=2, p_CAP=6,
+                         lg=1), 6, 13, 3),
     # .psi files written by the reference's own save / backup / snapshot, and the
     # wavefunctions its load / orthogonalizeWith produce (grid.h:789-1153)
     # MultiProductSplit<Split3Base, K> real-time runs, K = 2, 3, both gauges

@@ -67,7 +67,9 @@ def _assert_columns(got, ref):
         np.testing.assert_allclose(got[:, c], ref[:, c], rtol=OBS_TOL, atol=1e-12 * scale, err_msg=f"column {c}")
 
 
-@pytest.mark.parametrize("name", ["c1_vg", "c1_lg", "c2_vg", "c3_lg"])
+# *_bs: axis lengths with a prime factor above 5 (514, 46, 14), whose transforms run
+# as Bluestein convolutions and whose steps run as member-operation programs
+@pytest.mark.parametrize("name", ["c1_vg", "c1_lg", "c2_vg", "c3_lg", "c1_bs", "c2_bs", "c3_bs"])
 def test_full_runs(Q, name):
     z = C.load(name)
     p, dim = z["params"], int(z["dim"])
