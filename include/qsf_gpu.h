@@ -129,11 +129,13 @@ typedef struct qsf_grid qsf_grid;
  * `stream` is a cudaStream_t or NULL (the handle then creates its own stream).
  * Axis lengths: any n >= 2 (the reference's FFTW plans take any n, grid.h:251-274) up
  * to 16384 on a 1D line and 4096 on the axes of a 2D / 3D grid.  The lengths of the
- * built kernel list (2^a 3^b 5^c from 8 to 16384) take the fused kernels; the others
- * (up to 8192 in 1D, 2048 in 2D / 3D) transform each axis by Bluestein's chirp-z
- * convolution over a built length M >= 2n - 1, and qsf_step runs their steps as the
- * member operations evolve / fourier / average; batches and the server take built
- * lengths only (QSF_EINVAL).  Other lengths: QSF_EINVAL. */
+ * built kernel list (2^a, 3*2^a and 5*2^a from 8 to 16384: 33 lengths) take the fused
+ * kernels; the others (up to 16384 in 1D, 2048 in 2D / 3D) transform each axis by
+ * Bluestein's chirp-z convolution over a built length M >= 2n - 1 (a four-step
+ * M1 x M2 transform for 1D lines above 8192 points), and qsf_step runs their steps as
+ * the member operations evolve / fourier / average; batches take built lengths only
+ * (QSF_EINVAL), the server runs the others beside its batch.  Other lengths:
+ * QSF_EINVAL. */
 int qsf_grid_create(const qsf_grid_desc* desc, void* stream, qsf_grid** out);
 int qsf_grid_destroy(qsf_grid* g);
 /* number of grid points m and the device address of psi (complex128[m]) */

@@ -1,8 +1,8 @@
 // qsf_bluestein.cu -- fourier<R>() for axis lengths outside the built kernel list.
 //
 // The reference's FFTW plans take any n (wf/grid.h:251-274); the fused step kernels of
-// this library are compiled for a list of lengths 2^a 3^b 5^c (8 ... 16384, the
-// add_sizes_* tables).  For any other n one axis of the transform runs as Bluestein's
+// this library are compiled for a list of lengths 2^a, 3*2^a and 5*2^a (8 ... 16384,
+// the add_sizes_* tables).  For any other n one axis of the transform runs as Bluestein's
 // chirp-z convolution: with c[j] = exp(-i pi j^2 / n),
 //     X[k] = c[k] * sum_j (x[j] c[j]) conj(c[k - j]),
 // a linear convolution evaluated as a cyclic one of length M >= 2n - 1 (a length with

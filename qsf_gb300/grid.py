@@ -38,7 +38,8 @@ def _dp(a: np.ndarray):
 class Grid:
     """One wavefunction on the GPU (qsf_grid_create).  Axis lengths: any n >= 2 up to
     16384 on a 1D line and 4096 per axis in 2D / 3D; lengths of the built kernel list
-    (2^a 3^b 5^c) take the fused step kernels, the others (up to 2048 per axis in 2D / 3D)
+    (2^a, 3*2^a and 5*2^a from 8 to 16384) take the fused step kernels, the others (up to
+    16384 in 1D, 2048 per axis in 2D / 3D)
     Bluestein transforms and graph-replayed member-operation step programs."""
 
     def __init__(self, dim: int, n, dx, nCAP: int = 0, potential: int = POT_EBERLY, Ncharge: float = 1.0,

@@ -1,7 +1,7 @@
 """Axis lengths with a prime factor above 5 (Bluestein transforms, member-operation steps).
 
 The reference transforms any n through FFTW (wf/grid.h:251-274); the fused kernels of
-this library are built for 2^a 3^b 5^c.  Other lengths take one chirp-z convolution per
+this library are built for 2^a, 3*2^a and 5*2^a (8 ... 16384).  Other lengths take one chirp-z convolution per
 axis through the built M-point transforms (M >= 2n - 1) and qsf_step runs the reference's
 own member sequence evolve<X>(dt/2), fourier<P>, evolve<P>(dt), fourier<X>,
 evolve<X>(dt/2) (propagator.h:311-346).  Checked here: transforms against numpy's FFT
