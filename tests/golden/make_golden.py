@@ -65,6 +65,16 @@ CASES = {
                         ncycles=1, re_dt=0.05), 0, 5, 2),
     "mg3": ("mg3", dict(n=8, dx=0.5, nCAP=3, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, seed=9, F0=0.12, omega=1.5,
                         ncycles=1, re_dt=0.05), 0, 5, 3),
+    # multi-region grids and multi-product chains at lengths with a prime factor above 5
+    # (130 = 2 * 5 * 13, 34 = 2 * 17, 14 = 2 * 7, 258 = 2 * 3 * 43)
+    "mg1_bs": ("mg1", dict(n=130, dx=0.3, nCAP=16, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, seed=3, F0=0.1,
+                           omega=1.0, ncycles=1, re_dt=0.05), 0, 5, 1),
+    "mg2_bs": ("mg2", dict(n=34, dx=0.4, nCAP=4, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, seed=5, F0=0.1,
+                           omega=1.0, ncycles=1, re_dt=0.05), 0, 5, 2),
+    "mg3_bs": ("mg3", dict(n=14, dx=0.5, nCAP=3, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, seed=9, F0=0.12,
+                           omega=1.5, ncycles=1, re_dt=0.05), 0, 5, 3),
+    "mp_bs": ("mp", dict(n=258, dx=0.2, nCAP=25, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, re_dt=0.05, F0=0.05,
+                         omega=0.5, ncycles=1, phase=0.0), 0, 4, 1),
     "io1": ("io1", dict(n=16, dx=0.3, nCAP=2, seed=3), 0, 0, 1),
     "io2": ("io2", dict(n=8, dx=0.5, nCAP=1, seed=5), 0, 0, 2),
     "io3": ("io3", dict(n=8, dx=0.4, nCAP=1, seed=9), 0, 0, 3),

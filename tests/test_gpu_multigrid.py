@@ -38,7 +38,8 @@ def _gpu_run(p, dim, psi0):
     return psis, rows
 
 
-@pytest.mark.parametrize("name", ["mg1", "mg2", "mg3"])
+# *_bs: axis lengths with a prime factor above 5 (130, 34, 14): Bluestein transforms
+@pytest.mark.parametrize("name", ["mg1", "mg2", "mg3", "mg1_bs", "mg2_bs", "mg3_bs"])
 def test_multigrid_matches_reference(name):
     z = C.load(name)
     p, dim = z["params"], int(z["dim"])

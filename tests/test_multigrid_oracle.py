@@ -20,7 +20,8 @@ def test_region_order_and_sources():
     assert src3[4] == [(1, 1), (2, 0)]          # XY from X (via Y), Y (via X)
 
 
-@pytest.mark.parametrize("name", ["mg1", "mg2", "mg3"])
+# *_bs: axis lengths with a prime factor above 5 (130, 34, 14)
+@pytest.mark.parametrize("name", ["mg1", "mg2", "mg3", "mg1_bs", "mg2_bs", "mg3_bs"])
 def test_multigrid_matches_reference(name):
     z = C.load(name)
     p, dim = z["params"], int(z["dim"])

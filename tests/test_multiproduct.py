@@ -1,7 +1,7 @@
 """MultiProductSplit<Split3Base<X,P,X>, K> (splitting.h:63-91, propagator.h:331-413).
 
-The fixture tests/golden/mp.npz holds real-time 1D runs of the reference's own
-propagator with K = 2 and 3 in both gauges.  The oracle restates the chains literally
+The fixtures tests/golden/mp.npz and mp_bs.npz hold real-time 1D runs of the reference's
+own propagator with K = 2 and 3 in both gauges.  The oracle restates the chains literally
 (including the completion test `chain == ChainCount - 1`, which leaves a step's result
 equal to its last chain); the GPU path runs that last chain as K fused sub-steps."""
 import numpy as np
@@ -11,6 +11,8 @@ from oracle import oracle as O
 from tests import cases as C
 
 TAGS = [("MP2VG", 2, 0), ("MP3VG", 3, 0), ("MP2LG", 2, 1), ("MP3LG", 3, 1)]
+# mp: 256 points; mp_bs: 258 = 2 * 3 * 43 (Bluestein transforms on the GPU)
+FIXTURES = ["mp", "mp_bs"]
 MP_OUTPUTS = ["step", "time", "norm", "epot"]
 
 
@@ -18,9 +20,10 @@ def _rows(rows):
     return np.array([[r["step"], r["time"], r["norm"], r["epot"]] for r in rows])
 
 
+@pytest.mark.parametrize("name", FIXTURES)
 @pytest.mark.parametrize("tag,K,lg", TAGS)
-def test_oracle_chains_match_reference(tag, K, lg):
-    z = C.load("mp")
+def test_oracle_chains_match_reference(tag, K, lg, name):
+    z = C.load(name)
     p = z["params"]
     gauge = O.GAUGE_LENGTH if lg else O.GAUGE_VELOCITY
     c = O.Coupling(gauge, [O.Field(1, [C.pulse(p)])])
@@ -40,10 +43,11 @@ def test_chain_coefficients():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", FIXTURES)
 @pytest.mark.parametrize("tag,K,lg", TAGS)
-def test_gpu_multiproduct_matches_reference(tag, K, lg):
+def test_gpu_multiproduct_matches_reference(tag, K, lg, name):
     import qsf_gb300 as Q
-    z = C.load("mp")
+    z = C.load(name)
     p = z["params"]
     gauge = Q.GAUGE_LENGTH if lg else Q.GAUGE_VELOCITY
     c = Q.Coupling(gauge, [Q.Field(1, [C.gpu_pulse(p)])])
