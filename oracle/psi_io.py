@@ -175,7 +175,13 @@ def orthogonalize_with(path: str, psi: np.ndarray, dx, offset=None) -> Tuple[np.
     for a, b in zip(tmp.reshape(-1), psi.reshape(-1)):
         sp += a.conjugate() * b
     sp *= dV
-    out = psi - sp * tmp
+    # psi[i] -= sp * tmp[i] (grid.h:939), the complex product as separate real
+    # multiplies and adds: numpy's vector loops for complex products may fuse them into
+    # multiply-adds, which the reference's compiled code does not (-ffp-contract=off)
+    prod = np.empty_like(tmp)
+    prod.real = sp.real * tmp.real - sp.imag * tmp.imag
+    prod.imag = sp.real * tmp.imag + sp.imag * tmp.real
+    out = psi - prod
     nrm = float(np.sum(out.real * out.real + out.imag * out.imag)) * dV
     return out, sp, nrm
 

@@ -75,6 +75,14 @@ CASES = {
                            omega=1.5, ncycles=1, re_dt=0.05), 0, 5, 3),
     "mp_bs": ("mp", dict(n=258, dx=0.2, nCAP=25, Ncharge=1, Echarge=-1, Nsoft=1, Esoft=1, re_dt=0.05, F0=0.05,
                          omega=0.5, ncycles=1, phase=0.0), 0, 4, 1),
+    # primitives and .psi files at lengths with a prime factor above 5 (22 = 2 * 11, 14)
+    "prim2d_bs": ("prim2d", dict(n=22, dx=0.4, nCAP=3, Ncharge=2, Echarge=-1, Nsoft=1, Esoft=1, p_NS=4, p_SD=3,
+                                 p_DT=2, p_CAP=6, seed=7, delta=0.37, F0=0.11), 0, 0, 2),
+    "prim3d_bs": ("prim3d", dict(n=14, dx=0.5, nCAP=2, Ncharge=3, Echarge=-1, Nsoft=1, Esoft=1, p_NS=4, p_SD=3,
+                                 p_DT=2, p_CAP=5, seed=11, delta=0.29, F0=0.07), 0, 0, 3),
+    "io1_bs": ("io1", dict(n=22, dx=0.3, nCAP=2, seed=3), 0, 0, 1),
+    "io2_bs": ("io2", dict(n=14, dx=0.5, nCAP=1, seed=5), 0, 0, 2),
+    "io3_bs": ("io3", dict(n=14, dx=0.4, nCAP=1, seed=9), 0, 0, 3),
     "io1": ("io1", dict(n=16, dx=0.3, nCAP=2, seed=3), 0, 0, 1),
     "io2": ("io2", dict(n=8, dx=0.5, nCAP=1, seed=5), 0, 0, 2),
     "io3": ("io3", dict(n=8, dx=0.4, nCAP=1, seed=9), 0, 0, 3),

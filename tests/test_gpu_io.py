@@ -14,8 +14,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 pytestmark = pytest.mark.gpu
 
 
-def _golden(dim):
-    z = np.load(os.path.join(HERE, "golden", f"io{dim}.npz"))
+# (fixture, dim): io1..3 at 16, 8^2, 8^3 points; *_bs at 22, 14^2, 14^3 (lengths outside
+# the built list: Bluestein transforms in the P-representation saves)
+IO_CASES = [("io1", 1), ("io2", 2), ("io3", 3), ("io1_bs", 1), ("io2_bs", 2), ("io3_bs", 3)]
+
+
+def _golden(dim, name=None):
+    z = np.load(os.path.join(HERE, "golden", f"{name or 'io%d' % dim}.npz"))
     p = json.loads(str(z["params"]))
     return z, p
 
@@ -33,11 +38,11 @@ def _payload(raw: bytes, dim: int):
     return raw[:h["offset"]], np.frombuffer(raw[h["offset"]:], dtype=dt)
 
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
-def test_save_matches_reference_files(dim, tmp_path, monkeypatch):
+@pytest.mark.parametrize("name,dim", IO_CASES)
+def test_save_matches_reference_files(name, dim, tmp_path, monkeypatch):
     import qsf_gb300 as Q
     monkeypatch.chdir(tmp_path)
-    z, p = _golden(dim)
+    z, p = _golden(dim, name)
     g = _grid(dim, p, z["psi_in"])
     # X representation: the same bytes as the reference
     for kw, fname in ((dict(), "sx_repX.psi"), (dict(downscale=2), "sd_scale2_repX.psi"),
@@ -61,10 +66,10 @@ def test_save_matches_reference_files(dim, tmp_path, monkeypatch):
     g.close()
 
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
-def test_load_backup_restore(dim, tmp_path, monkeypatch):
+@pytest.mark.parametrize("name,dim", IO_CASES)
+def test_load_backup_restore(name, dim, tmp_path, monkeypatch):
     monkeypatch.chdir(tmp_path)
-    z, p = _golden(dim)
+    z, p = _golden(dim, name)
     for fname in ("sx_repX.psi", "sn_repX.psi"):
         (tmp_path / fname).write_bytes(z["file:" + fname].tobytes())
     g = _grid(dim, p, z["psi_b"])
@@ -92,10 +97,10 @@ def test_load_backup_restore(dim, tmp_path, monkeypatch):
     g.close()
 
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
-def test_orthogonalize_matches_oracle(dim, tmp_path, monkeypatch):
+@pytest.mark.parametrize("name,dim", IO_CASES)
+def test_orthogonalize_matches_oracle(name, dim, tmp_path, monkeypatch):
     monkeypatch.chdir(tmp_path)
-    z, p = _golden(dim)
+    z, p = _golden(dim, name)
     dx = [float(p["dx"])] * dim
     dV = float(np.prod(dx))
     f = z["psi_in"] / np.sqrt(np.sum(np.abs(z["psi_in"]) ** 2) * dV)

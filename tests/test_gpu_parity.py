@@ -24,7 +24,8 @@ def Q():
     return qsf_gb300
 
 
-@pytest.mark.parametrize("name", ["prim2d", "prim3d"])
+# *_bs: 22^2 and 14^3, lengths with a prime factor above 5 (Bluestein transforms)
+@pytest.mark.parametrize("name", ["prim2d", "prim3d", "prim2d_bs", "prim3d_bs"])
 def test_primitives(Q, name):
     z = C.load(name)
     p, dim = z["params"], int(z["dim"])

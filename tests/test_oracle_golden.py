@@ -18,7 +18,7 @@ def _prim_grid(p, dim, gauge):
     return C.oracle_grid(p, dim, c)
 
 
-@pytest.mark.parametrize("name", ["prim2d", "prim3d"])
+@pytest.mark.parametrize("name", ["prim2d", "prim3d", "prim2d_bs", "prim3d_bs"])
 def test_primitives_match_reference(name):
     z = C.load(name)
     p, dim = z["params"], int(z["dim"])

@@ -13,8 +13,13 @@ from oracle import psi_io as IO
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def _golden(dim):
-    z = np.load(os.path.join(HERE, "golden", f"io{dim}.npz"))
+# (fixture, dim): io1..3 at 16, 8^2, 8^3 points; *_bs at 22, 14^2, 14^3 (lengths outside
+# the GPU library's built list)
+IO_CASES = [("io1", 1), ("io2", 2), ("io3", 3), ("io1_bs", 1), ("io2_bs", 2), ("io3_bs", 3)]
+
+
+def _golden(dim, name=None):
+    z = np.load(os.path.join(HERE, "golden", f"{name or 'io%d' % dim}.npz"))
     p = json.loads(str(z["params"]))
     return z, [float(p["dx"])] * dim
 
@@ -32,18 +37,18 @@ SAVES = [  # (base, kwargs, file the reference wrote)
 ]
 
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
+@pytest.mark.parametrize("name,dim", IO_CASES)
 @pytest.mark.parametrize("base,kw,fname", SAVES)
-def test_save_bytes_equal_reference(dim, base, kw, fname, tmp_path):
-    z, dx = _golden(dim)
+def test_save_bytes_equal_reference(name, dim, base, kw, fname, tmp_path):
+    z, dx = _golden(dim, name)
     path = IO.save(z["psi_in"], dx, base, directory=str(tmp_path), **kw)
     assert os.path.basename(path) == fname
     assert open(path, "rb").read() == _ref_file(z, fname)
 
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
-def test_backup_and_snapshot_bytes(dim, tmp_path):
-    z, dx = _golden(dim)
+@pytest.mark.parametrize("name,dim", IO_CASES)
+def test_backup_and_snapshot_bytes(name, dim, tmp_path):
+    z, dx = _golden(dim, name)
     IO.backup(z["psi_in"], dx, 7, directory=str(tmp_path))
     assert open(tmp_path / "backup.psi", "rb").read() == _ref_file(z, "backup.psi")
     assert open(tmp_path / "backup.info", "rb").read() == _ref_file(z, "backup.info")
@@ -53,9 +58,9 @@ def test_backup_and_snapshot_bytes(dim, tmp_path):
     assert step == 7 and np.array_equal(psi, z["psi_in"])
 
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
-def test_load_equals_reference(dim, tmp_path):
-    z, dx = _golden(dim)
+@pytest.mark.parametrize("name,dim", IO_CASES)
+def test_load_equals_reference(name, dim, tmp_path):
+    z, dx = _golden(dim, name)
     for fname, key in (("sx_repX.psi", "psi_load_sx"), ("sn_repX.psi", "psi_load_sn")):
         (tmp_path / fname).write_bytes(_ref_file(z, fname))
         psi, h = IO.load(str(tmp_path / fname), z["psi_b"])
@@ -63,11 +68,11 @@ def test_load_equals_reference(dim, tmp_path):
         assert np.array_equal(psi, z[key]), fname
 
 
-@pytest.mark.parametrize("dim", [1, 2])
-def test_orthogonalize_reproduces_reference_offset(dim, tmp_path):
+@pytest.mark.parametrize("name,dim", [c for c in IO_CASES if c[1] < 3])
+def test_orthogonalize_reproduces_reference_offset(name, dim, tmp_path):
     """The reference reads the payload 3 bytes early; where its result is finite the
     restatement with the same offset gives the same values."""
-    z, dx = _golden(dim)
+    z, dx = _golden(dim, name)
     (tmp_path / "sx_repX.psi").write_bytes(_ref_file(z, "sx_repX.psi"))
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
@@ -77,10 +82,10 @@ def test_orthogonalize_reproduces_reference_offset(dim, tmp_path):
     assert fin.any() and np.array_equal(out[fin], ref[fin])
 
 
-@pytest.mark.parametrize("dim", [1, 2, 3])
-def test_orthogonalize_at_payload_projects_out(dim, tmp_path):
+@pytest.mark.parametrize("name,dim", IO_CASES)
+def test_orthogonalize_at_payload_projects_out(name, dim, tmp_path):
     """psi -= <f|psi> dV f removes f from psi when f is normalised (<f|f> dV = 1)."""
-    z, dx = _golden(dim)
+    z, dx = _golden(dim, name)
     dV = float(np.prod(dx))
     f = z["psi_in"] / np.sqrt(np.sum(np.abs(z["psi_in"]) ** 2) * dV)
     path = IO.save(f, dx, "s", directory=str(tmp_path))
