@@ -137,6 +137,7 @@ typedef struct qsf_grid qsf_grid;
  * (QSF_EINVAL), the server runs the others beside its batch.  Other lengths:
  * QSF_EINVAL. */
 int qsf_grid_create(const qsf_grid_desc* desc, void* stream, qsf_grid** out);
+/* Frees the grid's device state; a member of a batch leaves the batch first. */
 int qsf_grid_destroy(qsf_grid* g);
 /* number of grid points m and the device address of psi (complex128[m]) */
 int qsf_grid_size(const qsf_grid* g, int64_t* m);
@@ -274,9 +275,12 @@ int qsf_step(qsf_grid* g, const qsf_step_desc* d, double* rows, int64_t* steps_d
  * counterpart in the reference, which runs one solve per process group. */
 typedef struct qsf_batch qsf_batch;
 int qsf_batch_create(void* stream, qsf_batch** out);
+/* Destroying a batch leaves its member grids alive and out of any batch. */
 int qsf_batch_destroy(qsf_batch* b);
-/* Adds grid g (owned by the caller; it must stay alive while in the batch) with the
- * step program d (coupling rows are copied at this call).  d->kernel_ms is ignored. */
+/* Adds grid g (owned by the caller) with the step program d (coupling rows are copied
+ * at this call).  d->kernel_ms is ignored.  A grid is in at most one batch
+ * (QSF_ESTATE otherwise); qsf_grid_destroy of a member removes it from its batch
+ * first, so a later qsf_batch_run does not touch its memory. */
 int qsf_batch_add(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int64_t* slot);
 /* Removes a member; applies its pending Normalize factor first. */
 int qsf_batch_remove(qsf_batch* b, int64_t slot);

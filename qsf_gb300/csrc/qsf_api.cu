@@ -1051,6 +1051,7 @@ int qsf_grid_create(const qsf_grid_desc* d, void* stream, qsf_grid** out) {
 
 int qsf_grid_destroy(qsf_grid* g) {
   if (!g) return QSF_OK;
+  if (g->batch) qsf_batch_remove(g->batch, g->batch_slot);  // out of the batch's graph first
   if (g->stream) cudaStreamSynchronize(g->stream);
   auto fr = [](void* p) {
     if (p) cudaFree(p);
@@ -1732,6 +1733,10 @@ int qsf_batch_create(void* stream, qsf_batch** out) {
 int qsf_batch_destroy(qsf_batch* b) {
   if (!b) return QSF_OK;
   cudaStreamSynchronize(b->stream);
+  for (auto& kv : b->members) {  // the grids outlive the batch
+    kv.second.g->batch = nullptr;
+    kv.second.g->batch_slot = -1;
+  }
   free_groups(b);
   if (b->dG_all) cudaFree(b->dG_all);
   if (b->dS_all) cudaFree(b->dS_all);
@@ -1756,8 +1761,7 @@ int qsf::batch_add_nowait(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int
   if (!b || !g || !d || !slot) return fail(QSF_EINVAL, "null argument");
   if (d->substeps > 1) return fail(QSF_EINVAL, "batched solves run plain Strang steps (substeps <= 1)");
   if (!g->ks) return fail(QSF_EINVAL, "batched grids need a line length with fused kernels in this build");
-  for (auto& kv : b->members)
-    if (kv.second.g == g) return fail(QSF_ESTATE, "grid is already in the batch");
+  if (g->batch) return fail(QSF_ESTATE, "grid is already in a batch");
   BatchMember mb;
   mb.g = g;
   qsf_step_desc dd = *d;
@@ -1771,6 +1775,8 @@ int qsf::batch_add_nowait(qsf_batch* b, qsf_grid* g, const qsf_step_desc* d, int
   *slot = b->next_slot++;
   b->members[*slot] = mb;
   b->dirty = true;
+  g->batch = b;
+  g->batch_slot = *slot;
   return QSF_OK;
 }
 
@@ -1786,6 +1792,8 @@ int qsf_batch_remove(qsf_batch* b, int64_t slot) {
     QSF_CU(cudaGetLastError());
   }
   QSF_CU(cudaStreamSynchronize(b->stream));
+  mb.g->batch = nullptr;
+  mb.g->batch_slot = -1;
   b->members.erase(it);
   b->dirty = true;
   return QSF_OK;

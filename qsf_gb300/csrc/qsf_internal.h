@@ -67,6 +67,10 @@ struct qsf_grid {
   const KernelSet* ks = nullptr;  // kernels for this grid's line length
   GridDev* dG = nullptr;          // device copy of G (step kernels read descriptors from device arrays)
   StepDev* dS = nullptr;          // device copy of the current step descriptor
+  // the batch this grid is a member of (qsf_batch_add) and its slot there: destroying
+  // the grid removes it from that batch first (the batch's graph reads its memory)
+  qsf_batch* batch = nullptr;
+  int64_t batch_slot = -1;
   // static tables
   longlong2* xs = nullptr;
   long long* Vx = nullptr;

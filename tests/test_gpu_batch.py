@@ -54,3 +54,42 @@ def test_batch_matches_alone():
         assert done == len(sched)
         assert np.array_equal(rows_a, rows_b)
         assert np.array_equal(psi_a, g.download())
+
+
+def test_destroying_a_member_takes_it_out_of_its_batch():
+    """qsf_grid_destroy of a batch member removes it from the batch first: the batch's
+    next run leaves its memory alone, the other members finish as they would alone, and
+    the destroyed member's slot is gone.  A grid is in one batch at a time; destroying
+    a batch leaves its grids free to join another."""
+    import qsf_gb300 as Q
+    (g1, p1, s1, kw1), (g2, p2, s2, kw2) = [_solve(Q, *sp) for sp in
+                                            [(2, 48, Q.GAUGE_VELOCITY, 0.1, 1.3, 1), (2, 64, Q.GAUGE_LENGTH, 0.08, 1.1, 2)]]
+    rows_a, _ = g2.step(Q.MODE_RE, 0.05, len(s2), s2, **kw2)
+    rows_a, psi_a = rows_a.copy(), g2.download()
+    g2.upload(p2)
+    b = Q.Batch()
+    slot1 = b.add(g1, Q.MODE_RE, 0.05, len(s1), s1, **kw1)
+    slot2 = b.add(g2, Q.MODE_RE, 0.05, len(s2), s2, **kw2)
+    assert b.run(5) == 2
+    g1.close()
+    with pytest.raises(Q.QsfError):
+        b.result(slot1)
+    active = 1
+    while active:
+        active = b.run(37)
+    rows_b, done = b.result(slot2)
+    assert done == len(s2)
+    assert np.array_equal(rows_a, rows_b)
+    assert np.array_equal(psi_a, g2.download())
+    b2 = Q.Batch()
+    with pytest.raises(Q.QsfError):
+        b2.add(g2, Q.MODE_RE, 0.05, len(s2), s2, **kw2)
+    b.close()
+    g2.upload(p2)
+    slot = b2.add(g2, Q.MODE_RE, 0.05, len(s2), s2, **kw2)
+    while b2.run(64):
+        pass
+    rows_c, done = b2.result(slot)
+    assert done == len(s2) and np.array_equal(rows_a, rows_c)
+    b2.close()
+    g2.close()
