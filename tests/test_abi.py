@@ -42,3 +42,12 @@ def test_fft_plans(lib):
     assert Q.fft_radices(640) == [16, 8, 5]
     with pytest.raises(Q.QsfError):
         Q.fft_radices(7 * 64)
+
+
+def test_status_names_match_the_header():
+    """The binding's names of the QSF_E* status codes are the header's."""
+    import re
+    from qsf_gb300 import _lib
+    codes = {int(v): k for k, v in re.findall(r"#define QSF_(E[A-Z]+)\s+(\d+)", open(HEADER).read())}
+    assert codes and codes == _lib.ERRORS
+    assert re.search(r"#define QSF_OK 0\b", open(HEADER).read()) and _lib.QSF_OK == 0
