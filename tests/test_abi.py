@@ -51,3 +51,34 @@ def test_status_names_match_the_header():
     codes = {int(v): k for k, v in re.findall(r"#define QSF_(E[A-Z]+)\s+(\d+)", open(HEADER).read())}
     assert codes and codes == _lib.ERRORS
     assert re.search(r"#define QSF_OK 0\b", open(HEADER).read()) and _lib.QSF_OK == 0
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes mirror of a header struct has the C compiler's size and field
+    offsets (a probe program compiled against include/qsf_gpu.h prints them)."""
+    import shutil
+    import subprocess
+    from qsf_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    pairs = {"qsf_grid_desc": _lib.GridDesc, "qsf_step_desc": _lib.StepDesc, "qsf_request": _lib.Request,
+             "qsf_result": _lib.Result, "qsf_server_config": _lib.ServerConfig,
+             "qsf_server_stats": _lib.ServerStats, "qsf_dump_format": _lib.DumpFormat}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qsf_gpu.h"', "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            # a trailing underscore in Python stands for a C name that is a Python keyword
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname.rstrip("_")}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(ln.split()[:2]): int(ln.split()[2]) for ln in out if ln.strip()}
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
