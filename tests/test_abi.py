@@ -82,3 +82,13 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_kernel_kinds_match_the_header():
+    """qsf_step's per-kernel timing slots (QSF_K_*) in the binding's order."""
+    import re
+    from qsf_gb300 import _lib
+    kinds = dict(re.findall(r"#define QSF_K_([A-Z_]+)\s+(\d+)", open(HEADER).read()))
+    count = int(kinds.pop("COUNT"))
+    order = [k.lower() for k, _ in sorted(kinds.items(), key=lambda kv: int(kv[1]))]
+    assert order == _lib.KERNEL_KINDS and count == len(order)
