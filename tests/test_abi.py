@@ -92,3 +92,20 @@ def test_kernel_kinds_match_the_header():
     count = int(kinds.pop("COUNT"))
     order = [k.lower() for k, _ in sorted(kinds.items(), key=lambda kv: int(kv[1]))]
     assert order == _lib.KERNEL_KINDS and count == len(order)
+
+
+def test_python_constants_match_the_header():
+    """Every QSF_<NAME> integer the package also exports as <NAME> (modes,
+    representations, potentials, gauges, observables, operators, absorbers) and every
+    border type QSF_B_<NAME> (BORDERS) has the header's value."""
+    import re
+    import qsf_gb300 as Q
+    from qsf_gb300 import _lib
+    defs = {k: int(v) for k, v in re.findall(r"#define QSF_([A-Z0-9_]+)\s+(\d+)u?\b", open(HEADER).read())}
+    shared = [k for k in defs if hasattr(Q, k)]
+    assert len(shared) >= 15, shared
+    for k in shared:
+        assert getattr(Q, k) == defs[k], k
+    borders = {k[2:]: v for k, v in defs.items() if k.startswith("B_")}
+    assert borders == Q.BORDERS
+    assert defs["MAX_BORDERS"] == _lib.MAX_BORDERS
