@@ -9,6 +9,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <initializer_list>
 
 namespace qsf {
 
